@@ -1,0 +1,377 @@
+"""Benchmark of the GB300 TemGymCore hot path.
+
+Headline workload (one step): the 4D-STEM shadow-image batch - a 64 x 64 scan
+(step 1e-9 m, random rotation), one 1,024-ray point-source bundle per probe
+(4,194,304 ray traces), descan matrix I + N(0, 1e-3), camera length 0.1 m,
+per-probe dense 256 x 256 int32 detector images (1.07 GB written per step).
+Metric: ray-component steps per second (rays x components, forward trace +
+binning), whole job.  The working set (1.07 GB of images) exceeds the 129 MB
+L2, so no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Under torchrun (N > 1) every rank runs its own scan (weak scaling: probes
+are independent, there is no data-path collective); rank 0 prints the line.
+``--impl reference`` times the CPU restatement of the reference's per-probe
+loop (run_to_end + into_image) on all host cores, same metric and config.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "fwd+grad ray·component steps/s; field beam·px/s at stated err vs FP64 oracle"
+UNIT = "ray·component steps/s"
+SCAN = (64, 64)
+RAYS = 1024
+N_COMPONENTS = 5  # PointSource, ScanGrid, Scanner, Descanner, Detector
+FALLBACK_HBM_GBS = 6800.0
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            p = json.load(fh)
+        return float(p["hbm_gbs"]), float(p.get("bf16_tflops", 1900.0)), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, 1900.0, "fallback"
+
+
+def _traffic(name):
+    """Per-launch DRAM bytes of a kernel from the committed ncu summary."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as fh:
+            return json.load(fh).get(name)
+    except Exception:
+        return None
+
+
+class Clocks:
+    """nvidia-smi sampler running during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "50"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.p = None
+        time.sleep(0.15)
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.p is not None:
+            time.sleep(0.1)
+            self.p.terminate()
+            try:
+                self.out, _ = self.p.communicate(timeout=5)
+            except Exception:
+                self.p.kill()
+
+    def summary(self):
+        rows = []
+        for line in (self.out or "").strip().splitlines():
+            f = [v.strip() for v in line.split(",")]
+            if len(f) >= 7:
+                try:
+                    rows.append((float(f[0]), float(f[1]), f[2:]))
+                except ValueError:
+                    pass
+        if not rows:
+            return None
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        reasons = set()
+        for _, _, fl in rows:
+            for nm, v in zip(names[1:], fl[1:]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+# ------------------------------------------------------------------ helpers
+
+def _setup_dist(args):
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "gb300" else "gloo"
+        if args.impl == "gb300":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    elif args.impl == "gb300":
+        torch.cuda.set_device(0)
+    return world, rank, local
+
+
+def _barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def _max_over_ranks(v, world):
+    if world <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    dev = torch.device("cuda", torch.cuda.current_device()) if torch.cuda.is_available() else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _workload():
+    from temgymcore_gb300.workloads import stem_4d
+    return stem_4d(seed=0, scan=SCAN, rays_per_probe=RAYS)
+
+
+# ------------------------------------------------------------ CPU baseline
+
+def _cpu_probe_chunk(args):
+    """Reference loop restated (oracle): run_to_end + metres_to_pixels +
+    into_image per probe.  Returns elapsed seconds for ``probes``."""
+    sys.path.insert(0, ROOT)
+    import oracle
+    from oracle.rays import ORay
+    from temgymcore_gb300.workloads import stem_4d, stem_probe_model
+    probes, = args
+    w = stem_4d(seed=0, scan=SCAN, rays_per_probe=RAYS)
+    g = {k: w["detector"][k] for k in ("pixel_size", "shape")}
+    sg = {k: w["scangrid"][k] for k in ("pixel_size", "shape", "rotation")}
+    t0 = time.perf_counter()
+    for p in probes:
+        r, c = divmod(int(p), SCAN[1])
+        spx, spy = oracle.pixels_to_metres(sg, r, c)
+        spec = stem_probe_model(w, float(spx), float(spy))
+        out = oracle.run_to_end(ORay(w["x"].astype(np.float64), w["y"].astype(np.float64),
+                                     w["dx"].astype(np.float64), w["dy"].astype(np.float64),
+                                     0.0, 0.0), spec)
+        py, px = oracle.metres_to_pixels(g, out.x, out.y)
+        oracle.into_image(g, py, px)
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(sample_probes=SCAN[0] * SCAN[1]):
+    """Single-core oracle timing on a bounded sample (rank 0, N=1 only)."""
+    el = _cpu_probe_chunk((list(range(sample_probes)),))
+    v = sample_probes * RAYS * N_COMPONENTS / el
+    return {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{sample_probes} of {SCAN[0] * SCAN[1]} probes x {RAYS} rays, NumPy float64 "
+                      "restatement of run_to_end + metres_to_pixels + into_image per probe, 1 thread"}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    cores = os.cpu_count() or 1
+    # size each step so the whole --steps/--warmup run stays near a minute
+    t_probe = _cpu_probe_chunk((list(range(8)),)) / 8
+    per_worker = int(min(SCAN[0] * SCAN[1] // cores, max(1, 60.0 / (args.steps + args.warmup)
+                                                          / max(t_probe, 1e-6))))
+    per_step = per_worker * cores  # a bounded sample of the 4096-probe scan
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        def step():
+            chunks = [(list(range(i * per_worker, (i + 1) * per_worker)),) for i in range(cores)]
+            t0 = time.perf_counter()
+            pool.map(_cpu_probe_chunk, chunks)
+            return time.perf_counter() - t0
+        for _ in range(args.warmup):
+            step()
+        times = [step() for _ in range(args.steps)]
+    t = sum(times)
+    v = args.steps * per_step * RAYS * N_COMPONENTS / t
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded), no dataset",
+            "config": {"workload": "4D-STEM shadow images, 64x64 scan x 1024 rays, 256x256 detector",
+                       "sample_per_step": f"{per_step} probes"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{per_step} of 4096 probes per step, {cores} spawn workers"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------- GPU arm
+
+def _events(torch):
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def secondary_plain(torch, dev):
+    """Plain paraxial trace, 65,536 rays: fused trace + pixels + histogram."""
+    import temgymcore_gb300 as t
+    from temgymcore_gb300.workloads import build_model, plain_trace
+    w = plain_trace(seed=0, n=65536)
+    model = build_model(w["model"])
+    ray = t.Ray(x=torch.tensor(w["x"], device=dev), y=torch.tensor(w["y"], device=dev),
+                dx=torch.tensor(w["dx"], device=dev), dy=torch.tensor(w["dy"], device=dev),
+                z=0.0, pathlength=0.0)
+    acc = torch.zeros((256, 256), dtype=torch.int64, device=dev)
+    for _ in range(5):
+        t.trace_to_image(ray, model, acc=acc)
+    torch.cuda.synchronize()
+    a, b = _events(torch)
+    k = 200
+    a.record()
+    for _ in range(k):
+        t.trace_to_image(ray, model, acc=acc)
+    b.record()
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / k
+    return {"workload": "plain trace 65,536 rays, Lens+Detector 256x256, fused trace+pixels+hist",
+            "ms_per_step": ms, "rays_per_s": 65536 / (ms * 1e-3),
+            "ray_component_steps_per_s": 2 * 65536 / (ms * 1e-3),
+            "note": "launch-latency bound (3.7 MB per step); includes host-side model packing"}
+
+
+def run_gpu(args, world, rank, local):
+    import torch
+
+    import temgymcore_gb300 as t
+    from temgymcore_gb300.workloads import stem_model
+    dev = torch.device("cuda", torch.cuda.current_device())
+    w = _workload()
+    model = stem_model(w)
+    ray = t.Ray(x=torch.tensor(w["x"], device=dev), y=torch.tensor(w["y"], device=dev),
+                dx=torch.tensor(w["dx"], device=dev), dy=torch.tensor(w["dy"], device=dev),
+                z=0.0, pathlength=0.0)
+    n_probes = SCAN[0] * SCAN[1]
+    out = torch.empty((n_probes, 256, 256), dtype=torch.int32, device=dev)
+    for _ in range(args.warmup):
+        t.scan_images(ray, model, out=out)
+    torch.cuda.synchronize()
+    a, b = _events(torch)
+    _barrier(world)
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        a.record()
+        for _ in range(args.steps):
+            t.scan_images(ray, model, out=out)
+        b.record()
+        torch.cuda.synchronize()
+    _barrier(world)
+    ms = a.elapsed_time(b) / args.steps
+    ms = _max_over_ranks(ms, world)
+    units = n_probes * RAYS * N_COMPONENTS
+    value = world * units / (ms * 1e-3)
+    err = t._native.error_word()
+
+    hbm, bf16, peak_src = _peaks()
+    alg_bytes = n_probes * 256 * 256 * 4 + RAYS * 16
+    achieved = alg_bytes / (ms * 1e-3) / 1e9
+    roof = {"kernel": "k_scan_hist", "bound": "hbm", "achieved": achieved, "peak": hbm,
+            "unit": "GB/s", "frac": achieved / hbm, "peak_source": peak_src,
+            "algorithmic_bytes_per_launch": alg_bytes, "traffic": _traffic("k_scan_hist")}
+    if args.headline_only:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+                              "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+                              "scan": list(SCAN), "roofline": roof, "clocks": clk.summary(),
+                              "error_word": err}))
+        return
+
+    # end to end through the public API with host buffers
+    pin_in = torch.empty((4, RAYS), dtype=torch.float32).pin_memory()
+    for i, k in enumerate(("x", "y", "dx", "dy")):
+        pin_in[i] = torch.from_numpy(w[k])
+    pin_out = torch.empty((n_probes, 256, 256), dtype=torch.int32).pin_memory()
+    dev_in = torch.empty((4, RAYS), dtype=torch.float32, device=dev)
+    e2e_steps = max(3, min(args.steps, 20))
+
+    def e2e_step():
+        dev_in.copy_(pin_in, non_blocking=True)
+        r = t.Ray(x=dev_in[0], y=dev_in[1], dx=dev_in[2], dy=dev_in[3], z=0.0, pathlength=0.0)
+        t.scan_images(r, model, out=out)
+        pin_out.copy_(out, non_blocking=True)
+    for _ in range(2):
+        e2e_step()
+    torch.cuda.synchronize()
+    _barrier(world)
+    a2, b2 = _events(torch)
+    a2.record()
+    for _ in range(e2e_steps):
+        e2e_step()
+    b2.record()
+    torch.cuda.synchronize()
+    e2e_ms = _max_over_ranks(a2.elapsed_time(b2) / e2e_steps, world)
+    e2e = {"value": world * units / (e2e_ms * 1e-3), "unit": UNIT,
+           "h2d_bytes_per_step": int(pin_in.numel() * 4), "d2h_bytes_per_step": int(pin_out.numel() * 4),
+           "ms_per_step": e2e_ms, "steps": e2e_steps}
+    del pin_out
+
+    secondary = {}
+    if rank == 0:
+        try:
+            secondary["plain_trace"] = secondary_plain(torch, dev)
+        except Exception as e:  # report, never hide
+            secondary["plain_trace"] = {"error": repr(e)}
+    cpu = cpu_baseline() if (rank == 0 and world == 1) else None
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 rays / f64 binning ties", "data": "synthetic (seeded)",
+            "config": {"workload": "4D-STEM shadow images: 64x64 scan (step 1e-9 m, rotation "
+                                   "U(0,2pi)), 1024-ray point-source bundle per probe, descan I+N(0,1e-3), "
+                                   "camera length 0.1 m, 256x256 int32 images at 5.5e-5 m",
+                       "rays_per_step": n_probes * RAYS, "components": N_COMPONENTS,
+                       "l2": "no flush: 1.07 GB of images written per step > 129 MB L2",
+                       "parallelism": f"dp{world} (independent scans per rank)"},
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps,
+            "clocks": clk.summary(), "error_word": err, "secondary": secondary}
+    if rank == 0:
+        print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--scan", type=int, nargs=2, default=None, metavar=("ROWS", "COLS"),
+                    help="smaller scan for profiling captures (default 64 64)")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="skip the secondary workloads, e2e and CPU baseline")
+    args = ap.parse_args()
+    if args.scan:
+        global SCAN
+        SCAN = tuple(args.scan)
+    world, rank, local = _setup_dist(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_gpu(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,197 @@
+/*
+ * temgym_gb300.h - C ABI of the GB300 (sm_103a) implementation of TemGymCore's
+ * batched paraxial ray propagation and Gaussian-beamlet detector field.
+ *
+ * The reference (temgym_core, pure Python on JAX) has no FFI: its "plugin
+ * API" is Python duck typing.  Each entry point below replaces a Python call
+ * site of the reference (cited per function); the Python package
+ * temgymcore_gb300 binds them with ctypes (see INTEGRATION.md for the
+ * binding a temgym_core maintainer would add).
+ *
+ * Conventions
+ *   - Every function returns an int status: TG_OK (0) or a negative TG_ERR_*.
+ *   - Buffers marked "device" are caller-owned CUDA device pointers; the
+ *     library allocates nothing except where a function says otherwise.
+ *   - `stream` is a cudaStream_t passed as void*; NULL is the legacy stream.
+ *     Calls enqueue work and return without synchronising, so they can be
+ *     captured into a CUDA graph.
+ *   - Kernels never trap: a device-side problem (non-finite coordinate in a
+ *     histogram, bad table entry, exhausted wait) sets bits in a device error
+ *     word, read back with tg_get_error_word().
+ *   - Ray state is float32 structure-of-arrays; pathlength, phases and ABCD
+ *     matrices are float64.
+ */
+#ifndef TEMGYM_GB300_H
+#define TEMGYM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define TG_OK 0
+#define TG_ERR_INVALID (-1)     /* null pointer, bad size, bad enum        */
+#define TG_ERR_UNSUPPORTED (-2) /* component kind / option not supported  */
+#define TG_ERR_ALIGN (-3)       /* pointer alignment requirement violated  */
+#define TG_ERR_CUDA (-4)        /* a CUDA runtime call failed              */
+#define TG_ERR_TOO_LARGE (-5)   /* size beyond a stated maximum            */
+#define TG_ERR_WORKSPACE (-6)   /* caller workspace too small              */
+
+/* device error-word bits (tg_get_error_word) */
+#define TG_EW_NONFINITE 0x1u    /* non-finite coordinate met by a binner   */
+#define TG_EW_TABLE 0x2u        /* out-of-range entry in a packed table    */
+#define TG_EW_TIMEOUT 0x4u      /* a bounded wait gave up                  */
+#define TG_EW_MMA 0x8u          /* tensor-core pipeline wait gave up       */
+
+/* ---- component kinds (components.py) ---------------------------------- */
+enum tg_kind {
+  TG_PLANE = 0,     /* Plane, Detector, ScanGrid, Source: identity        */
+  TG_LENS = 1,      /* p[0] = focal_length                                 */
+  TG_SCANNER = 2,   /* p[0..3] = scan_pos_x, scan_pos_y, tilt_x, tilt_y     */
+  TG_DESCANNER = 3, /* p[0..3] = scan pos/tilt; p[4..19] = 4x4 matrix M     */
+                    /* (rows x,y,dx,dy; cols spx,spy,stx,sty, row-major);  */
+                    /* p[20..23] = offsets.  Delta = M s + off - s.  The    */
+                    /* reference's 12 coefficients are M[:,0:2] and off    */
+                    /* with M[:,2:4] = 0.                                  */
+  TG_DEFLECTOR = 4, /* p[0..1] = def_x, def_y                              */
+  TG_BIPRISM = 5,   /* p[0] = def_x                                        */
+  TG_ROTATOR = 6,   /* p[0] = angle in degrees                             */
+  TG_THICKLENS = 7, /* z = z_po; p[0] = focal_length; p[1] = z_pi          */
+  TG_APERTURE = 8   /* p[0] = radius; p[1..2] = centre x, y (extension)    */
+};
+
+/* component flag: scan position comes from the probe (tg_scan_*) */
+#define TG_FLAG_PER_PROBE 0x1
+
+typedef struct tg_component {
+  int32_t kind;  /* enum tg_kind */
+  int32_t flags; /* TG_FLAG_* */
+  double z;      /* axial position in metres (ThickLens: z_po) */
+  double p[24];  /* kind-specific parameters, see enum tg_kind */
+} tg_component;
+
+typedef struct tg_model {
+  int32_t n_components;            /* <= TG_MAX_COMPONENTS */
+  const tg_component *components;  /* host pointer */
+} tg_model;
+
+#define TG_MAX_COMPONENTS 60
+
+/* Structure-of-arrays rays (ray.py:8-45).  x, y, dx, dy: device float32 of
+ * length n.  z and pathlength: device float64 arrays, or NULL to use the
+ * uniform *_scalar value.  amplitude: optional device float32 (NULL = none).
+ */
+typedef struct tg_rays {
+  int64_t n;
+  float *x, *y, *dx, *dy;
+  double *z;
+  double z_scalar;
+  double *pathlength;
+  double pl_scalar;
+  float *amplitude;
+} tg_rays;
+
+/* Detector pixel map (grid.py:51-63,120-153).  m is the first two rows of
+ * the float64 metres->pixels matrix; py = (m[0]*y + m[1]*x) + m[2],
+ * px = (m[3]*y + m[4]*x) + m[5], rounded half-to-even to int32. */
+typedef struct tg_grid {
+  int32_t h, w;
+  double m[6];
+} tg_grid;
+
+/* ---- library --------------------------------------------------------- */
+/* Version string of this library. */
+const char *tg_version(void);
+/* Human-readable text for a status code. */
+const char *tg_status_string(int status);
+/* Read (and optionally clear) the device error word of the current device;
+ * synchronises the device. */
+int tg_get_error_word(uint32_t *out, int clear);
+
+/* ---- ray chain -------------------------------------------------------- */
+/*
+ * tg_trace_fwd - fused forward trace (+ optional pixel binning + histogram).
+ * Replaces run.py:85-116 run_to_end (with run_iter's always-inserted
+ * propagator, run.py:75-82), followed optionally by grid.py:120-153
+ * Detector.metres_to_pixels and grid.py:231-280 Detector.into_image.
+ *   out:   output rays (x, y, dx, dy float32; pathlength float64 if non-NULL;
+ *          amplitude if both in/out amplitude non-NULL).  Output z is
+ *          uniform and is returned in *z_out (may be NULL).
+ *   grid:  NULL = no binning.  pix_y/pix_x (device int32, length n) may be
+ *          NULL.  hist (device, grid h*w) may be NULL; hist_i64 selects
+ *          int64 (reference dtype) or int32 counters.  hist is ADDED to.
+ */
+int tg_trace_fwd(const tg_model *model, const tg_rays *in, tg_rays *out,
+                 double *z_out, const tg_grid *grid, int32_t *pix_y,
+                 int32_t *pix_x, void *hist, int32_t hist_i64, void *stream);
+
+/*
+ * tg_bin - metres->pixels + histogram for existing rays (no trace).
+ * Replaces grid.py:120-153 and grid.py:231-280 (+ utils.py:83-114).
+ * mask: optional device uint8 (0 = do not count), may be NULL.
+ */
+int tg_bin(int64_t n, const float *x, const float *y, const uint8_t *mask,
+           const tg_grid *grid, int32_t *pix_y, int32_t *pix_x, void *hist,
+           int32_t hist_i64, void *stream);
+
+/*
+ * tg_abcd_compose - float64 5x5 ABCD about a central ray, composed from the
+ * per-step component matrices (host code, no GPU needed).
+ * Replaces jax.jacobian(run_to_end) + utils.py:7-43 custom_jacobian_matrix
+ * (README.md:224-234) and, with steps != NULL, run.py:150-179 solve_model
+ * (steps receives 2*n_components row-major 5x5 matrices).
+ * central: x, y, dx, dy, z of the central ray (biprism sign depends on it).
+ */
+int tg_abcd_compose(const tg_model *model, const double central[5],
+                    double out[25], double *steps);
+
+/*
+ * tg_trace_vjp - adjoint of tg_trace_fwd (reverse mode, forward state
+ * recomputed per ray, nothing stored between the passes).
+ * Replaces jax.grad / jax.vjp of run_to_end (README.md:113-160,
+ * run.py:182-267 run_with_grads).
+ *   gout:  upstream gradients (x, y, dx, dy float32; pathlength float64 or
+ *          NULL = zero).  gin: gradients w.r.t. the input rays (any of its
+ *          pointers may be NULL; gin->pathlength receives float64).
+ *   raw:   device float64 [n_steps][4], n_steps = 2*n_components, ADDED to:
+ *          per step the ray-summed adjoint quantities from which parameter
+ *          gradients follow ("adjoint").
+ *   workspace: device scratch of tg_trace_vjp_workspace(n) bytes.
+ */
+size_t tg_trace_vjp_workspace(int64_t n, const tg_model *model);
+int tg_trace_vjp(const tg_model *model, const tg_rays *in, const tg_rays *gout,
+                 tg_rays *gin, double *raw, void *workspace, size_t ws_bytes,
+                 void *stream);
+
+/* ---- 4D-STEM scan batch ---------------------------------------------- */
+/* Probe p sits at scan-grid pixel (row, col) = (p / cols, p % cols); its
+ * scan position is y = (t[0]*row + t[1]*col) + t[2], x = (t[3]*row +
+ * t[4]*col) + t[5] (the ScanGrid pixels->metres map, grid.py:155-182), or
+ * positions[2p], positions[2p+1] (x, y; device float64) when non-NULL.
+ * Every Scanner / Descanner flagged TG_FLAG_PER_PROBE takes that position. */
+typedef struct tg_scan {
+  int32_t n_probes;
+  int32_t cols;
+  double t[6];
+  const double *positions;
+} tg_scan;
+
+/*
+ * tg_scan_hist - per-probe detector images of one ray bundle.
+ * Replaces the per-scan-position loop of run.py:85-116 run_to_end followed
+ * by grid.py:231-280 Detector.into_image (one Python call per position in
+ * the reference).
+ *   bundle: rays leaving the source (uniform z), shared by every probe.
+ *   hist:   device int32 [n_probes][h][w], OVERWRITTEN (dense images).
+ *   probe_xy: optional device float32 [n_probes][2][n]: detector x then y.
+ */
+int tg_scan_hist(const tg_model *model, const tg_rays *bundle, const tg_scan *scan,
+                 const tg_grid *grid, int32_t *hist, float *probe_xy, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TEMGYM_GB300_H */

@@ -1,0 +1,250 @@
+// scan.cu - 4D-STEM batch: one ray bundle traced through the model at every
+// scan position (probe), binned into one dense detector image per probe.
+//
+// This replaces the reference's per-scan-position Python loop of
+// run_to_end (run.py:85-116) + Detector.into_image (grid.py:231-280).
+//
+// Kernel layout: a persistent grid walks the probes; one CTA owns one probe
+// at a time.  The CTA
+//   1. derives the probe's scan position (float64, from the ScanGrid pixel
+//      map or an explicit list) and the per-probe Scanner/Descanner shifts,
+//   2. traces the bundle (L2-resident, read by every CTA) in registers and
+//      keeps each ray's packed pixel in shared memory,
+//   3. reduces the hits' bounding box; when it fits the shared-memory window
+//      (the normal case: a probe lights a small disc) it histograms there,
+//   4. streams the whole dense image to HBM once with 16-byte stores
+//      (window counts inside, zeros elsewhere).
+// A probe whose hits do not fit the window, or a bundle larger than the
+// shared ray buffer, takes the slow path: zero-fill, barrier, global atomics.
+// The HBM traffic is therefore the dense histogram write, ~h*w*4 bytes/probe.
+#include <cstring>
+
+#include "tg_common.cuh"
+
+TG_DEFINE_ERROR_WORD(scan)
+
+namespace tg {
+
+constexpr int kScanThreads = 256;
+constexpr int kMaxSmemRays = 4096;  // packed pixels kept in shared memory
+constexpr int kWinBins = 7680;      // shared histogram window (u32 counters);
+                                    // static shared memory stays under 48 KB
+
+struct ScanArgs {
+  int64_t n;  // rays per probe
+  const float *x, *y, *dx, *dy;
+  double z_scalar;
+  int32_t n_probes, cols;
+  double t[6];
+  const double* positions;
+  int32_t* hist;  // [n_probes][h][w]
+  float* probe_xy;  // optional [n_probes][2][n]
+  int32_t h, w;
+  int32_t vec4;  // rows are 16-byte aligned: dense write with int4 stores
+};
+
+__device__ __forceinline__ void probe_shifts(const Program& P, const ScanArgs& A, int p,
+                                             float4* pshift) {
+  double spx, spy;
+  if (A.positions) {
+    spx = A.positions[2 * (size_t)p];
+    spy = A.positions[2 * (size_t)p + 1];
+  } else {
+    double r = (double)(p / A.cols), c = (double)(p % A.cols);
+    spy = __dadd_rn(__dadd_rn(__dmul_rn(A.t[0], r), __dmul_rn(A.t[1], c)), A.t[2]);
+    spx = __dadd_rn(__dadd_rn(__dmul_rn(A.t[3], r), __dmul_rn(A.t[4], c)), A.t[5]);
+  }
+  for (int k = 0; k < P.n_probe_ops; ++k) {
+    const double* q = P.pcoef[k];
+    pshift[k] = make_float4((float)(q[0] * spx + q[1] * spy + q[2]),
+                            (float)(q[3] * spx + q[4] * spy + q[5]),
+                            (float)(q[6] * spx + q[7] * spy + q[8]),
+                            (float)(q[9] * spx + q[10] * spy + q[11]));
+  }
+}
+
+__device__ __forceinline__ void trace_one(const Program& P, const float4* pshift, float x,
+                                          float y, float dx, float dy, double z, RayS& r,
+                                          bool& alive) {
+  r = RayS{x, y, dx, dy, 0.f};
+  double dvar = 0.0;
+  uint64_t sb = 0;
+  alive = true;
+  for (int s = 0; s < P.n_steps; ++s)
+    op_forward(P.op[s], pshift, r, P.zc_first, z, dvar, sb, alive);
+}
+
+__device__ __forceinline__ int block_min(int v, int* red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  int r = red[0];
+  for (int i = 1; i < (int)(blockDim.x >> 5); ++i) r = min(r, red[i]);
+  return r;
+}
+
+__device__ __forceinline__ int block_max(int v, int* red) {
+  return -block_min(-v, red);
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+k_scan_hist(const __grid_constant__ Program P, const __grid_constant__ ScanArgs A,
+            const __grid_constant__ BinCoef B) {
+  __shared__ float4 pshift[kMaxProbeOps];
+  __shared__ uint32_t pix[kMaxSmemRays];  // (py << 16) | px, or 0xffffffff = no hit
+  __shared__ uint32_t win[kWinBins];
+  __shared__ int red[kScanThreads / 32];
+  const int64_t n = A.n;
+  const bool fits = n <= kMaxSmemRays;
+  const int H = A.h, W = A.w;
+  for (int p = blockIdx.x; p < A.n_probes; p += gridDim.x) {
+    if (threadIdx.x == 0) probe_shifts(P, A, p, pshift);
+    __syncthreads();
+    int rmin = 0x7fffffff, rmax = -1, cmin = 0x7fffffff, cmax = -1;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+      RayS r;
+      bool alive;
+      trace_one(P, pshift, A.x[i], A.y[i], A.dx[i], A.dy[i], A.z_scalar, r, alive);
+      if (A.probe_xy) {
+        A.probe_xy[(size_t)p * 2 * n + i] = r.x;
+        A.probe_xy[(size_t)p * 2 * n + n + i] = r.y;
+      }
+      int py, px;
+      bin_yx(r.x, r.y, B, py, px);
+      bool ok = alive && py >= 0 && py < H && px >= 0 && px < W;
+      if (!(isfinite(r.x) && isfinite(r.y))) atomicOr(&g_tg_err, TG_EW_NONFINITE);
+      if (fits) pix[i] = ok ? ((uint32_t)py << 16) | (uint32_t)px : 0xffffffffu;
+      if (ok) {
+        rmin = min(rmin, py); rmax = max(rmax, py);
+        cmin = min(cmin, px); cmax = max(cmax, px);
+      }
+    }
+    rmin = block_min(rmin, red);
+    rmax = block_max(rmax, red);
+    cmin = block_min(cmin, red);
+    cmax = block_max(cmax, red);
+    int32_t* img = A.hist + (size_t)p * H * W;
+    const int wr = rmax - rmin + 1, wc = cmax - cmin + 1;
+    const bool any = rmax >= 0;
+    const bool windowed = fits && (!any || (int64_t)wr * wc <= kWinBins);
+    if (windowed) {
+      if (any) {
+        for (int i = threadIdx.x; i < wr * wc; i += blockDim.x) win[i] = 0u;
+        __syncthreads();
+        for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+          uint32_t v = pix[i];
+          if (v != 0xffffffffu) {
+            int py = (int)(v >> 16), px = (int)(v & 0xffffu);
+            atomicAdd(&win[(py - rmin) * wc + (px - cmin)], 1u);
+          }
+        }
+        __syncthreads();
+      }
+      // dense write of the whole image: window counts inside, zeros outside
+      if (A.vec4) {
+        const int w4 = W >> 2;
+        const int total = H * w4;
+        for (int i = threadIdx.x; i < total; i += blockDim.x) {
+          const int row = i / w4, c0 = (i - row * w4) << 2;
+          int4 v = make_int4(0, 0, 0, 0);
+          if (any && row >= rmin && row <= rmax && c0 + 3 >= cmin && c0 <= cmax) {
+            const uint32_t* wrow = win + (row - rmin) * wc;
+            int c = c0;
+            v.x = (c >= cmin && c <= cmax) ? (int)wrow[c - cmin] : 0; ++c;
+            v.y = (c >= cmin && c <= cmax) ? (int)wrow[c - cmin] : 0; ++c;
+            v.z = (c >= cmin && c <= cmax) ? (int)wrow[c - cmin] : 0; ++c;
+            v.w = (c >= cmin && c <= cmax) ? (int)wrow[c - cmin] : 0;
+          }
+          __stcs(reinterpret_cast<int4*>(img) + i, v);
+        }
+      } else {
+        for (int i = threadIdx.x; i < H * W; i += blockDim.x) {
+          const int row = i / W, c = i - row * W;
+          int v = 0;
+          if (any && row >= rmin && row <= rmax && c >= cmin && c <= cmax)
+            v = (int)win[(row - rmin) * wc + (c - cmin)];
+          __stcs(img + i, v);
+        }
+      }
+    } else {
+      // slow path: zero the image, then global atomics (re-trace if needed)
+      for (int i = threadIdx.x; i < H * W; i += blockDim.x) img[i] = 0;
+      __syncthreads();
+      for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        int py, px;
+        bool ok;
+        if (fits) {
+          uint32_t v = pix[i];
+          ok = v != 0xffffffffu;
+          py = (int)(v >> 16);
+          px = (int)(v & 0xffffu);
+        } else {
+          RayS r;
+          bool alive;
+          trace_one(P, pshift, A.x[i], A.y[i], A.dx[i], A.dy[i], A.z_scalar, r, alive);
+          bin_yx(r.x, r.y, B, py, px);
+          ok = alive && py >= 0 && py < H && px >= 0 && px < W;
+        }
+        if (ok) atomicAdd(img + py * W + px, 1);
+      }
+    }
+    __syncthreads();  // shared buffers are reused by the next probe
+  }
+}
+
+static int sm_count_scan() {
+  static int cached = 0;
+  if (!cached) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&cached, cudaDevAttrMultiProcessorCount, dev);
+    if (cached <= 0) cached = 148;
+  }
+  return cached;
+}
+
+}  // namespace tg
+
+using namespace tg;
+
+extern "C" int tg_scan_hist(const tg_model* model, const tg_rays* bundle, const tg_scan* scan,
+                            const tg_grid* grid, int32_t* hist, float* probe_xy, void* stream) {
+  if (!model || !bundle || !scan || !grid) return TG_ERR_INVALID;
+  if (!hist && scan->n_probes > 0) return TG_ERR_INVALID;
+  if (bundle->n < 0 || scan->n_probes < 0 || grid->h <= 0 || grid->w <= 0) return TG_ERR_INVALID;
+  if (grid->h > 65535 || grid->w > 65535) return TG_ERR_TOO_LARGE;
+  if (!scan->positions && scan->cols <= 0) return TG_ERR_INVALID;
+  if (bundle->z) return TG_ERR_UNSUPPORTED;  // one source plane for the bundle
+  if (bundle->n > 0 && (!bundle->x || !bundle->y || !bundle->dx || !bundle->dy))
+    return TG_ERR_INVALID;
+  Program P;
+  int st = compile_program(model, false, bundle->z_scalar, &P);
+  if (st != TG_OK) return st;
+  if (scan->n_probes == 0) return TG_OK;
+  ScanArgs A;
+  std::memset(&A, 0, sizeof(A));
+  A.n = bundle->n;
+  A.x = bundle->x; A.y = bundle->y; A.dx = bundle->dx; A.dy = bundle->dy;
+  A.z_scalar = bundle->z_scalar;
+  A.n_probes = scan->n_probes;
+  A.cols = scan->cols;
+  for (int i = 0; i < 6; ++i) A.t[i] = scan->t[i];
+  A.positions = scan->positions;
+  A.hist = hist;
+  A.probe_xy = probe_xy;
+  A.h = grid->h;
+  A.w = grid->w;
+  A.vec4 = ((grid->w & 3) == 0) && ((reinterpret_cast<uintptr_t>(hist) & 15) == 0);
+  BinCoef B = make_bincoef(grid);
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scan_hist, kScanThreads, 0);
+  if (per_sm < 1) per_sm = 1;
+  int blocks = sm_count_scan() * per_sm;
+  if (blocks > scan->n_probes) blocks = scan->n_probes;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  k_scan_hist<<<blocks, kScanThreads, 0, s>>>(P, A, B);
+  return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
+}

@@ -1,0 +1,223 @@
+// tg_common.cuh - shared definitions of the sm_103a ray-chain kernels.
+//
+// A model (list of tg_component, host float64) is compiled on the host into
+// a Program: a flat list of steps.  Every component contributes two steps,
+// in the order of run.py:75-82: a free-space propagator over
+// (component.z - ray.z), then the component itself.  Because all rays share
+// the same z after the first propagator, every propagation distance after the
+// first is uniform; the compiler resolves them in float64 on the host and the
+// device applies them in float32.  The uniform part of the pathlength
+// (sum of distances) is accumulated on the host in float64; the per-ray part
+// (lens / deflector / biprism terms) is accumulated on the device in float32
+// and added to the float64 pathlength once per ray.
+//
+// The Program travels as a __grid_constant__ kernel parameter (constant
+// bank), so every thread reads the same step descriptor with a broadcast.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/temgym_gb300.h"
+
+namespace tg {
+
+enum OpKind : int32_t {
+  OP_NOP = 0,
+  OP_FREE = 1,       // c0 = d
+  OP_FREE_VARZ = 2,  // first propagator with per-ray z: d_i = zc - z_i
+  OP_LENS = 3,       // c0 = 1/f, c1 = 1/(2f)
+  OP_SHIFT = 4,      // c0..c3 = dx, dy, ddx, ddy (scanner / descanner)
+  OP_DEFLECT = 5,    // c0, c1 = def_x, def_y; pl += dx*x + dy*y (incoming)
+  OP_BIPRISM = 6,    // c0 = def_x;   dx += def_x*sign(x); pl += dx*x + dy*y
+  OP_ROTATE = 7,     // c0 = cos, c1 = sin
+  OP_APERTURE = 8,   // c0 = r^2, c1 = cx, c2 = cy
+  OP_PROBE_SHIFT = 9 // per-probe shift: Delta = K (4x2) sp + k0 (float64 in pcoef)
+};
+
+struct Op {
+  int32_t kind;
+  int32_t aux;   // OP_PROBE_SHIFT: index into Program::pcoef; OP_BIPRISM: sign-bit slot
+  float c[6];
+};
+
+constexpr int kMaxSteps = 2 * TG_MAX_COMPONENTS;
+constexpr int kMaxProbeOps = 8;
+
+struct Program {
+  int32_t n_steps;
+  int32_t n_biprism;
+  int32_t has_aperture;
+  int32_t n_probe_ops;
+  double zc_first;    // z of the first component (OP_FREE_VARZ)
+  double pl_const;    // float64 sum of the uniform distances
+  double z_out;       // uniform output z
+  double pcoef[kMaxProbeOps][12];  // per-probe shift: rows (x,y,dx,dy) x (spx, spy, 1)
+  Op op[kMaxSteps];
+  double dstep[kMaxSteps];  // float64 distance of each propagator step (0 elsewhere)
+  int32_t comp_kind[kMaxSteps];  // tg_kind of the component behind each step (-1 = propagator)
+};
+
+// Host-side compilation (model.cpp).  per_ray_z: input z is a per-ray array.
+int compile_program(const tg_model* model, bool per_ray_z, double z_scalar,
+                    Program* prog);
+
+// Device error word: one per translation unit; tg_get_error_word ORs them.
+#define TG_DEFINE_ERROR_WORD(tu)                                             \
+  static __device__ uint32_t g_tg_err;                                       \
+  extern "C" int tg_internal_err_##tu(uint32_t* out, int clear) {            \
+    uint32_t v = 0;                                                          \
+    if (cudaMemcpyFromSymbol(&v, g_tg_err, sizeof(v)) != cudaSuccess)        \
+      return TG_ERR_CUDA;                                                    \
+    *out |= v;                                                               \
+    if (clear) {                                                             \
+      uint32_t z = 0;                                                        \
+      if (cudaMemcpyToSymbol(g_tg_err, &z, sizeof(z)) != cudaSuccess)        \
+        return TG_ERR_CUDA;                                                  \
+    }                                                                        \
+    return TG_OK;                                                            \
+  }
+
+__device__ __forceinline__ float sgnf(float v) {
+  return v > 0.f ? 1.f : (v < 0.f ? -1.f : 0.f);
+}
+
+// ---------------------------------------------------------------- binning
+// metres -> pixel index, bit-exact with the float64 reference arithmetic
+// ((m0*a + m1*b) + m2, no FMA, rint half-to-even, saturating int32, NaN->0).
+// Fast path: float32 evaluation with a rigorous error bound; a value whose
+// distance to the nearest half-integer is within the bound (or that is
+// large / non-finite) is recomputed exactly in float64.  Ties are therefore
+// decided by the float64 path, so the result equals the float64 result.
+struct BinCoef {
+  float f[6];
+  double d[6];
+};
+
+__device__ __forceinline__ int bin_exact64(double a, double b, double m0,
+                                           double m1, double m2) {
+  double v = __dadd_rn(__dadd_rn(__dmul_rn(m0, a), __dmul_rn(m1, b)), m2);
+  return __double2int_rn(v);  // cvt.rni.s32.f64: saturating, NaN -> 0
+}
+
+__device__ __forceinline__ int bin_one(float a, float b, float m0, float m1,
+                                       float m2, double d0, double d1,
+                                       double d2) {
+  float p0 = m0 * a, p1 = m1 * b;
+  float v = (p0 + p1) + m2;
+  float s = fabsf(p0) + fabsf(p1) + fabsf(m2);
+  // |v - exact| <= ~5 * 2^-24 * s; use 2^-19 * s (16x margin) + denormal guard
+  float bound = s * 1.9073486e-06f + 1e-30f;
+  float fl = floorf(v);
+  float dist = fabsf((v - fl) - 0.5f);
+  bool ok = (fabsf(v) < 4194304.f) && (dist > bound);  // |v| < 2^22, finite
+  if (ok) return __float2int_rn(v);
+  return bin_exact64((double)a, (double)b, d0, d1, d2);
+}
+
+__device__ __forceinline__ void bin_yx(float x, float y, const BinCoef& bc,
+                                       int& py, int& px) {
+  py = bin_one(y, x, bc.f[0], bc.f[1], bc.f[2], bc.d[0], bc.d[1], bc.d[2]);
+  px = bin_one(y, x, bc.f[3], bc.f[4], bc.f[5], bc.d[3], bc.d[4], bc.d[5]);
+}
+
+inline BinCoef make_bincoef(const tg_grid* g) {
+  BinCoef b;
+  for (int i = 0; i < 6; ++i) {
+    b.d[i] = g->m[i];
+    b.f[i] = (float)g->m[i];
+  }
+  return b;
+}
+
+// Warp-aggregated histogram increment: lanes hitting the same bin combine
+// into one atomic issued by the lowest lane (all 32 lanes must call).
+template <typename CountT>
+__device__ __forceinline__ void hist_add_warp(CountT* hist, int bin, bool valid) {
+  unsigned key = valid ? (unsigned)bin : 0xffffffffu;
+  unsigned peers = __match_any_sync(0xffffffffu, key);
+  int lane = threadIdx.x & 31;
+  if (valid && lane == (__ffs(peers) - 1)) {
+    unsigned cnt = __popc(peers);
+    if constexpr (sizeof(CountT) == 8)
+      atomicAdd(reinterpret_cast<unsigned long long*>(hist) + bin,
+                (unsigned long long)cnt);
+    else
+      atomicAdd(reinterpret_cast<unsigned int*>(hist) + bin, cnt);
+  }
+}
+
+// ---------------------------------------------------------------- ray ops
+struct RayS {
+  float x, y, dx, dy, plv;  // plv: per-ray (varying) pathlength part
+};
+
+// Apply one forward step.  zi is the ray's input z (OP_FREE_VARZ only);
+// pshift holds the current probe's shifts (OP_PROBE_SHIFT only);
+// dvar receives that per-ray float64 distance.  sbits records biprism signs
+// (2 bits per biprism: 1 = +, 2 = -) and alive is cleared by apertures.
+__device__ __forceinline__ void op_forward(const Op& op, const float4* pshift,
+                                           RayS& r, double zc, double zi,
+                                           double& dvar, uint64_t& sbits,
+                                           bool& alive) {
+  switch (op.kind) {
+    case OP_FREE: {
+      float d = op.c[0];
+      r.x = fmaf(r.dx, d, r.x);
+      r.y = fmaf(r.dy, d, r.y);
+    } break;
+    case OP_FREE_VARZ: {
+      double dd = zc - zi;
+      dvar = dd;
+      float d = (float)dd;
+      r.x = fmaf(r.dx, d, r.x);
+      r.y = fmaf(r.dy, d, r.y);
+    } break;
+    case OP_LENS: {
+      float x = r.x, y = r.y;
+      r.plv -= (x * x + y * y) * op.c[1];
+      r.dx = fmaf(-x, op.c[0], r.dx);
+      r.dy = fmaf(-y, op.c[0], r.dy);
+    } break;
+    case OP_SHIFT:
+      r.x += op.c[0];
+      r.y += op.c[1];
+      r.dx += op.c[2];
+      r.dy += op.c[3];
+      break;
+    case OP_PROBE_SHIFT: {  // per-probe constants staged in shared memory
+      float4 s = pshift[op.aux];
+      r.x += s.x;
+      r.y += s.y;
+      r.dx += s.z;
+      r.dy += s.w;
+    } break;
+    case OP_DEFLECT: {
+      r.plv += r.dx * r.x + r.dy * r.y;
+      r.dx += op.c[0];
+      r.dy += op.c[1];
+    } break;
+    case OP_BIPRISM: {
+      r.plv += r.dx * r.x + r.dy * r.y;
+      float s = sgnf(r.x);
+      sbits |= (uint64_t)(s > 0.f ? 1u : (s < 0.f ? 2u : 0u)) << (2 * op.aux);
+      r.dx = fmaf(op.c[0], s, r.dx);
+    } break;
+    case OP_ROTATE: {
+      float c = op.c[0], s = op.c[1];
+      float x = r.x, y = r.y, dx = r.dx, dy = r.dy;
+      r.x = x * c - y * s;
+      r.y = x * s + y * c;
+      r.dx = dx * c - dy * s;
+      r.dy = dx * s + dy * c;
+    } break;
+    case OP_APERTURE: {
+      float ex = r.x - op.c[1], ey = r.y - op.c[2];
+      if (!(ex * ex + ey * ey < op.c[0])) alive = false;
+    } break;
+    default:
+      break;
+  }
+}
+
+}  // namespace tg

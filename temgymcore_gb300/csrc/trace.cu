@@ -1,0 +1,543 @@
+// trace.cu - fused forward ray chain (+ binning + histogram), standalone
+// binning, and the recompute-based adjoint.
+//
+// One kernel pass reads each ray once (x, y, dx, dy as float4 vectors of four
+// consecutive rays per thread), runs the whole component chain in registers,
+// and writes the outputs once.  The float64 work per ray is one add for the
+// pathlength and, for the rare coordinates near a pixel-rounding tie, one
+// exact float64 binning evaluation (see tg_common.cuh).
+#include <cstring>
+
+#include "tg_common.cuh"
+
+TG_DEFINE_ERROR_WORD(trace)
+
+namespace tg {
+
+struct FwdArgs {
+  int64_t n;
+  const float *x, *y, *dx, *dy;
+  const double* z;
+  double z_scalar;
+  const double* pl;
+  double pl_scalar;
+  const float* amp;
+  float *ox, *oy, *odx, *ody;
+  double* opl;
+  double* oz;
+  float* oamp;
+  int32_t *pix_y, *pix_x;
+  void* hist;
+  int32_t h, w;
+  int32_t do_bin;
+};
+
+template <int R>
+__device__ __forceinline__ void load4(const float* __restrict__ p, int64_t i0,
+                                      int64_t n, float v[R], bool vec) {
+  if (R == 4 && vec) {
+    float4 t = __ldg(reinterpret_cast<const float4*>(p + i0));
+    v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+  } else {
+#pragma unroll
+    for (int k = 0; k < R; ++k) v[k] = (i0 + k < n) ? __ldg(p + i0 + k) : 0.f;
+  }
+}
+
+template <int R>
+__device__ __forceinline__ void store4(float* __restrict__ p, int64_t i0,
+                                       int64_t n, const float v[R], bool vec) {
+  if (R == 4 && vec) {
+    *reinterpret_cast<float4*>(p + i0) = make_float4(v[0], v[1], v[2], v[3]);
+  } else {
+#pragma unroll
+    for (int k = 0; k < R; ++k)
+      if (i0 + k < n) p[i0 + k] = v[k];
+  }
+}
+
+template <int R, typename CountT>
+__global__ void __launch_bounds__(256)
+k_trace_fwd(const __grid_constant__ Program P, const __grid_constant__ FwdArgs A,
+            const __grid_constant__ BinCoef B) {
+  const int64_t n = A.n;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x * R;
+  // block-uniform loop: every lane of every warp takes the same trip count,
+  // so warp-collective histogram aggregation below is always legal.
+  for (int64_t blk = (int64_t)blockIdx.x * blockDim.x * R; blk < n; blk += stride) {
+    const int64_t i0 = blk + (int64_t)threadIdx.x * R;
+    const bool vec = (R == 4) && (i0 + 3 < n);
+    float x[R], y[R], dx[R], dy[R];
+    load4<R>(A.x, i0, n, x, vec);
+    load4<R>(A.y, i0, n, y, vec);
+    load4<R>(A.dx, i0, n, dx, vec);
+    load4<R>(A.dy, i0, n, dy, vec);
+    RayS r[R];
+    double zi[R], dvar[R];
+    uint64_t sb[R];
+    bool alive[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+      r[k] = RayS{x[k], y[k], dx[k], dy[k], 0.f};
+      zi[k] = (A.z && i0 + k < n) ? A.z[i0 + k] : A.z_scalar;
+      dvar[k] = 0.0;
+      sb[k] = 0;
+      alive[k] = true;
+    }
+    for (int s = 0; s < P.n_steps; ++s) {
+      const Op op = P.op[s];
+#pragma unroll
+      for (int k = 0; k < R; ++k)
+        op_forward(op, nullptr, r[k], P.zc_first, zi[k], dvar[k], sb[k], alive[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+      x[k] = r[k].x; y[k] = r[k].y; dx[k] = r[k].dx; dy[k] = r[k].dy;
+    }
+    store4<R>(A.ox, i0, n, x, vec);
+    store4<R>(A.oy, i0, n, y, vec);
+    store4<R>(A.odx, i0, n, dx, vec);
+    store4<R>(A.ody, i0, n, dy, vec);
+    if (A.opl) {
+#pragma unroll
+      for (int k = 0; k < R; ++k) {
+        if (i0 + k < n) {
+          double p0 = A.pl ? A.pl[i0 + k] : A.pl_scalar;
+          A.opl[i0 + k] = ((p0 + P.pl_const) + dvar[k]) + (double)r[k].plv;
+        }
+      }
+    }
+    if (A.oz) {
+#pragma unroll
+      for (int k = 0; k < R; ++k)
+        if (i0 + k < n) A.oz[i0 + k] = P.z_out;
+    }
+    if (A.oamp) {
+#pragma unroll
+      for (int k = 0; k < R; ++k)
+        if (i0 + k < n) {
+          float a0 = A.amp ? A.amp[i0 + k] : 1.f;
+          A.oamp[i0 + k] = alive[k] ? a0 : 0.f;
+        }
+    }
+    if (A.do_bin) {
+#pragma unroll
+      for (int k = 0; k < R; ++k) {
+        int py, px;
+        bin_yx(x[k], y[k], B, py, px);
+        const bool inr = (i0 + k < n);
+        if (inr) {
+          if (A.pix_y) A.pix_y[i0 + k] = py;
+          if (A.pix_x) A.pix_x[i0 + k] = px;
+          if (!(isfinite(x[k]) && isfinite(y[k]))) atomicOr(&g_tg_err, TG_EW_NONFINITE);
+        }
+        if (A.hist) {
+          bool ok = inr && alive[k] && py >= 0 && py < A.h && px >= 0 && px < A.w;
+          hist_add_warp<CountT>(reinterpret_cast<CountT*>(A.hist), ok ? py * A.w + px : 0, ok);
+        }
+      }
+    }
+  }
+}
+
+struct BinArgs {
+  int64_t n;
+  const float *x, *y;
+  const uint8_t* mask;
+  int32_t *pix_y, *pix_x;
+  void* hist;
+  int32_t h, w;
+};
+
+template <typename CountT>
+__global__ void __launch_bounds__(256)
+k_bin(const __grid_constant__ BinArgs A, const __grid_constant__ BinCoef B) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t blk = (int64_t)blockIdx.x * blockDim.x; blk < A.n; blk += stride) {
+    const int64_t i = blk + threadIdx.x;
+    const bool inr = i < A.n;
+    float x = inr ? A.x[i] : 0.f, y = inr ? A.y[i] : 0.f;
+    int py, px;
+    bin_yx(x, y, B, py, px);
+    if (inr) {
+      if (A.pix_y) A.pix_y[i] = py;
+      if (A.pix_x) A.pix_x[i] = px;
+      if (!(isfinite(x) && isfinite(y))) atomicOr(&g_tg_err, TG_EW_NONFINITE);
+    }
+    if (A.hist) {
+      bool ok = inr && (!A.mask || A.mask[i]) && py >= 0 && py < A.h && px >= 0 && px < A.w;
+      hist_add_warp<CountT>(reinterpret_cast<CountT*>(A.hist), ok ? py * A.w + px : 0, ok);
+    }
+  }
+}
+
+static int sm_count() {
+  static int cached = 0;
+  if (!cached) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&cached, cudaDevAttrMultiProcessorCount, dev);
+    if (cached <= 0) cached = 148;
+  }
+  return cached;
+}
+
+static inline bool al16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
+}  // namespace tg
+
+using namespace tg;
+
+extern "C" int tg_trace_fwd(const tg_model* model, const tg_rays* in, tg_rays* out,
+                            double* z_out, const tg_grid* grid, int32_t* pix_y,
+                            int32_t* pix_x, void* hist, int32_t hist_i64,
+                            void* stream) {
+  if (!model || !in || !out) return TG_ERR_INVALID;
+  if (in->n < 0) return TG_ERR_INVALID;
+  if (in->n > 0 && (!in->x || !in->y || !in->dx || !in->dy || !out->x || !out->y ||
+                    !out->dx || !out->dy))
+    return TG_ERR_INVALID;
+  if ((pix_y || pix_x || hist) && !grid) return TG_ERR_INVALID;
+  if (grid && (grid->h <= 0 || grid->w <= 0)) return TG_ERR_INVALID;
+  Program P;
+  int st = compile_program(model, in->z != nullptr, in->z_scalar, &P);
+  if (st != TG_OK) return st;
+  if (P.n_probe_ops) return TG_ERR_UNSUPPORTED;  // per-probe models: tg_scan_*
+  if (z_out) *z_out = P.z_out;
+  if (in->n == 0) return TG_OK;
+  FwdArgs A;
+  std::memset(&A, 0, sizeof(A));
+  A.n = in->n;
+  A.x = in->x; A.y = in->y; A.dx = in->dx; A.dy = in->dy;
+  A.z = in->z; A.z_scalar = in->z_scalar;
+  A.pl = in->pathlength; A.pl_scalar = in->pl_scalar;
+  A.amp = in->amplitude;
+  A.ox = out->x; A.oy = out->y; A.odx = out->dx; A.ody = out->dy;
+  A.opl = out->pathlength; A.oz = out->z; A.oamp = out->amplitude;
+  A.pix_y = pix_y; A.pix_x = pix_x; A.hist = hist;
+  A.do_bin = (grid != nullptr) && (pix_y || pix_x || hist);
+  BinCoef B;
+  std::memset(&B, 0, sizeof(B));
+  if (grid) {
+    B = make_bincoef(grid);
+    A.h = grid->h;
+    A.w = grid->w;
+  }
+  bool vec = al16(A.x) && al16(A.y) && al16(A.dx) && al16(A.dy) && al16(A.ox) &&
+             al16(A.oy) && al16(A.odx) && al16(A.ody);
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  const int threads = 256;
+  const int R = vec ? 4 : 1;
+  int64_t blocks_needed = (A.n + (int64_t)threads * R - 1) / ((int64_t)threads * R);
+  int64_t cap = (int64_t)sm_count() * 8;
+  int blocks = (int)(blocks_needed < cap ? blocks_needed : cap);
+  if (vec) {
+    if (hist_i64) k_trace_fwd<4, long long><<<blocks, threads, 0, s>>>(P, A, B);
+    else k_trace_fwd<4, int><<<blocks, threads, 0, s>>>(P, A, B);
+  } else {
+    if (hist_i64) k_trace_fwd<1, long long><<<blocks, threads, 0, s>>>(P, A, B);
+    else k_trace_fwd<1, int><<<blocks, threads, 0, s>>>(P, A, B);
+  }
+  return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
+}
+
+extern "C" int tg_bin(int64_t n, const float* x, const float* y, const uint8_t* mask,
+                      const tg_grid* grid, int32_t* pix_y, int32_t* pix_x, void* hist,
+                      int32_t hist_i64, void* stream) {
+  if (n < 0 || !grid || grid->h <= 0 || grid->w <= 0) return TG_ERR_INVALID;
+  if (n > 0 && (!x || !y)) return TG_ERR_INVALID;
+  if (n == 0) return TG_OK;
+  BinArgs A;
+  A.n = n; A.x = x; A.y = y; A.mask = mask; A.pix_y = pix_y; A.pix_x = pix_x;
+  A.hist = hist; A.h = grid->h; A.w = grid->w;
+  BinCoef B = make_bincoef(grid);
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  int64_t need = (n + 255) / 256;
+  int64_t cap = (int64_t)sm_count() * 8;
+  int blocks = (int)(need < cap ? need : cap);
+  if (hist_i64) k_bin<long long><<<blocks, 256, 0, s>>>(A, B);
+  else k_bin<int><<<blocks, 256, 0, s>>>(A, B);
+  return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
+}
+
+// =====================================================================
+// Adjoint (reverse mode) of the forward chain.
+//
+// Each thread re-runs the forward chain for its rays (keeping only the final
+// state and the biprism sign bits), then walks the steps backwards: it
+// recovers the state entering each step by applying that step's inverse
+// (every step is invertible; biprism signs come from the recorded bits),
+// propagates the adjoint (lambda_x, lambda_y, lambda_dx, lambda_dy,
+// lambda_pl) through the step's transposed Jacobian, and accumulates the
+// step's parameter sensitivities.  Nothing is stored between the passes.
+//
+// Per-step sums (float32 within a warp, float64 across warps and blocks):
+//   propagator : dL/dd
+//   lens       : dL/df
+//   shift      : dL/d(delta x, delta y, delta dx, delta dy)
+//   deflector  : dL/d(def_x, def_y)
+//   biprism    : dL/d(def_x)
+//   rotator    : dL/d(angle in radians)
+// Block partials go to the workspace and are reduced in a fixed order by a
+// second kernel, so results are deterministic run to run.
+// =====================================================================
+namespace tg {
+
+struct VjpArgs {
+  int64_t n;
+  const float *x, *y, *dx, *dy;
+  const double* z;
+  double z_scalar;
+  const float *gx, *gy, *gdx, *gdy;
+  const double* gpl;
+  float *ix, *iy, *idx, *idy;
+  double *ipl, *iz;
+  double* partial;  // [gridDim.x][n_steps][4], NULL: no parameter sums
+};
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ int op_nsums(int kind) {
+  switch (kind) {
+    case OP_FREE: case OP_FREE_VARZ: case OP_LENS: case OP_BIPRISM: case OP_ROTATE: return 1;
+    case OP_DEFLECT: return 2;
+    case OP_SHIFT: case OP_PROBE_SHIFT: return 4;
+    default: return 0;
+  }
+}
+
+struct Adj {
+  float lx, ly, ldx, ldy, lpl;
+};
+
+// Reverse one step: on entry r is the state after the step and a the adjoint
+// after it; on exit both describe the state before it.  c receives the step's
+// parameter sensitivities for this ray.  gz receives dL/dz_in (OP_FREE_VARZ).
+__device__ __forceinline__ void op_reverse(const Op& op, const float4* pshift, RayS& r,
+                                           Adj& a, uint64_t sbits, double dvar,
+                                           float c[4], float& gz) {
+  switch (op.kind) {
+    case OP_FREE:
+    case OP_FREE_VARZ: {
+      float d = (op.kind == OP_FREE) ? op.c[0] : (float)dvar;
+      float g = a.lx * r.dx + a.ly * r.dy + a.lpl;
+      c[0] = g;
+      if (op.kind == OP_FREE_VARZ) gz = -g;
+      r.x = fmaf(-r.dx, d, r.x);
+      r.y = fmaf(-r.dy, d, r.y);
+      a.ldx = fmaf(a.lx, d, a.ldx);
+      a.ldy = fmaf(a.ly, d, a.ldy);
+    } break;
+    case OP_LENS: {
+      float k = op.c[0], h = op.c[1];
+      float x = r.x, y = r.y;
+      r.dx = fmaf(x, k, r.dx);
+      r.dy = fmaf(y, k, r.dy);
+      c[0] = (a.ldx * x + a.ldy * y) * (k * k) + a.lpl * (x * x + y * y) * (k * h);
+      a.lx = a.lx - a.ldx * k - a.lpl * 2.f * x * h;
+      a.ly = a.ly - a.ldy * k - a.lpl * 2.f * y * h;
+    } break;
+    case OP_SHIFT:
+    case OP_PROBE_SHIFT: {
+      float4 s = (op.kind == OP_SHIFT) ? make_float4(op.c[0], op.c[1], op.c[2], op.c[3])
+                                       : pshift[op.aux];
+      r.x -= s.x; r.y -= s.y; r.dx -= s.z; r.dy -= s.w;
+      c[0] = a.lx; c[1] = a.ly; c[2] = a.ldx; c[3] = a.ldy;
+    } break;
+    case OP_DEFLECT: {
+      c[0] = a.ldx;
+      c[1] = a.ldy;
+      r.dx -= op.c[0];
+      r.dy -= op.c[1];
+      a.lx = fmaf(a.lpl, r.dx, a.lx);
+      a.ly = fmaf(a.lpl, r.dy, a.ly);
+      a.ldx = fmaf(a.lpl, r.x, a.ldx);
+      a.ldy = fmaf(a.lpl, r.y, a.ldy);
+    } break;
+    case OP_BIPRISM: {
+      uint32_t b = (uint32_t)(sbits >> (2 * op.aux)) & 3u;
+      float s = b == 1u ? 1.f : (b == 2u ? -1.f : 0.f);
+      c[0] = a.ldx * s;
+      r.dx = fmaf(-op.c[0], s, r.dx);
+      a.lx = fmaf(a.lpl, r.dx, a.lx);
+      a.ly = fmaf(a.lpl, r.dy, a.ly);
+      a.ldx = fmaf(a.lpl, r.x, a.ldx);
+      a.ldy = fmaf(a.lpl, r.y, a.ldy);
+    } break;
+    case OP_ROTATE: {
+      float cs = op.c[0], sn = op.c[1];
+      c[0] = -a.lx * r.y + a.ly * r.x - a.ldx * r.dy + a.ldy * r.dx;
+      float x = r.x, y = r.y, dx = r.dx, dy = r.dy;
+      r.x = x * cs + y * sn;
+      r.y = -x * sn + y * cs;
+      r.dx = dx * cs + dy * sn;
+      r.dy = -dx * sn + dy * cs;
+      float lx = a.lx, ly = a.ly, ldx = a.ldx, ldy = a.ldy;
+      a.lx = lx * cs + ly * sn;
+      a.ly = -lx * sn + ly * cs;
+      a.ldx = ldx * cs + ldy * sn;
+      a.ldy = -ldx * sn + ldy * cs;
+    } break;
+    default:
+      break;
+  }
+}
+
+template <int R>
+__global__ void __launch_bounds__(256)
+k_trace_vjp(const __grid_constant__ Program P, const __grid_constant__ VjpArgs A) {
+  __shared__ double acc[kMaxSteps * 4];
+  const bool sums = A.partial != nullptr;
+  if (sums)
+    for (int i = threadIdx.x; i < P.n_steps * 4; i += blockDim.x) acc[i] = 0.0;
+  __syncthreads();
+  const int64_t n = A.n;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x * R;
+  const int lane = threadIdx.x & 31;
+  for (int64_t blk = (int64_t)blockIdx.x * blockDim.x * R; blk < n; blk += stride) {
+    const int64_t i0 = blk + (int64_t)threadIdx.x * R;
+    const bool vec = (R == 4) && (i0 + 3 < n);
+    float x[R], y[R], dx[R], dy[R];
+    load4<R>(A.x, i0, n, x, vec);
+    load4<R>(A.y, i0, n, y, vec);
+    load4<R>(A.dx, i0, n, dx, vec);
+    load4<R>(A.dy, i0, n, dy, vec);
+    RayS r[R];
+    Adj ad[R];
+    double zi[R], dvar[R];
+    uint64_t sb[R];
+    bool alive[R];
+    float gz[R];
+    float gx[R], gy[R], gdx[R], gdy[R];
+    load4<R>(A.gx, i0, n, gx, vec);
+    load4<R>(A.gy, i0, n, gy, vec);
+    load4<R>(A.gdx, i0, n, gdx, vec);
+    load4<R>(A.gdy, i0, n, gdy, vec);
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+      const bool inr = i0 + k < n;
+      r[k] = RayS{x[k], y[k], dx[k], dy[k], 0.f};
+      zi[k] = (A.z && inr) ? A.z[i0 + k] : A.z_scalar;
+      dvar[k] = 0.0;
+      sb[k] = 0;
+      alive[k] = true;
+      gz[k] = 0.f;
+      float gp = (A.gpl && inr) ? (float)A.gpl[i0 + k] : 0.f;
+      // rays beyond n carry zero adjoints so they add nothing to the sums
+      ad[k] = inr ? Adj{gx[k], gy[k], gdx[k], gdy[k], gp} : Adj{0.f, 0.f, 0.f, 0.f, 0.f};
+    }
+    for (int s = 0; s < P.n_steps; ++s) {
+      const Op op = P.op[s];
+#pragma unroll
+      for (int k = 0; k < R; ++k)
+        op_forward(op, nullptr, r[k], P.zc_first, zi[k], dvar[k], sb[k], alive[k]);
+    }
+    for (int s = P.n_steps - 1; s >= 0; --s) {
+      const Op op = P.op[s];
+      float c[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int k = 0; k < R; ++k) {
+        float ck[4] = {0.f, 0.f, 0.f, 0.f};
+        op_reverse(op, nullptr, r[k], ad[k], sb[k], dvar[k], ck, gz[k]);
+        c[0] += ck[0]; c[1] += ck[1]; c[2] += ck[2]; c[3] += ck[3];
+      }
+      if (sums) {
+        const int ns = op_nsums(op.kind);
+        for (int j = 0; j < ns; ++j) {
+          float v = warp_sum(c[j]);
+          if (lane == 0) atomicAdd(&acc[4 * s + j], (double)v);
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+      gx[k] = ad[k].lx; gy[k] = ad[k].ly; gdx[k] = ad[k].ldx; gdy[k] = ad[k].ldy;
+    }
+    if (A.ix) store4<R>(A.ix, i0, n, gx, vec);
+    if (A.iy) store4<R>(A.iy, i0, n, gy, vec);
+    if (A.idx) store4<R>(A.idx, i0, n, gdx, vec);
+    if (A.idy) store4<R>(A.idy, i0, n, gdy, vec);
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+      if (i0 + k < n) {
+        if (A.ipl) A.ipl[i0 + k] = A.gpl ? A.gpl[i0 + k] : 0.0;
+        if (A.iz) A.iz[i0 + k] = (double)gz[k];
+      }
+    }
+  }
+  if (sums) {
+    __syncthreads();
+    double* dst = A.partial + (size_t)blockIdx.x * P.n_steps * 4;
+    for (int i = threadIdx.x; i < P.n_steps * 4; i += blockDim.x) dst[i] = acc[i];
+  }
+}
+
+// raw[i] += sum over blocks of partial[b][i], in block order.
+__global__ void k_reduce_partials(const double* __restrict__ partial, int nblocks,
+                                  int width, double* __restrict__ raw) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= width) return;
+  double s = 0.0;
+  for (int b = 0; b < nblocks; ++b) s += partial[(size_t)b * width + i];
+  raw[i] += s;
+}
+
+static int vjp_grid(int64_t n) {
+  int64_t need = (n + 1023) / 1024;
+  int64_t cap = (int64_t)sm_count() * 4;
+  int64_t g = need < cap ? need : cap;
+  return (int)(g < 1 ? 1 : g);
+}
+
+}  // namespace tg
+
+extern "C" size_t tg_trace_vjp_workspace(int64_t n, const tg_model* model) {
+  if (!model || n < 0) return 0;
+  return (size_t)vjp_grid(n) * (size_t)(2 * model->n_components) * 4 * sizeof(double);
+}
+
+extern "C" int tg_trace_vjp(const tg_model* model, const tg_rays* in, const tg_rays* gout,
+                            tg_rays* gin, double* raw, void* workspace, size_t ws_bytes,
+                            void* stream) {
+  if (!model || !in || !gout) return TG_ERR_INVALID;
+  if (in->n < 0 || gout->n != in->n) return TG_ERR_INVALID;
+  if (in->n > 0 && (!in->x || !in->y || !in->dx || !in->dy || !gout->x || !gout->y ||
+                    !gout->dx || !gout->dy))
+    return TG_ERR_INVALID;
+  Program P;
+  int st = compile_program(model, in->z != nullptr, in->z_scalar, &P);
+  if (st != TG_OK) return st;
+  if (P.n_probe_ops) return TG_ERR_UNSUPPORTED;
+  if (in->n == 0) return TG_OK;
+  const int grid = vjp_grid(in->n);
+  const size_t need = (size_t)grid * P.n_steps * 4 * sizeof(double);
+  if (raw && P.n_steps > 0 && (!workspace || ws_bytes < need)) return TG_ERR_WORKSPACE;
+  VjpArgs A;
+  std::memset(&A, 0, sizeof(A));
+  A.n = in->n;
+  A.x = in->x; A.y = in->y; A.dx = in->dx; A.dy = in->dy;
+  A.z = in->z; A.z_scalar = in->z_scalar;
+  A.gx = gout->x; A.gy = gout->y; A.gdx = gout->dx; A.gdy = gout->dy;
+  A.gpl = gout->pathlength;
+  if (gin) {
+    if (gin->n != in->n) return TG_ERR_INVALID;
+    A.ix = gin->x; A.iy = gin->y; A.idx = gin->dx; A.idy = gin->dy;
+    A.ipl = gin->pathlength; A.iz = gin->z;
+  }
+  A.partial = (raw && P.n_steps > 0) ? reinterpret_cast<double*>(workspace) : nullptr;
+  bool vec = al16(A.x) && al16(A.y) && al16(A.dx) && al16(A.dy) && al16(A.gx) &&
+             al16(A.gy) && al16(A.gdx) && al16(A.gdy) && (!A.ix || al16(A.ix)) &&
+             (!A.iy || al16(A.iy)) && (!A.idx || al16(A.idx)) && (!A.idy || al16(A.idy));
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (vec) k_trace_vjp<4><<<grid, 256, 0, s>>>(P, A);
+  else k_trace_vjp<1><<<grid, 256, 0, s>>>(P, A);
+  if (A.partial) {
+    int width = P.n_steps * 4;
+    k_reduce_partials<<<(width + 127) / 128, 128, 0, s>>>(A.partial, grid, width, raw);
+  }
+  return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
+}

@@ -1,0 +1,49 @@
+"""Propagators (propagator.py:8-116).
+
+Only paraxial free space (propagator.py:43-76) is on the GPU path; it is
+fused into the chain kernel rather than applied as a separate pass.
+"""
+from __future__ import annotations
+
+from typing import NamedTuple
+
+
+class BasePropagator:
+    """propagator.py:8-19."""
+
+    def __call__(self, ray, distance):
+        raise NotImplementedError
+
+    def with_distance(self, distance) -> "Propagator":
+        return Propagator(distance, self)
+
+
+class Propagator(NamedTuple):
+    """propagator.py:22-40: callable (distance, propagator) pair."""
+    distance: float
+    propagator: BasePropagator
+
+    def __call__(self, ray):
+        return self.propagator(ray, self.distance)
+
+
+class FreeSpaceParaxial(BasePropagator):
+    """x += dx*d, y += dy*d, z += d, pathlength += d (propagator.py:51-72)."""
+
+    def __call__(self, ray, distance):
+        from .components import Plane
+        from .run import run_component
+        z = ray.z if not hasattr(ray.z, "reshape") else ray.z
+        return run_component(Plane(z=z + distance), ray)
+
+    @staticmethod
+    def propagate(ray, distance):
+        return FreeSpaceParaxial()(ray, distance)
+
+
+class FreeSpaceDirCosine(BasePropagator):
+    """Direction-cosine propagation (propagator.py:79-116) is outside the
+    accelerated paraxial path."""
+
+    def __call__(self, ray, distance):
+        raise NotImplementedError("FreeSpaceDirCosine is not part of the GPU paraxial path")

@@ -1,0 +1,421 @@
+"""Model execution (drop-in for temgym_core.run, run.py:17-267).
+
+``run_to_end`` packs the model into the C-ABI component table and makes ONE
+fused kernel launch over all rays (forward), or, under autograd, registers
+the recompute-based adjoint kernel as the backward.  There is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from typing import Sequence
+
+import numpy as np
+import torch
+
+from . import _native as N
+from .components import Component, Descanner, Grid, ThickLens, Source, _f
+from .propagator import FreeSpaceParaxial, Propagator
+from .ray import Ray, as_f32, as_f64_or_scalar
+
+
+# ----------------------------------------------------------------- packing
+
+def _check_model(model) -> list:
+    comps = list(model)
+    for c in comps:
+        if not isinstance(c, (Component, Source)):
+            raise NotImplementedError(
+                f"{type(c).__name__} is not a built-in component; the GPU path has no "
+                "generic-callable fallback")
+    if len(comps) > N.MAX_COMPONENTS:
+        raise ValueError(f"model has {len(comps)} components; the maximum is {N.MAX_COMPONENTS}")
+    return comps
+
+
+def pack_model(model):
+    """(TgModel, keep-alive array) for a sequence of components."""
+    comps = _check_model(model)
+    arr = (N.TgComponent * max(1, len(comps)))()
+    for i, c in enumerate(comps):
+        c._pack(arr[i])
+    m = N.TgModel()
+    m.n_components = len(comps)
+    m.components = C.cast(arr, C.POINTER(N.TgComponent))
+    return m, arr
+
+
+def _rays_struct(n, x, y, dx, dy, z_t, z_s, pl_t, pl_s, amp=None) -> N.TgRays:
+    r = N.TgRays()
+    r.n = n
+    r.x, r.y, r.dx, r.dy = N.ptr(x), N.ptr(y), N.ptr(dx), N.ptr(dy)
+    r.z = N.ptr(z_t)
+    r.z_scalar = z_s
+    r.pathlength = N.ptr(pl_t)
+    r.pl_scalar = pl_s
+    r.amplitude = N.ptr(amp)
+    return r
+
+
+class _Soa:
+    """Device structure-of-arrays view of a Ray."""
+
+    def __init__(self, ray: Ray, device):
+        n = ray.size
+        self.n = n
+        self.x = as_f32(ray.x, n, device)
+        self.y = as_f32(ray.y, n, device)
+        self.dx = as_f32(ray.dx, n, device)
+        self.dy = as_f32(ray.dy, n, device)
+        self.z_t, self.z_s = as_f64_or_scalar(ray.z, n, device)
+        self.pl_t, self.pl_s = as_f64_or_scalar(ray.pathlength, n, device)
+        amp = getattr(ray, "amplitude", None)
+        self.amp = None
+        if amp is not None and not isinstance(amp, complex) and not np.iscomplexobj(np.asarray(
+                amp.detach().cpu() if isinstance(amp, torch.Tensor) else amp)):
+            self.amp = as_f32(amp, n, device)
+
+    def struct(self) -> N.TgRays:
+        return _rays_struct(self.n, self.x, self.y, self.dx, self.dy, self.z_t, self.z_s,
+                            self.pl_t, self.pl_s, self.amp)
+
+
+def _ray_scalar_input(ray: Ray) -> bool:
+    return all(not isinstance(getattr(ray, f), (torch.Tensor, np.ndarray)) or
+               getattr(ray, f).ndim == 0 for f in ("x", "y", "dx", "dy"))
+
+
+def _fwd_launch(model, soa: _Soa, grid=None, want_pix=False, hist=None, want_amp=False):
+    dev = soa.x.device
+    n = soa.n
+    ox = torch.empty(n, dtype=torch.float32, device=dev)
+    oy = torch.empty_like(ox)
+    odx = torch.empty_like(ox)
+    ody = torch.empty_like(ox)
+    opl = torch.empty(n, dtype=torch.float64, device=dev)
+    oamp = torch.empty(n, dtype=torch.float32, device=dev) if (want_amp or soa.amp is not None) else None
+    m, keep = pack_model(model)
+    out = _rays_struct(n, ox, oy, odx, ody, None, 0.0, opl, 0.0, oamp)
+    zout = C.c_double(0.0)
+    py = px = None
+    g = None
+    if grid is not None:
+        g = grid._tg_grid()
+        if want_pix:
+            py = torch.empty(n, dtype=torch.int32, device=dev)
+            px = torch.empty(n, dtype=torch.int32, device=dev)
+    if hist is not None and hist.dtype not in (torch.int32, torch.int64):
+        raise TypeError("histogram accumulator must be int32 or int64")
+    st = N.lib().tg_trace_fwd(C.byref(m), C.byref(soa.struct()), C.byref(out), C.byref(zout),
+                              C.byref(g) if g is not None else None, N.ptr(py), N.ptr(px),
+                              N.ptr(hist), 1 if (hist is not None and hist.dtype == torch.int64) else 0,
+                              N.stream_ptr())
+    del keep
+    N.check(st, "tg_trace_fwd")
+    return ox, oy, odx, ody, opl, zout.value, oamp, py, px
+
+
+# ---------------------------------------------------------- differentiable
+
+_DESCAN_FIELDS = ("pxo_pxi", "pxo_pyi", "pyo_pxi", "pyo_pyi", "sxo_pxi", "sxo_pyi", "syo_pxi",
+                  "syo_pyi", "offpxi", "offpyi", "offsxi", "offsyi", "pxo_sxi", "pxo_syi",
+                  "pyo_sxi", "pyo_syi", "sxo_sxi", "sxo_syi", "syo_sxi", "syo_syi")
+# DescanError field -> (row, col) of the 4x4 matrix, or ("off", row)
+_DESCAN_POS = {"pxo_pxi": (0, 0), "pxo_pyi": (0, 1), "pyo_pxi": (1, 0), "pyo_pyi": (1, 1),
+               "sxo_pxi": (2, 0), "sxo_pyi": (2, 1), "syo_pxi": (3, 0), "syo_pyi": (3, 1),
+               "offpxi": ("off", 0), "offpyi": ("off", 1), "offsxi": ("off", 2),
+               "offsyi": ("off", 3), "pxo_sxi": (0, 2), "pxo_syi": (0, 3), "pyo_sxi": (1, 2),
+               "pyo_syi": (1, 3), "sxo_sxi": (2, 2), "sxo_syi": (2, 3), "syo_sxi": (3, 2),
+               "syo_syi": (3, 3)}
+
+
+def _grad_params(comps) -> list:
+    """(component index, path, tensor) for every parameter tensor needing grad."""
+    out = []
+    for i, c in enumerate(comps):
+        names = [f for f in getattr(c, "__dataclass_fields__", {})]
+        for name in names:
+            v = getattr(c, name)
+            if isinstance(v, torch.Tensor) and v.requires_grad:
+                out.append((i, name, v))
+            if name == "descan_error":
+                for dn in _DESCAN_FIELDS:
+                    dv = getattr(v, dn)
+                    if isinstance(dv, torch.Tensor) and dv.requires_grad:
+                        out.append((i, "descan_error." + dn, dv))
+    return out
+
+
+def param_gradient(comps, i, path, raw):
+    """dL/d(parameter) from the adjoint's per-step sums raw[(2*n_components), 4]."""
+    c = comps[i]
+    nc = len(comps)
+    comp = raw[2 * i + 1]
+    if path in ("z", "z_po"):
+        g = raw[2 * i, 0]
+        if i + 1 < nc and not isinstance(c, ThickLens):
+            g = g - raw[2 * i + 2, 0]
+        return g
+    if path == "z_pi":
+        return -raw[2 * i + 2, 0] if i + 1 < nc else raw[0, 0] * 0.0
+    if path == "focal_length" or path == "def_x":
+        return comp[0]
+    if path == "def_y":
+        return comp[1]
+    if path == "angle":
+        return comp[0] * (math.pi / 180.0)
+    if isinstance(c, Descanner):
+        m = torch.as_tensor(c.descan_error.as_matrix4(), dtype=torch.float64, device=raw.device)
+        s = [_f(c.scan_pos_x), _f(c.scan_pos_y), _f(c.scan_tilt_x), _f(c.scan_tilt_y)]
+        g4 = comp[0:4]
+        sp = {"scan_pos_x": 0, "scan_pos_y": 1, "scan_tilt_x": 2, "scan_tilt_y": 3}
+        if path in sp:
+            j = sp[path]
+            return (g4 * m[:, j]).sum() - g4[j]
+        dn = path.split(".", 1)[1]
+        pos = _DESCAN_POS[dn]
+        if pos[0] == "off":
+            return g4[pos[1]]
+        return g4[pos[0]] * s[pos[1]]
+    sp = {"scan_pos_x": 0, "scan_pos_y": 1, "scan_tilt_x": 2, "scan_tilt_y": 3}
+    if path in sp:
+        return comp[sp[path]]
+    raise NotImplementedError(f"no gradient rule for {type(c).__name__}.{path}")
+
+
+class _TraceFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, spec, x, y, dx, dy, pl, zin, *params):
+        comps, soa = spec["comps"], spec["soa"]
+        ox, oy, odx, ody, opl, zout, _, _, _ = _fwd_launch(comps, soa)
+        spec["zout"] = zout
+        ctx.spec = spec
+        return ox, oy, odx, ody, opl
+
+    @staticmethod
+    def backward(ctx, gx, gy, gdx, gdy, gpl):
+        spec = ctx.spec
+        comps, soa, plist = spec["comps"], spec["soa"], spec["params"]
+        n = soa.n
+        dev = soa.x.device
+        z32 = lambda: torch.zeros(n, dtype=torch.float32, device=dev)  # noqa: E731
+        gx = z32() if gx is None else gx.to(torch.float32).contiguous()
+        gy = z32() if gy is None else gy.to(torch.float32).contiguous()
+        gdx = z32() if gdx is None else gdx.to(torch.float32).contiguous()
+        gdy = z32() if gdy is None else gdy.to(torch.float32).contiguous()
+        gpl = None if gpl is None else gpl.to(torch.float64).contiguous()
+        ix, iy, idx, idy = z32(), z32(), z32(), z32()
+        ipl = torch.empty(n, dtype=torch.float64, device=dev)
+        need_raw = bool(plist) or spec["z_grad"]
+        m, keep = pack_model(comps)
+        raw = torch.zeros((2 * len(comps), 4), dtype=torch.float64, device=dev) if need_raw else None
+        ws = None
+        if need_raw:
+            nbytes = N.lib().tg_trace_vjp_workspace(n, C.byref(m))
+            ws = torch.empty(max(8, nbytes), dtype=torch.uint8, device=dev)
+        gout = _rays_struct(n, gx, gy, gdx, gdy, None, 0.0, gpl, 0.0)
+        gin = _rays_struct(n, ix, iy, idx, idy, None, 0.0, ipl, 0.0)
+        st = N.lib().tg_trace_vjp(C.byref(m), C.byref(soa.struct()), C.byref(gout), C.byref(gin),
+                                  N.ptr(raw), N.ptr(ws), 0 if ws is None else ws.numel(),
+                                  N.stream_ptr())
+        del keep
+        N.check(st, "tg_trace_vjp")
+        pgrads = []
+        for (i, path, t) in plist:
+            g = param_gradient(comps, i, path, raw)
+            pgrads.append(g.to(t.dtype).reshape(t.shape))
+        gz = (-raw[0, 0]).reshape(()) if (spec["z_grad"] and raw is not None and len(comps)) else None
+        shape = spec["shape"]
+        if gpl is None:
+            ipl = None
+        return (None, ix.reshape(shape), iy.reshape(shape), idx.reshape(shape),
+                idy.reshape(shape), ipl if ipl is None else ipl.reshape(shape), gz, *pgrads)
+
+
+def _needs_grad(ray, comps) -> bool:
+    if not torch.is_grad_enabled():
+        return False
+    for f in ("x", "y", "dx", "dy", "pathlength", "z"):
+        v = getattr(ray, f)
+        if isinstance(v, torch.Tensor) and v.requires_grad:
+            return True
+    return bool(_grad_params(comps))
+
+
+def _in_shape(ray: Ray):
+    return () if _ray_scalar_input(ray) else (ray.size,)
+
+
+def _device():
+    N.require_cuda()
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def run_to_end(ray: Ray, components: Sequence[Component],
+               propagator=FreeSpaceParaxial()) -> Ray:
+    """Propagate rays through every component (run.py:85-116), one fused
+    GPU launch.  Returns a Ray with float32 x, y, dx, dy, float64 pathlength
+    and uniform z."""
+    if not isinstance(propagator, FreeSpaceParaxial):
+        raise NotImplementedError("only FreeSpaceParaxial is on the GPU path")
+    comps = _check_model(components)
+    dev = _device()
+    soa = _Soa(ray, dev)
+    shape = _in_shape(ray)
+    if _needs_grad(ray, comps):
+        plist = _grad_params(comps)
+        zt = ray.z if isinstance(ray.z, torch.Tensor) and ray.z.requires_grad and ray.z.dim() == 0 else None
+        spec = {"comps": comps, "soa": soa, "params": plist, "shape": shape,
+                "z_grad": zt is not None}
+        xs = [ray.x, ray.y, ray.dx, ray.dy]
+        xs = [v if isinstance(v, torch.Tensor) and v.requires_grad else
+              torch.zeros((), device=dev) for v in xs]
+        pl = ray.pathlength if isinstance(ray.pathlength, torch.Tensor) and ray.pathlength.requires_grad \
+            else torch.zeros((), device=dev, dtype=torch.float64)
+        zin = zt if zt is not None else torch.zeros((), device=dev, dtype=torch.float64)
+        ox, oy, odx, ody, opl = _TraceFn.apply(spec, *xs, pl, zin, *[p[2] for p in plist])
+        zout = spec["zout"]
+    else:
+        ox, oy, odx, ody, opl, zout, _, _, _ = _fwd_launch(comps, soa)
+    out = Ray(x=ox.reshape(shape), y=oy.reshape(shape), dx=odx.reshape(shape),
+              dy=ody.reshape(shape), z=zout, pathlength=opl.reshape(shape),
+              _one=ray._one)
+    return out
+
+
+def run_component(component: Component, ray: Ray) -> Ray:
+    """One component's __call__ on the GPU.  Unlike run_to_end no free-space
+    step is applied: the ray must already sit at the component (the reference
+    component call does not move the ray)."""
+    comps = [component]
+    z_s = None
+    zz = ray.z
+    # The kernel always inserts a propagator; place it at the ray's own z so
+    # the inserted distance is exactly 0 (matches components.py semantics).
+    import dataclasses as _dc
+    if isinstance(zz, torch.Tensor) and zz.dim() > 0 or isinstance(zz, np.ndarray) and zz.ndim > 0:
+        raise NotImplementedError("component call on rays with per-ray z")
+    z_s = _f(zz)
+    if isinstance(component, ThickLens):
+        moved = _dc.replace(component, z_po=z_s, z_pi=z_s - (_f(component.z_po) - _f(component.z_pi)))
+    elif _dc.is_dataclass(component) and "z" in component.__dataclass_fields__:
+        moved = _dc.replace(component, z=z_s)
+    else:
+        moved = component
+    comps = [moved]
+    out = run_to_end(ray, comps)
+    return out
+
+
+def run_iter(ray: Ray, components: Sequence[Component], propagator=FreeSpaceParaxial()):
+    """run.py:47-82: yields (Propagator, ray) then (component, ray) per element."""
+    from .components import Plane
+    for c in _check_model(components):
+        d = _f(c.z) - _f(ray.z)
+        ray = run_to_end(ray, [Plane(z=_f(c.z))])
+        yield Propagator(d, propagator), ray
+        ray = run_component(c, ray)
+        yield c, ray
+
+
+def _central(ray: Ray):
+    r = ray if _ray_scalar_input(ray) else ray[0]
+    v = [r.x, r.y, r.dx, r.dy, r.z]
+    return [float(np.asarray(a.detach().cpu() if isinstance(a, torch.Tensor) else a).reshape(-1)[0])
+            for a in v]
+
+
+def abcd_matrix(ray: Ray, components: Sequence[Component]) -> np.ndarray:
+    """float64 5x5 ABCD of the model about a central ray: the reference's
+    custom_jacobian_matrix(jax.jacobian(run_to_end)(ray, model))
+    (README.md:224-234, utils.py:7-43), composed from component matrices."""
+    m, keep = pack_model(components)
+    cen = (C.c_double * 5)(*_central(ray))
+    out = (C.c_double * 25)()
+    N.check(N.lib().tg_abcd_compose(C.byref(m), cen, out, None), "tg_abcd_compose")
+    del keep
+    return np.array(out[:], dtype=np.float64).reshape(5, 5)
+
+
+def solve_model(ray: Ray, model: Sequence[Component], propagator=FreeSpaceParaxial()) -> np.ndarray:
+    """run.py:150-179: per-step 5x5 matrices, shape (2*n_components, 5, 5)."""
+    comps = _check_model(model)
+    m, keep = pack_model(comps)
+    cen = (C.c_double * 5)(*_central(ray))
+    out = (C.c_double * 25)()
+    steps = (C.c_double * (50 * max(1, len(comps))))()
+    N.check(N.lib().tg_abcd_compose(C.byref(m), cen, out, steps), "tg_abcd_compose")
+    del keep
+    return np.array(steps[:50 * len(comps)], dtype=np.float64).reshape(-1, 5, 5)
+
+
+# ------------------------------------------------------------------ binning
+
+def bin_pixels(grid: Grid, x, y):
+    """Bit-exact metres->pixels on the GPU (grid.py:120-153)."""
+    dev = _device()
+    xt = x if isinstance(x, torch.Tensor) else torch.as_tensor(np.asarray(x, dtype=np.float32))
+    yt = y if isinstance(y, torch.Tensor) else torch.as_tensor(np.asarray(y, dtype=np.float32))
+    shape = tuple(xt.shape)
+    n = max(xt.numel(), yt.numel())
+    xs = as_f32(xt, n, dev)
+    ys = as_f32(yt, n, dev)
+    py = torch.empty(n, dtype=torch.int32, device=dev)
+    px = torch.empty(n, dtype=torch.int32, device=dev)
+    g = grid._tg_grid()
+    N.check(N.lib().tg_bin(n, N.ptr(xs), N.ptr(ys), None, C.byref(g), N.ptr(py), N.ptr(px),
+                           None, 0, N.stream_ptr()), "tg_bin")
+    from . import PixelsYX
+    return PixelsYX(y=py.reshape(shape), x=px.reshape(shape))
+
+
+def image_from(grid: Grid, ray, acc=None):
+    """grid.py:231-280 on the GPU."""
+    dev = _device()
+    h, w = int(grid.shape[0]), int(grid.shape[1])
+    if acc is None:
+        acc = torch.zeros((h, w), dtype=torch.int64, device=dev)
+    if tuple(acc.shape) != (h, w):
+        raise ValueError(f"accumulator shape {tuple(acc.shape)} != grid shape {(h, w)}")
+    if acc.dtype not in (torch.int32, torch.int64) or not acc.is_cuda or not acc.is_contiguous():
+        raise TypeError("accumulator must be a contiguous int32/int64 CUDA tensor")
+    if isinstance(ray, Ray):
+        n = ray.size
+        xs = as_f32(ray.x, n, dev)
+        ys = as_f32(ray.y, n, dev)
+        g = grid._tg_grid()
+        N.check(N.lib().tg_bin(n, N.ptr(xs), N.ptr(ys), None, C.byref(g), None, None,
+                               N.ptr(acc), 1 if acc.dtype == torch.int64 else 0,
+                               N.stream_ptr()), "tg_bin")
+        return acc
+    # PixelsYX input: integer indices already computed
+    py, px = ray
+    py = torch.as_tensor(py, device=dev).reshape(-1).long()
+    px = torch.as_tensor(px, device=dev).reshape(-1).long()
+    ok = (py >= 0) & (py < h) & (px >= 0) & (px < w)
+    acc.view(-1).index_put_((py[ok] * w + px[ok],),
+                            torch.ones(int(ok.sum()), dtype=acc.dtype, device=dev), accumulate=True)
+    return acc
+
+
+def trace_to_image(ray: Ray, components: Sequence[Component], detector: Grid | None = None,
+                   acc: torch.Tensor | None = None, want_pixels: bool = True):
+    """Fused run_to_end + Detector.metres_to_pixels + Detector.into_image in a
+    single kernel pass.  Returns (ray_out, PixelsYX or None, image)."""
+    comps = _check_model(components)
+    if detector is None:
+        detector = comps[-1]
+    if not isinstance(detector, Grid):
+        raise ValueError("trace_to_image needs a Detector/ScanGrid")
+    dev = _device()
+    soa = _Soa(ray, dev)
+    h, w = int(detector.shape[0]), int(detector.shape[1])
+    if acc is None:
+        acc = torch.zeros((h, w), dtype=torch.int64, device=dev)
+    ox, oy, odx, ody, opl, zout, oamp, py, px = _fwd_launch(comps, soa, detector, want_pixels, acc)
+    shape = _in_shape(ray)
+    out = Ray(x=ox.reshape(shape), y=oy.reshape(shape), dx=odx.reshape(shape),
+              dy=ody.reshape(shape), z=zout, pathlength=opl.reshape(shape), _one=ray._one)
+    from . import PixelsYX
+    pix = PixelsYX(y=py.reshape(shape), x=px.reshape(shape)) if want_pixels else None
+    return out, pix, acc

@@ -1,0 +1,115 @@
+"""Seeded synthetic workloads with the shapes of the benchmark configurations.
+
+Each generator returns plain NumPy inputs plus a model description as a list
+of dicts (``{"kind": ..., <reference field names>}``); ``build_model`` turns
+that description into this package's components.  No dataset is read: the
+reference publishes no benchmark data, so inputs are drawn from the stated
+distributions with ``numpy.random.default_rng(seed)``.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import components as K
+
+_KIND = {"lens": K.Lens, "plane": K.Plane, "detector": K.Detector, "scangrid": K.ScanGrid,
+         "scanner": K.Scanner, "descanner": K.Descanner, "deflector": K.Deflector,
+         "biprism": K.Biprism, "rotator": K.Rotator, "thicklens": K.ThickLens,
+         "aperture": K.Aperture, "source": K.PointSource}
+
+
+def build_model(spec):
+    """List of dict descriptions -> list of components."""
+    out = []
+    for c in spec:
+        kw = {k: v for k, v in c.items() if k != "kind"}
+        cls = _KIND[c["kind"]]
+        if c["kind"] == "descanner" and "descan_error" in kw:
+            kw["descan_error"] = K.DescanError(**kw["descan_error"])
+        if c["kind"] in ("detector", "scangrid"):
+            kw["pixel_size"] = tuple(kw["pixel_size"])
+            kw["shape"] = tuple(int(v) for v in kw["shape"])
+            if "centre" in kw:
+                kw["centre"] = tuple(kw["centre"])
+        if c["kind"] == "source":
+            kw = {"z": kw["z"]}
+        out.append(cls(**kw))
+    return out
+
+
+def plain_trace(seed: int = 0, n: int = 65536):
+    """Plain paraxial trace: N float32 rays, x, y ~ U(-1e-3, 1e-3) m,
+    dx, dy ~ N(0, 1e-3) rad, z = 0, pathlength = 0; Lens(z=0.5, f=0.2) then
+    Detector(z=1.0, pixel 1e-5 m, 256 x 256)."""
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(-1e-3, 1e-3, n).astype(np.float32)
+    y = rng.uniform(-1e-3, 1e-3, n).astype(np.float32)
+    dx = rng.normal(0.0, 1e-3, n).astype(np.float32)
+    dy = rng.normal(0.0, 1e-3, n).astype(np.float32)
+    spec = [{"kind": "lens", "z": 0.5, "focal_length": 0.2},
+            {"kind": "detector", "z": 1.0, "pixel_size": (1e-5, 1e-5), "shape": (256, 256)}]
+    return {"x": x, "y": y, "dx": dx, "dy": dy, "z": 0.0, "pathlength": 0.0, "model": spec}
+
+
+def stem_4d(seed: int = 0, scan=(64, 64), rays_per_probe: int = 1024, scan_step: float = 1e-9,
+            defocus: float = 1e-6, camera_length: float = 0.1, det_px: float = 5.5e-5,
+            det_shape=(256, 256), semi_conv: float = 5e-3):
+    """4D-STEM shadow-image model.
+
+    A point source at z = 0 emits one bundle of ``rays_per_probe`` rays with
+    slopes dx, dy ~ U(-semi_conv, semi_conv) rad (shared by every probe, as a
+    fixed PointSource sampling is); the sample plane sits ``defocus`` below it
+    and carries a ScanGrid (``scan`` positions, step ``scan_step``, rotation
+    U(0, 360) degrees), the Scanner and the Descanner; the detector is
+    ``camera_length`` further down.  The descan matrix is I + N(0, 1e-3)
+    (rows x, y, dx, dy; columns scan x, y, tilt x, tilt y).
+    """
+    rng = np.random.default_rng(seed)
+    dxs = rng.uniform(-semi_conv, semi_conv, rays_per_probe).astype(np.float32)
+    dys = rng.uniform(-semi_conv, semi_conv, rays_per_probe).astype(np.float32)
+    rot_deg = float(rng.uniform(0.0, 2 * np.pi) * 180.0 / np.pi)
+    descan = np.eye(4) + rng.normal(0.0, 1e-3, (4, 4))
+    z_s = defocus
+    spec_scan = {"kind": "scangrid", "z": z_s, "pixel_size": (scan_step, scan_step),
+                 "shape": tuple(scan), "rotation": rot_deg}
+    det = {"kind": "detector", "z": z_s + camera_length, "pixel_size": (det_px, det_px),
+           "shape": tuple(det_shape)}
+    return {"x": np.zeros(rays_per_probe, np.float32), "y": np.zeros(rays_per_probe, np.float32),
+            "dx": dxs, "dy": dys, "z": 0.0, "pathlength": 0.0,
+            "scangrid": spec_scan, "descan": descan, "detector": det,
+            "source_z": 0.0}
+
+
+def descan_error_from_matrix(m) -> dict:
+    m = np.asarray(m, dtype=np.float64)
+    return {"pxo_pxi": m[0, 0], "pxo_pyi": m[0, 1], "pyo_pxi": m[1, 0], "pyo_pyi": m[1, 1],
+            "sxo_pxi": m[2, 0], "sxo_pyi": m[2, 1], "syo_pxi": m[3, 0], "syo_pyi": m[3, 1],
+            "pxo_sxi": m[0, 2], "pxo_syi": m[0, 3], "pyo_sxi": m[1, 2], "pyo_syi": m[1, 3],
+            "sxo_sxi": m[2, 2], "sxo_syi": m[2, 3], "syo_sxi": m[3, 2], "syo_syi": m[3, 3]}
+
+
+def stem_probe_model(w: dict, spx: float, spy: float):
+    """Per-probe model description of ``stem_4d`` at one scan position."""
+    z = w["scangrid"]["z"]
+    err = descan_error_from_matrix(w["descan"])
+    return [{"kind": "source", "z": w["source_z"]},
+            dict(w["scangrid"]),
+            {"kind": "scanner", "z": z, "scan_pos_x": spx, "scan_pos_y": spy},
+            {"kind": "descanner", "z": z, "scan_pos_x": spx, "scan_pos_y": spy,
+             "descan_error": err},
+            dict(w["detector"])]
+
+
+def stem_model(w: dict):
+    """Components of ``stem_4d`` (scan positions are supplied per probe)."""
+    _d = descan_error_from_matrix
+    sg = w["scangrid"]
+    z = sg["z"]
+    return [K.PointSource(z=w["source_z"]),
+            K.ScanGrid(z=z, pixel_size=tuple(sg["pixel_size"]), shape=tuple(sg["shape"]),
+                       rotation=sg["rotation"]),
+            K.Scanner(z=z, scan_pos_x=0.0, scan_pos_y=0.0),
+            K.Descanner(z=z, scan_pos_x=0.0, scan_pos_y=0.0,
+                        descan_error=K.DescanError(**_d(w["descan"]))),
+            K.Detector(z=w["detector"]["z"], pixel_size=tuple(w["detector"]["pixel_size"]),
+                       shape=tuple(w["detector"]["shape"]))]

@@ -1,0 +1,200 @@
+"""The oracle against the reference's own known answers (CPU only)."""
+import numpy as np
+import pytest
+
+import oracle
+from oracle.rays import ORay, accumulate_matrices, free_matrix, component_matrix
+from oracle import field as OF
+
+
+def _ray(v):
+    return ORay(*v[:4], z=v[4], pathlength=v[5])
+
+
+def test_readme_quickstart(kats):
+    q = kats["readme_quickstart"]
+    r = q["ray"]
+    o = oracle.run_to_end(ORay(r["x"], r["y"], r["dx"], r["dy"], r["z"], r["pathlength"]), q["model"])
+    e = q["expected"]
+    for k in ("x", "y", "dx", "dy", "z", "pathlength"):
+        assert abs(float(getattr(o, k)) - e[k]) < 1e-12, k
+    assert abs(float(o.pathlength) - q["printed_pathlength"]) < 0.005
+
+
+def test_readme_abcd_and_steps(kats):
+    q = kats["readme_quickstart"]
+    r = q["ray"]
+    ray = ORay(r["x"], r["y"], r["dx"], r["dy"], r["z"], r["pathlength"])
+    np.testing.assert_allclose(oracle.model_abcd(ray, q["model"]), kats["readme_abcd"]["abcd"], atol=1e-15)
+    steps = oracle.solve_model(ray, q["model"])
+    np.testing.assert_allclose(steps, kats["readme_abcd"]["per_step"], atol=1e-15)
+
+
+def test_readme_grads_by_complex_step(kats):
+    q = kats["readme_quickstart"]
+    r = q["ray"]
+    h = 1e-30
+    # d x_out / d f  and  d x_out / d z_lens
+    m = [dict(q["model"][0], focal_length=1.0 + 1j * h), q["model"][1]]
+    o = oracle.run_to_end(ORay(r["x"], r["y"], r["dx"], r["dy"], r["z"], r["pathlength"]), m)
+    gf = np.imag(o.x) / h
+    m = [dict(q["model"][0], z=0.5 + 1j * h), q["model"][1]]
+    o = oracle.run_to_end(ORay(r["x"], r["y"], r["dx"], r["dy"], r["z"], r["pathlength"]), m)
+    gz = np.imag(o.x) / h
+    np.testing.assert_allclose([gf, gz], kats["readme_grads"]["dx_out_d_f_and_z"], rtol=1e-12)
+    o = oracle.run_to_end(ORay(0.01 + 1j * h, 0.2, 0.3, 0.4, 0.0, 0.6), q["model"])
+    assert abs(np.imag(o.dx) / h - kats["readme_grads"]["ddx_out_dx_in"]) < 1e-12
+    assert abs(np.imag(o.dy) / h - kats["readme_grads"]["ddy_out_dx_in"]) < 1e-12
+
+
+def test_pixel_kats(kats):
+    for (xy, rot, exp) in kats["scangrid_m2p"]["cases"]:
+        g = {"pixel_size": (0.1, 0.1), "shape": (11, 11), "rotation": rot}
+        assert tuple(int(v) for v in oracle.metres_to_pixels(g, xy[0], xy[1])) == tuple(exp)
+    for (px, rot, exp) in kats["scangrid_p2m"]["cases"]:
+        g = {"pixel_size": (0.1, 0.1), "shape": (11, 11), "rotation": rot}
+        np.testing.assert_allclose(oracle.pixels_to_metres(g, px[0], px[1]), exp, atol=1e-6)
+    for (xy, exp) in kats["detector_m2p"]["cases"]:
+        g = {"pixel_size": (0.1, 0.1), "shape": (11, 11)}
+        assert tuple(int(v) for v in oracle.metres_to_pixels(g, xy[0], xy[1])) == tuple(exp)
+    for (px, exp) in kats["detector_p2m"]["cases"]:
+        g = {"pixel_size": (0.1, 0.1), "shape": (11, 11)}
+        np.testing.assert_allclose(oracle.pixels_to_metres(g, px[0], px[1]), exp, atol=1e-6)
+
+
+@pytest.mark.parametrize("shape", [(5, 5), (3, 7), (4, 4), (5, 8)])
+def test_scangrid_symmetry(shape):
+    h, w = shape
+    g = {"pixel_size": (0.1, 0.1), "shape": shape}
+    _, yv = oracle.pixels_to_metres(g, np.arange(h), np.zeros(h))
+    xv, _ = oracle.pixels_to_metres(g, np.zeros(w), np.arange(w))
+    for size, v in ((h, yv), (w, xv)):
+        if size % 2 == 0:
+            assert np.count_nonzero(v) == size
+            assert v[size // 2] == pytest.approx(-v[size // 2 - 1])
+        else:
+            assert np.count_nonzero(v) == size - 1
+            assert v[size // 2] == pytest.approx(0.0)
+
+
+def test_scanner_descanner_formulas(kats):
+    for c in kats["scanner"]["cases"]:
+        spx, spy, stx, sty = c["scanner"]
+        o = oracle.apply_component({"kind": "scanner", "z": 23, "scan_pos_x": spx, "scan_pos_y": spy,
+                                    "scan_tilt_x": stx, "scan_tilt_y": sty}, _ray(c["ray"]))
+        np.testing.assert_allclose([o.x, o.y, o.dx, o.dy], c["expected"], atol=1e-12)
+    for c in kats["descanner"]["cases"]:
+        spx, spy, stx, sty = c["scan"]
+        o = oracle.apply_component({"kind": "descanner", "z": 23, "scan_pos_x": spx, "scan_pos_y": spy,
+                                    "scan_tilt_x": stx, "scan_tilt_y": sty,
+                                    "descan_error": c["err"]}, _ray(c["ray"]))
+        np.testing.assert_allclose([o.x, o.y, o.dx, o.dy], c["expected"], atol=1e-12)
+    d = kats["descanner_jacobian"]
+    m = component_matrix({"kind": "descanner", "z": 0.0, "scan_pos_x": d["scan"][0],
+                          "scan_pos_y": d["scan"][1], "descan_error": d["err"]})
+    np.testing.assert_allclose(m, d["expected"], atol=1e-12)
+
+
+def test_biprism_and_chain(kats):
+    b = kats["biprism"]
+    m = component_matrix({"kind": "biprism", "z": 0.0, "def_x": b["deflection"]}, 1e-15)
+    assert abs(m[2, 4] - b["jac_dx_one"]) < 1e-12
+    model = [{"kind": "biprism", "z": 0.0, "def_x": b["deflection"]},
+             {"kind": "detector", "z": b["z_det"], "pixel_size": (1e-4, 1e-4), "shape": (512, 512)}]
+    a = oracle.model_abcd(ORay(1e-15, 0.0, 0.0, 0.0, 0.0, 0.0), model)
+    assert abs(a[0, 4] - b["prop_x_one"]) < 1e-12 and abs(a[2, 4] - b["prop_dx_one"]) < 1e-12
+    c = kats["lens_biprism_chain"]
+    cr = c["central_ray"]
+    a = oracle.model_abcd(ORay(cr["x"], cr["y"], cr["dx"], cr["dy"], cr["z"], 0.0), c["model"])
+    np.testing.assert_allclose(a, c["abcd"], atol=c["atol"])
+
+
+def test_propagation_and_run_iter(kats):
+    for c in kats["propagation"]["cases"]:
+        o = oracle.propagate(_ray(c["ray"]), c["d"])
+        np.testing.assert_allclose([o.x, o.y, o.dx, o.dy, o.z, o.pathlength], c["expected"], atol=1e-12)
+        np.testing.assert_allclose(free_matrix(c["d"])[0, 2], c["d"])
+    ri = kats["run_iter"]
+    res = list(oracle.run_iter(_ray(ri["ray"]), ri["model"]))
+    prev = _ray(ri["ray"])
+    for i, comp in enumerate(ri["model"]):
+        (_, d), pr = res[2 * i]
+        assert d == comp["z"] - prev.z
+        np.testing.assert_allclose(pr.x, prev.x + prev.dx * d)
+        prev = res[2 * i + 1][1]
+    # no-propagation case equals composing the components directly
+    r0 = _ray(ri["noprop_ray"])
+    out = oracle.run_to_end(r0, ri["noprop_model"])
+    ref = r0
+    for comp in ri["noprop_model"]:
+        ref = oracle.apply_component(comp, ref)
+    for k in ("x", "y", "dx", "dy", "z", "pathlength"):
+        np.testing.assert_allclose(getattr(out, k), getattr(ref, k))
+
+
+def test_accumulate_order(kats):
+    mats = []
+    for s in kats["accumulate"]["scales"]:
+        m = np.eye(5) * s
+        m[4] = [0, 0, 0, 0, 1]
+        mats.append(m)
+    np.testing.assert_allclose(accumulate_matrices(mats), mats[2] @ mats[1] @ mats[0])
+
+
+def test_gauss_free_space_closed_form(kats):
+    g = kats["gauss_free_space"]
+    wl, w0, L = g["wavelength"], g["w0"], g["L"]
+    k = 2 * np.pi / wl
+    q = 1j * wl / (np.pi * w0 * w0)
+    q1 = np.array([[[q, 0], [0, q]]], dtype=np.complex128)
+    A = np.array([np.eye(2)])
+    B = np.array([L * np.eye(2)])
+    C = np.zeros((1, 2, 2))
+    D = np.array([np.eye(2)])
+    q2 = OF.Qinv_ABCD(q1, A, B, C, D)
+    f = OF.beam_field_pixels(np.array([1.0 + 0j]), np.array([0.0]), q1, q2, np.zeros((1, 2)),
+                             np.zeros((1, 2)), A, B, np.zeros((1, 2)), np.zeros((1, 2)),
+                             np.array([k]), np.array(g["r2"]))[0]
+    ref = np.array(g["field_re"]) + 1j * np.array(g["field_im"])
+    np.testing.assert_allclose(f, ref, rtol=g["rtol"], atol=g["atol"])
+    # Qinv_ABCD identity (tests/test_gaussians.py:218-226)
+    q1 = np.array([[[2j, 0], [0, 3j]]])
+    np.testing.assert_allclose(OF.Qinv_ABCD(q1, A, np.zeros((1, 2, 2)), C, D), q1, rtol=1e-12)
+
+
+def test_gauss_quadrant(kats):
+    g = kats["gauss_quadrant"]
+    det = {"kind": "detector", "z": g["z"], "pixel_size": g["pixel_size"], "shape": g["shape"]}
+    xs, ys = np.meshgrid(*[np.arange(s) for s in g["shape"][::-1]])
+    c = OF.make_gaussian_image({"x": 0.0, "y": 0.0, "dx": 0.0, "dy": 0.0, "z": 0.0, "pathlength": 0.0,
+                                "amplitude": 1.0, "waist_xy": [[g["w0"], g["w0"]]],
+                                "radii_of_curv": [[np.inf, np.inf]], "wavelength": g["wavelength"],
+                                "theta": 0.0}, [det])
+    cy, cx = np.unravel_index(np.argmax(np.abs(c)), c.shape)
+    xc, yc = oracle.pixels_to_metres(det, cy, cx)
+    t = g["tilt"]
+    for dx, dy in ((t, t), (t, -t), (-t, t), (-t, -t)):
+        im = OF.make_gaussian_image({"x": 0.0, "y": 0.0, "dx": dx, "dy": dy, "z": 0.0, "pathlength": 0.0,
+                                     "amplitude": 1.0, "waist_xy": [[g["w0"], g["w0"]]],
+                                     "radii_of_curv": [[np.inf, np.inf]],
+                                     "wavelength": g["wavelength"], "theta": 0.0}, [det])
+        my, mx = np.unravel_index(np.argmax(np.abs(im)), im.shape)
+        xm, ym = oracle.pixels_to_metres(det, my, mx)
+        assert np.sign(xm - xc) == np.sign(dx) and np.sign(ym - yc) == np.sign(dy)
+
+
+def test_phase_reduction_exact():
+    rng = np.random.default_rng(3)
+    k = 2 * np.pi / 1.97e-12
+    pl = 1.0 + rng.normal(0, 1e-6, 64)
+    red = oracle.phase_offset_exact(k, pl)
+    # cross-check against extended precision (x86 80-bit here; 128-bit on Arm)
+    ld = np.longdouble
+    exact = (ld(k) * pl.astype(ld))
+    twopi = ld("6.283185307179586476925286766559")
+    ref = exact - np.rint(exact / twopi) * twopi
+    err = np.abs(np.angle(np.exp(1j * (red - ref.astype(np.float64)))))
+    assert err.max() < 1e-6
+    # the literal float64 product is off by up to ~ulp(3e12) / 2 ~ 2.4e-4 rad
+    lit = np.angle(np.exp(1j * (k * pl)))
+    assert np.abs(np.angle(np.exp(1j * (lit - red)))).max() > 1e-6
