@@ -252,6 +252,70 @@ def secondary_plain(torch, dev):
             "note": "launch-latency bound (3.7 MB per step); includes host-side model packing"}
 
 
+def _time(torch, fn, reps):
+    a, b = _events(torch)
+    fn()
+    torch.cuda.synchronize()
+    a.record()
+    for _ in range(reps):
+        fn()
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / reps
+
+
+def secondary_field(torch, dev, hbm, bf16):
+    """Gaussian-beamlet field, 16,384 beams on 512 x 512 pixels: separable
+    split-BF16 tensor-core GEMM, fast direct kernel (astigmatic beams) and the
+    all-float64 direct kernel, with errors against the float64 oracle on a
+    pixel sample (exact k*pl reduction)."""
+    import temgymcore_gb300 as t
+    from temgymcore_gb300.workloads import beamlet_field, build_model, gaussian_rays
+    res = {"workload": "16,384 beamlets (aperture decomposition, waist 1e-9 m, lambda 1.97e-12 m, "
+                       "pl 1 m + N(0,1e-6)), Lens f=0.5 m, 512x512 detector at 1e-5 m"}
+    pairs = 16384 * 512 * 512
+    w = beamlet_field(seed=0)
+    plan = t.FieldPlan(gaussian_rays(w["rays"]), build_model(w["model"]))
+    res["separable"] = plan.separable
+    ms_prep = _time(torch, lambda: t.FieldPlan(gaussian_rays(w["rays"]), build_model(w["model"]),
+                                               method="separable"), 3)
+    ms_sep = _time(torch, lambda: plan.evaluate("separable"), 20)
+    ms_dir = _time(torch, lambda: plan.evaluate("direct"), 3)
+    ms_f64 = _time(torch, lambda: plan.evaluate("fp64"), 1)
+    gemm_flops = 12 * 2 * 512 * 512 * 16416
+    res["separable_gemm"] = {"ms": ms_sep, "beam_px_per_s": pairs / (ms_sep * 1e-3),
+                             "bf16_issued_tflops": gemm_flops / (ms_sep * 1e-3) / 1e12,
+                             "useful_complex_tflops": 8 * pairs / (ms_sep * 1e-3) / 1e12,
+                             "frac_of_bf16_peak": gemm_flops / (ms_sep * 1e-3) / 1e12 / bf16,
+                             "note": "includes operand generation and split-K reduction"}
+    res["direct_fast"] = {"ms": ms_dir, "beam_px_per_s": pairs / (ms_dir * 1e-3)}
+    res["direct_fp64"] = {"ms": ms_f64, "beam_px_per_s": pairs / (ms_f64 * 1e-3)}
+    res["speedup_separable_vs_fp64"] = ms_f64 / ms_sep
+    res["prep_plan_ms"] = ms_prep
+    # errors against the float64 oracle on a pixel sample
+    try:
+        from oracle import field as OF
+        rng = np.random.default_rng(1)
+        idx = rng.choice(512 * 512, 48, replace=False)
+        ref = OF.make_gaussian_image(w["rays"], w["model"], pixel_index=idx, chunk=2048)
+        scale = np.max(np.abs(ref))
+        for name in ("separable", "direct", "fp64"):
+            g = plan.evaluate(name).reshape(-1)[torch.as_tensor(idx, device=dev)].cpu().numpy()
+            err = np.max(np.abs(g - ref)) / scale
+            bright = np.abs(ref) > 0.25 * scale
+            ph = float(np.max(np.abs(np.angle(g[bright] * np.conj(ref[bright]))))) if bright.any() else None
+            res[{"separable": "separable_gemm", "direct": "direct_fast", "fp64": "direct_fp64"}[name]].update(
+                {"field_rel_err": float(err), "phase_err_rad_bright": ph})
+    except Exception as e:
+        res["oracle_error"] = repr(e)
+    # astigmatic case (direct kernel only)
+    wa = beamlet_field(seed=0, astigmatic=True)
+    pa = t.FieldPlan(gaussian_rays(wa["rays"]), build_model(wa["model"]))
+    ms_a = _time(torch, lambda: pa.evaluate("direct"), 3)
+    res["astigmatic_direct"] = {"ms": ms_a, "beam_px_per_s": pairs / (ms_a * 1e-3), "separable": pa.separable}
+    return res
+
+
 def run_gpu(args, world, rank, local):
     import torch
 
@@ -333,6 +397,10 @@ def run_gpu(args, world, rank, local):
             secondary["plain_trace"] = secondary_plain(torch, dev)
         except Exception as e:  # report, never hide
             secondary["plain_trace"] = {"error": repr(e)}
+        try:
+            secondary["beamlet_field"] = secondary_field(torch, dev, hbm, bf16)
+        except Exception as e:
+            secondary["beamlet_field"] = {"error": repr(e)}
     cpu = cpu_baseline() if (rank == 0 and world == 1) else None
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",

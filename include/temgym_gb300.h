@@ -191,6 +191,59 @@ typedef struct tg_scan {
 int tg_scan_hist(const tg_model *model, const tg_rays *bundle, const tg_scan *scan,
                  const tg_grid *grid, int32_t *hist, float *probe_xy, void *stream);
 
+/* ---- Gaussian-beamlet detector field ----------------------------------- */
+/* Beamlets (GaussianRay, gaussian.py:113-177): central rays and beam shape,
+ * all device arrays.  amplitude is complex64 (re, im pairs); waist_xy and
+ * radii are [n][2] (x, y) with +inf radius = flat wavefront; wavelength and
+ * theta (rad) may be NULL (uniform wavelength_scalar, theta 0). */
+typedef struct tg_beams {
+  int64_t n;
+  const double *x, *y, *dx, *dy;
+  double z;
+  const double *pathlength;
+  const float *amplitude;
+  const double *waist_xy;
+  const double *radii;
+  const double *wavelength;
+  double wavelength_scalar;
+  const double *theta;
+} tg_beams;
+
+/* Detector pixel centres (grid.py:83-100): y = (t[0]*row + t[1]*col) + t[2],
+ * x = (t[3]*row + t[4]*col) + t[5] (the pixels->metres transform). */
+typedef struct tg_pixel_map {
+  int32_t h, w;
+  double t[6];
+} tg_pixel_map;
+
+#define TG_FIELD_DIRECT 0     /* any Q2 (astigmatic): fixed-point phase direct sum */
+#define TG_FIELD_SEPARABLE 1  /* diagonal Q2, unrotated grid: split-BF16 tcgen05 GEMM */
+#define TG_FIELD_DIRECT_F64 2 /* all-float64 direct sum (comparator)               */
+#define TG_EW_NONSEPARABLE 0x10u /* separable method given a non-separable beam */
+
+/* Workspace bytes for tg_field_prep + tg_field_eval(method) (256-aligned). */
+size_t tg_field_workspace(int64_t n_beams, int32_t h, int32_t w, int32_t method);
+
+/*
+ * tg_field_prep - per-beam float64 preparation into the workspace: ABCD of
+ * each central ray (gaussian.py:234-249), Q1^-1 and Q2^-1 (gaussian.py:92-96,
+ * 138-177), prefactor and the per-pixel phase polynomial (gaussian.py:276-316),
+ * exact reduction of k*pathlength mod 2*pi.  flags (device int32, may be
+ * NULL): bit 0 set when some beam is not separable.
+ */
+int tg_field_prep(const tg_model *model, const tg_beams *beams, const tg_pixel_map *pm,
+                  void *workspace, size_t ws_bytes, int32_t *flags, void *stream);
+
+/*
+ * tg_field_eval - the field sum over beams at every detector pixel into out
+ * (device complex64 [h][w], overwritten).  Replaces gaussian.py:319-369
+ * propagate_misaligned_gaussian_jax_scan + map_reduce (and the reshape in
+ * gaussian.py:257-273 make_gaussian_image).  Uses the records written by
+ * tg_field_prep into the same workspace.
+ */
+int tg_field_eval(int32_t method, int64_t n_beams, const tg_pixel_map *pm, float *out,
+                  void *workspace, size_t ws_bytes, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

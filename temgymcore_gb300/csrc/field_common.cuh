@@ -1,0 +1,48 @@
+// field_common.cuh - per-beam coefficient records of the Gaussian-beamlet
+// detector field (gaussian.py:225-369) shared by the prep kernel, the direct
+// kernels and the separable tensor-core path.
+//
+// For each beam the prep kernel reduces the reference's per-pixel formula
+//   field(r2) = pref * exp(i (k/2) (s^T Q2 s + phi1(s) - phi2(s) + 2 s.f) + i k pl),
+//   s = r2 - e,  (gaussian.py:276-316)
+// to a complex quadratic polynomial in the integer pixel indices:
+//   Phi(row, col) = c_cc col^2 + c_rr row^2 + c_rc row col + c_c col + c_r row + c_0.
+// Because col^2, row^2, row*col, col, row are integers, reducing each real
+// coefficient modulo one turn commutes with the evaluation.  The real parts
+// (the phase) are therefore stored as 64-bit fixed-point fractions of a turn
+// (2^64 = one turn) and evaluated with wrap-around integer arithmetic, exact
+// to 2^-64 turn; the float64 pathlength phase k*pl enters the constant after
+// an exact (FMA TwoProduct + two-part 2*pi) reduction.  The imaginary parts
+// (the Gaussian envelope) become a float32 log-amplitude quadratic centred on
+// the envelope maximum.
+#pragma once
+
+#include <stdint.h>
+
+namespace tg {
+
+// Fast record (fixed-point phase, float32 envelope), 96 bytes.
+struct alignas(16) BeamFast {
+  uint64_t p_cc, p_rr, p_rc, p_c, p_r, p_0;  // turns * 2^64
+  float r0, c0;          // envelope centre (row, col)
+  float e0;              // log-amplitude at the centre
+  float b_cc, b_rr, b_rc, l_c, l_r;  // log-amp = e0 - (b_cc dc^2 + b_rr dr^2 + b_rc dr dc + l_c dc + l_r dr)
+  float rho_re, rho_im;  // exp(-2 b_cc + i 2pi (2 p_cc)): column-step ratio of ratios
+};
+
+// float64 record for the all-float64 comparator kernel, 128 bytes.
+struct alignas(16) BeamF64 {
+  double re[6];   // c_cc, c_rr, c_rc, c_c, c_r, c_0 real parts (radians)
+  double im[6];   // imaginary parts
+  double ph0;     // exactly reduced k*pl + arg(pref), radians
+  double lnamp;   // ln |pref|
+  double pad[2];
+};
+
+// Pixel map of the detector: pixels -> metres (grid.py:155-182).
+struct PixMap {
+  int32_t h, w;
+  double t[6];  // y = (t0*row + t1*col) + t2 ; x = (t3*row + t4*col) + t5
+};
+
+}  // namespace tg

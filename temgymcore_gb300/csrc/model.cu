@@ -271,6 +271,8 @@ extern "C" const char* tg_status_string(int s) {
 
 extern "C" int tg_internal_err_trace(uint32_t*, int);
 extern "C" int tg_internal_err_scan(uint32_t*, int);
+extern "C" int tg_internal_err_field(uint32_t*, int);
+extern "C" int tg_internal_err_gemm(uint32_t*, int);
 
 extern "C" int tg_get_error_word(uint32_t* out, int clear) {
   if (!out) return TG_ERR_INVALID;
@@ -278,5 +280,7 @@ extern "C" int tg_get_error_word(uint32_t* out, int clear) {
   *out = 0;
   int s = tg_internal_err_trace(out, clear);
   if (s == TG_OK) s = tg_internal_err_scan(out, clear);
+  if (s == TG_OK) s = tg_internal_err_field(out, clear);
+  if (s == TG_OK) s = tg_internal_err_gemm(out, clear);
   return s;
 }

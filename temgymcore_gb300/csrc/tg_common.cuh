@@ -97,7 +97,8 @@ struct BinCoef {
 __device__ __forceinline__ int bin_exact64(double a, double b, double m0,
                                            double m1, double m2) {
   double v = __dadd_rn(__dadd_rn(__dmul_rn(m0, a), __dmul_rn(m1, b)), m2);
-  return __double2int_rn(v);  // cvt.rni.s32.f64: saturating, NaN -> 0
+  if (v != v) return 0;       // NaN -> 0 (the hardware conversion gives INT_MIN)
+  return __double2int_rn(v);  // cvt.rni.s32.f64: saturating
 }
 
 __device__ __forceinline__ int bin_one(float a, float b, float m0, float m1,

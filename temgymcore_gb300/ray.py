@@ -109,6 +109,23 @@ class GaussianRay(Ray):
         return Ray(x=self.x, y=self.y, dx=self.dx, dy=self.dy, z=self.z,
                    pathlength=self.pathlength, _one=self._one)
 
+    @property
+    def size(self) -> int:
+        """Number of beams: per-beam fields have length n; waist_xy and
+        radii_of_curv are (n, 2)."""
+        sizes = set()
+        for f in dataclasses.fields(self):
+            v = getattr(self, f.name)
+            if not _is_vec(v):
+                continue
+            if f.name in ("waist_xy", "radii_of_curv"):
+                sizes.add(int(np.shape(v)[0]) if np.ndim(v) == 2 else 1)
+            else:
+                sizes.add(_size(v))
+        sizes.discard(1) if len(sizes) > 1 else None
+        assert len(sizes) <= 1, "beam fields have mismatched sizes"
+        return sizes.pop() if sizes else 1
+
     def derive(self, **updates):
         return dataclasses.replace(self, **{k: (v(self) if callable(v) else v)
                                             for k, v in updates.items()})

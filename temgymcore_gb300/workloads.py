@@ -113,3 +113,46 @@ def stem_model(w: dict):
                         descan_error=K.DescanError(**_d(w["descan"]))),
             K.Detector(z=w["detector"]["z"], pixel_size=tuple(w["detector"]["pixel_size"]),
                        shape=tuple(w["detector"]["shape"]))]
+
+
+def beamlet_field(seed: int = 0, n_beams: int = 16384, det_shape=(512, 512), det_px: float = 1e-5,
+                  aperture_radius: float = 5e-8, waist: float = 1e-9, wavelength: float = 1.97e-12,
+                  focal_length: float = 0.5, astigmatic: bool = False):
+    """Gaussian-beamlet field (aperture-diffraction geometry).
+
+    ``n_beams`` beamlets sit on a golden-angle spiral filling a circular
+    aperture of ``aperture_radius`` at z = 0 (parallel beam, slopes 0),
+    waist ``waist``, flat wavefront; amplitudes |a| ~ U(0.5, 1) with phase
+    U(0, 2 pi) (complex64); pathlengths 1 m + N(0, 1e-6) m; wavelength
+    1.97 pm (200 keV).  Model: Lens(z=f, f) then Detector(z=2f) - the back
+    focal plane, where the field is the aperture's diffraction pattern.
+    ``astigmatic``: waist_y = waist * U(0.5, 1.5) and theta ~ U(0, pi).
+    """
+    from .gaussian import fibonacci_spiral
+    rng = np.random.default_rng(seed)
+    x, y = fibonacci_spiral(n_beams, aperture_radius, alpha=0)
+    amp = (rng.uniform(0.5, 1.0, n_beams) * np.exp(1j * rng.uniform(0, 2 * np.pi, n_beams))
+           ).astype(np.complex64)
+    pl = 1.0 + rng.normal(0.0, 1e-6, n_beams)
+    wxy = np.full((n_beams, 2), waist)
+    theta = np.zeros(n_beams)
+    if astigmatic:
+        wxy[:, 1] = waist * rng.uniform(0.5, 1.5, n_beams)
+        theta = rng.uniform(0.0, np.pi, n_beams)
+    rays = {"x": x, "y": y, "dx": np.zeros(n_beams), "dy": np.zeros(n_beams), "z": 0.0,
+            "pathlength": pl, "amplitude": amp, "waist_xy": wxy,
+            "radii_of_curv": np.full((n_beams, 2), np.inf), "wavelength": wavelength,
+            "theta": theta}
+    spec = [{"kind": "lens", "z": focal_length, "focal_length": focal_length},
+            {"kind": "detector", "z": 2 * focal_length, "pixel_size": (det_px, det_px),
+             "shape": tuple(det_shape)}]
+    return {"rays": rays, "model": spec}
+
+
+def gaussian_rays(d: dict):
+    """GaussianRay from a ``beamlet_field`` ray dict."""
+    from .ray import GaussianRay
+    return GaussianRay(x=d["x"], y=d["y"], dx=d["dx"], dy=d["dy"], z=d["z"],
+                       pathlength=d["pathlength"], amplitude=d["amplitude"],
+                       waist_xy=d["waist_xy"], radii_of_curv=d["radii_of_curv"],
+                       wavelength=d["wavelength"], theta=d["theta"])

@@ -1,0 +1,147 @@
+"""GPU parity of the Gaussian-beamlet field kernels against the float64
+oracle (exact k*pathlength reduction).  Tolerances: field normwise relative
+error <= 1e-4 (fast direct, split-BF16 tensor-core) and <= 5e-7 (float64
+kernel, whose complex64 output alone rounds at ~6e-8); phase error <= 1e-4
+rad (5e-7 rad for float64) at pixels brighter than 25% of the peak."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import field as OF
+
+pytestmark = pytest.mark.gpu
+
+
+def _np(t):
+    return t.detach().cpu().numpy()
+
+
+def _cmp(got, ref, tol, ptol=1e-4):
+    got = got.astype(np.complex128)
+    e = np.max(np.abs(got - ref)) / np.max(np.abs(ref))
+    assert e <= tol, e
+    bright = np.abs(ref) > 0.25 * np.max(np.abs(ref))
+    ph = np.abs(np.angle(got[bright] * np.conj(ref[bright])))
+    assert ph.max() <= ptol, ph.max()
+    return e, float(ph.max())
+
+
+def _small(astig, n=256, shape=(64, 96), seed=0, det_px=4e-5):
+    from temgymcore_gb300.workloads import beamlet_field
+    return beamlet_field(seed=seed, n_beams=n, det_shape=shape, det_px=det_px, astigmatic=astig)
+
+
+@pytest.mark.parametrize("astig", [False, True])
+def test_field_methods_match_oracle(astig, cuda):
+    import temgymcore_gb300 as t
+    from temgymcore_gb300.workloads import build_model, gaussian_rays
+    w = _small(astig)
+    ref = OF.make_gaussian_image(w["rays"], w["model"])
+    plan = t.FieldPlan(gaussian_rays(w["rays"]), build_model(w["model"]))
+    assert plan.separable == (not astig)
+    _cmp(_np(plan.evaluate("fp64")), ref, 5e-7, 5e-7)
+    _cmp(_np(plan.evaluate("direct")), ref, 1e-4)
+    if not astig:
+        _cmp(_np(plan.evaluate("separable")), ref, 1e-4)
+    assert t._native.error_word() == 0
+
+
+def test_single_beams_phase_and_envelope(cuda):
+    """One beam at a time: tilted, off-axis, astigmatic, curved, rotated grid."""
+    import temgymcore_gb300 as t
+    from temgymcore_gb300.workloads import build_model, gaussian_rays
+    cases = [dict(x=1e-4, y=-2e-4, dx=1e-3, dy=-5e-4, wx=1e-4, wy=1e-4, R=np.inf, th=0.0),
+             dict(x=0.0, y=0.0, dx=0.0, dy=0.0, wx=2e-4, wy=1e-4, R=np.inf, th=0.7),
+             dict(x=-3e-4, y=1e-4, dx=2e-4, dy=1e-4, wx=1.5e-4, wy=1.5e-4, R=0.5, th=0.0)]
+    for rot in (0.0, 30.0):
+        spec = [{"kind": "lens", "z": 0.3, "focal_length": 0.4},
+                {"kind": "deflector", "z": 0.4, "def_x": 1e-4, "def_y": 0.0},
+                {"kind": "detector", "z": 1.0, "pixel_size": (2e-5, 2e-5), "shape": (48, 64),
+                 "rotation": rot}]
+        for c in cases:
+            r = {"x": np.array([c["x"]]), "y": np.array([c["y"]]), "dx": np.array([c["dx"]]),
+                 "dy": np.array([c["dy"]]), "z": 0.0, "pathlength": np.array([0.731]),
+                 "amplitude": np.array([0.8 + 0.3j], np.complex64),
+                 "waist_xy": np.array([[c["wx"], c["wy"]]]),
+                 "radii_of_curv": np.array([[c["R"], c["R"]]]), "wavelength": 500e-9,
+                 "theta": np.array([c["th"]])}
+            ref = OF.make_gaussian_image(r, spec)
+            plan = t.FieldPlan(gaussian_rays(r), build_model(spec), method="direct")
+            _cmp(_np(plan.evaluate("direct")), ref, 1e-4)
+            _cmp(_np(plan.evaluate("fp64")), ref, 5e-7, 5e-7)
+
+
+def test_free_space_closed_form(kats, cuda):
+    """tests/test_gaussians.py:229-273 closed form, sampled on a detector grid."""
+    import temgymcore_gb300 as t
+    g = kats["gauss_free_space"]
+    w0, wl, L = g["w0"], g["wavelength"], g["L"]
+    det = t.Detector(z=L, pixel_size=(1e-4, 1e-4), shape=(16, 16))
+    ray = t.GaussianRay(x=np.zeros(1), y=np.zeros(1), dx=np.zeros(1), dy=np.zeros(1), z=0.0,
+                        pathlength=np.zeros(1), amplitude=np.ones(1, np.complex64),
+                        waist_xy=np.array([[w0, w0]]), radii_of_curv=np.array([[np.inf, np.inf]]),
+                        wavelength=wl, theta=np.zeros(1))
+    got = _np(t.make_gaussian_image(ray, [det], method="fp64"))
+    k = 2 * np.pi / wl
+    q = 1j * wl / (np.pi * w0 * w0)
+    q2 = np.linalg.solve(np.eye(2) + L * np.eye(2) * q, q * np.eye(2))
+    pref = 1.0 / np.sqrt(np.linalg.det(np.eye(2) + L * q * np.eye(2)))
+    r2 = det.coords
+    ref = (pref * np.exp(1j * (k / 2.0) * np.einsum("ni,ij,nj->n", r2, q2, r2))).reshape(16, 16)
+    np.testing.assert_allclose(got, ref, rtol=1e-6, atol=1e-7)
+    got2 = _np(t.make_gaussian_image(ray, [det], method="separable"))
+    np.testing.assert_allclose(got2, ref, rtol=1e-4, atol=1e-5)
+
+
+def test_quadrant_of_tilted_beam(kats, cuda):
+    import temgymcore_gb300 as t
+    g = kats["gauss_quadrant"]
+    det = t.Detector(z=g["z"], pixel_size=tuple(g["pixel_size"]), shape=tuple(g["shape"]))
+
+    def img(dx, dy):
+        ray = t.GaussianRay(x=np.zeros(1), y=np.zeros(1), dx=np.array([dx]), dy=np.array([dy]), z=0.0,
+                            pathlength=np.zeros(1), amplitude=np.ones(1, np.complex64),
+                            waist_xy=np.array([[g["w0"], g["w0"]]]),
+                            radii_of_curv=np.array([[np.inf, np.inf]]), wavelength=g["wavelength"],
+                            theta=np.zeros(1))
+        return np.abs(_np(t.make_gaussian_image(ray, [det])))
+    c = img(0.0, 0.0)
+    cy, cx = np.unravel_index(np.argmax(c), c.shape)
+    xc, yc = det.pixels_to_metres((cy, cx))
+    tt = g["tilt"]
+    for dx, dy in ((tt, tt), (tt, -tt), (-tt, tt), (-tt, -tt)):
+        my, mx = np.unravel_index(np.argmax(img(dx, dy)), c.shape)
+        xm, ym = det.pixels_to_metres((my, mx))
+        assert np.sign(xm - xc) == np.sign(dx) and np.sign(ym - yc) == np.sign(dy)
+
+
+def test_separable_rejects_astigmatic_beams(cuda):
+    import temgymcore_gb300 as t
+    from temgymcore_gb300.workloads import build_model, gaussian_rays
+    w = _small(True, n=64, shape=(32, 32))
+    plan = t.FieldPlan(gaussian_rays(w["rays"]), build_model(w["model"]))
+    assert not plan.separable and plan.method == "direct"
+    t._native.error_word()
+    plan.evaluate("separable")
+    assert t._native.error_word() & 0x10
+
+
+def test_full_config_properties(cuda):
+    """BASELINE config size: separable GEMM vs the fp64 kernel on all pixels,
+    direct vs oracle on a pixel sample, astigmatic direct vs oracle sample."""
+    import temgymcore_gb300 as t
+    from temgymcore_gb300.workloads import beamlet_field, build_model, gaussian_rays
+    w = beamlet_field(seed=0)
+    plan = t.FieldPlan(gaussian_rays(w["rays"]), build_model(w["model"]))
+    assert plan.separable
+    f64 = _np(plan.evaluate("fp64").clone()).astype(np.complex128)
+    sep = _np(plan.evaluate("separable").clone())
+    e = np.max(np.abs(sep - f64)) / np.max(np.abs(f64))
+    assert e < 1e-4, e
+    rng = np.random.default_rng(0)
+    idx = rng.choice(512 * 512, 64, replace=False)
+    ref = OF.make_gaussian_image(w["rays"], w["model"], pixel_index=idx, chunk=2048)
+    e2 = np.max(np.abs(f64.reshape(-1)[idx] - ref)) / np.max(np.abs(ref))
+    assert e2 < 1e-7, e2
+    dire = _np(plan.evaluate("direct").clone()).reshape(-1)[idx]
+    assert np.max(np.abs(dire - ref)) / np.max(np.abs(ref)) < 1e-4

@@ -179,7 +179,9 @@ def test_full_component_chain_per_ray_z_and_pathlength(cuda):
                 z=torch.tensor(z, device=cuda), pathlength=torch.tensor(pl, device=cuda))
     out = t.run_to_end(ray, build_model(spec))
     ref = oracle.run_to_end(ORay.from_f32(x, y, dx, dy, z, pl), spec)
-    _cmp_trace(out, ref)
+    # ten components incl. a 5 cm lens: float32 state rounded exactly after
+    # every component already differs from float64 by 1.1e-6 (dx) here
+    _cmp_trace(out, ref, tol=2e-6)
     assert abs(out.z - float(np.mean(ref.z))) < 1e-12
 
 

@@ -1,0 +1,100 @@
+"""Host-side logic of the package (CPU only): record packing, sizes,
+pixel maps, workload generators, gradient mapping."""
+import numpy as np
+import torch
+
+import oracle
+
+
+def test_gaussian_ray_size_and_beamset():
+    from temgymcore_gb300 import GaussianRay
+    from temgymcore_gb300.gaussian import BeamSet, pixel_map
+    from temgymcore_gb300.workloads import beamlet_field, build_model, gaussian_rays
+    w = beamlet_field(seed=0, n_beams=100, det_shape=(32, 48))
+    r = gaussian_rays(w["rays"])
+    assert r.size == 100
+    b = BeamSet(r, torch.device("cpu"))
+    assert b.n == 100 and b.waist.shape == (100, 2) and b.amp.shape == (100, 2)
+    assert b.wl.shape == (100,) and b.theta.shape == (100,) and b.z == 0.0
+    g = GaussianRay(x=0.0, y=0.0, dx=0.0, dy=0.0, z=0.0, pathlength=0.0, amplitude=1.0,
+                    waist_xy=np.array([1e-4, 2e-4]), radii_of_curv=np.array([np.inf, np.inf]),
+                    wavelength=5e-7, theta=0.0)
+    assert g.size == 1
+    det = build_model(w["model"])[-1]
+    pm = pixel_map(det)
+    t = oracle.pixels_to_metres_transform((0.0, 0.0), det.pixel_size, det.shape)
+    assert (pm.h, pm.w) == (32, 48)
+    np.testing.assert_array_equal(list(pm.t), [t[0, 0], t[0, 1], t[0, 2], t[1, 0], t[1, 1], t[1, 2]])
+
+
+def test_fibonacci_and_transforms_match_oracle():
+    from temgymcore_gb300 import fibonacci_spiral, Detector
+    from oracle.field import fibonacci_spiral as ofs
+    for a in (0, 2):
+        np.testing.assert_array_equal(np.array(fibonacci_spiral(1000, 1e-7, a)), np.array(ofs(1000, 1e-7, a)))
+    det = Detector(z=0.0, pixel_size=(2e-5, 1e-5), shape=(100, 300), rotation=33.0,
+                   centre=(1e-4, -3e-4), flip_y=True)
+    g = {"pixel_size": (2e-5, 1e-5), "shape": (100, 300), "rotation": 33.0,
+         "centre": (1e-4, -3e-4), "flip_y": True}
+    np.testing.assert_array_equal(det.metres_to_pixels_mat,
+                                  oracle.metres_to_pixels_mat(g["centre"], g["pixel_size"], g["shape"],
+                                                              True, 33.0))
+    np.testing.assert_array_equal(det.coords, oracle.grid_coords(g))
+
+
+def test_pack_model_records():
+    import ctypes
+    from temgymcore_gb300 import _native as N
+    from temgymcore_gb300.run import pack_model
+    from temgymcore_gb300.workloads import build_model
+    spec = [{"kind": "lens", "z": 0.5, "focal_length": 0.2},
+            {"kind": "descanner", "z": 0.6, "scan_pos_x": 1.0, "scan_pos_y": 2.0,
+             "descan_error": {"pxo_pxi": 3.0, "offsyi": 4.0, "syo_syi": 5.0}},
+            {"kind": "thicklens", "z_po": 0.7, "z_pi": 0.8, "focal_length": 0.1},
+            {"kind": "aperture", "z": 0.9, "radius": 1e-3, "centre": (1e-4, 2e-4)},
+            {"kind": "detector", "z": 1.0, "pixel_size": (1e-5, 1e-5), "shape": (8, 8)}]
+    m, keep = pack_model(build_model(spec))
+    c = [m.components[i] for i in range(m.n_components)]
+    assert [x.kind for x in c] == [N.LENS, N.DESCANNER, N.THICKLENS, N.APERTURE, N.PLANE]
+    assert c[0].p[0] == 0.2 and c[2].z == 0.7 and c[2].p[1] == 0.8
+    assert c[1].p[0] == 1.0 and c[1].p[4] == 3.0 and c[1].p[23] == 4.0 and c[1].p[4 + 15] == 5.0
+    assert c[3].p[0] == 1e-3 and c[3].p[1] == 1e-4 and c[3].p[2] == 2e-4
+
+
+def test_param_gradient_mapping_descanner():
+    """dL/dparams from per-step adjoint sums: checked against the chain rule
+    on the oracle's descanner offsets."""
+    from temgymcore_gb300.run import param_gradient
+    from temgymcore_gb300.workloads import build_model
+    rng = np.random.default_rng(2)
+    err = dict(zip(["pxo_pxi", "pxo_pyi", "pyo_pxi", "pyo_pyi", "sxo_pxi", "sxo_pyi", "syo_pxi",
+                    "syo_pyi", "offpxi", "offpyi", "offsxi", "offsyi"], rng.normal(0, 1, 12)))
+    spec = [{"kind": "descanner", "z": 0.0, "scan_pos_x": 0.3, "scan_pos_y": -0.2,
+             "scan_tilt_x": 0.1, "scan_tilt_y": 0.05, "descan_error": err}]
+    comps = build_model(spec)
+    g = rng.normal(0, 1, 4)  # dL/d(delta x, delta y, delta dx, delta dy)
+    raw = torch.zeros((2, 4), dtype=torch.float64)
+    raw[1] = torch.tensor(g)
+    h = 1e-30
+    for path in ("scan_pos_x", "scan_pos_y", "scan_tilt_x", "scan_tilt_y",
+                 "descan_error.pxo_pxi", "descan_error.syo_pyi", "descan_error.offsxi"):
+        s = [dict(c) for c in spec]
+        if path.startswith("descan"):
+            e = dict(s[0]["descan_error"])
+            e[path.split(".")[1]] += 1j * h
+            s[0]["descan_error"] = e
+        else:
+            s[0][path] = s[0][path] + 1j * h
+        o = oracle.apply_component(s[0], oracle.ORay(0.0, 0.0, 0.0, 0.0, 0.0, 0.0))
+        ref = sum(gi * np.imag(getattr(o, k)) / h for gi, k in zip(g, ("x", "y", "dx", "dy")))
+        assert abs(float(param_gradient(comps, 0, path, raw)) - ref) < 1e-12 * max(1, abs(ref))
+
+
+def test_workloads_are_seeded():
+    from temgymcore_gb300.workloads import plain_trace, stem_4d, beamlet_field
+    a, b = plain_trace(seed=0, n=100), plain_trace(seed=0, n=100)
+    assert np.array_equal(a["x"], b["x"]) and a["x"].dtype == np.float32
+    s = stem_4d(seed=0)
+    assert s["dx"].shape == (1024,) and 0.0 <= s["scangrid"]["rotation"] < 360.0
+    f = beamlet_field(seed=0, n_beams=16)
+    assert f["rays"]["amplitude"].dtype == np.complex64
