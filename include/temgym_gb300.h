@@ -5,8 +5,7 @@
  * The reference (temgym_core, pure Python on JAX) has no FFI: its "plugin
  * API" is Python duck typing.  Each entry point below replaces a Python call
  * site of the reference (cited per function); the Python package
- * temgymcore_gb300 binds them with ctypes (see INTEGRATION.md for the
- * binding a temgym_core maintainer would add).
+ * temgymcore_gb300 binds them with ctypes.
  *
  * Conventions
  *   - Every function returns an int status: TG_OK (0) or a negative TG_ERR_*.
@@ -158,7 +157,9 @@ int tg_abcd_compose(const tg_model *model, const double central[5],
  *          pointers may be NULL; gin->pathlength receives float64).
  *   raw:   device float64 [n_steps][4], n_steps = 2*n_components, ADDED to:
  *          per step the ray-summed adjoint quantities from which parameter
- *          gradients follow ("adjoint").
+ *          gradients follow: propagator dL/dd; lens dL/df; scanner and
+ *          descanner dL/d(offset x, y, dx, dy); deflector dL/d(def_x, def_y);
+ *          biprism dL/d(def_x); rotator dL/d(angle in radians).
  *   workspace: device scratch of tg_trace_vjp_workspace(n) bytes.
  */
 size_t tg_trace_vjp_workspace(int64_t n, const tg_model *model);

@@ -127,7 +127,7 @@ def test_separable_rejects_astigmatic_beams(cuda):
 
 
 def test_full_config_properties(cuda):
-    """BASELINE config size: separable GEMM vs the fp64 kernel on all pixels,
+    """Full size (16,384 beams, 512 x 512): separable GEMM vs the fp64 kernel on all pixels,
     direct vs oracle on a pixel sample, astigmatic direct vs oracle sample."""
     import temgymcore_gb300 as t
     from temgymcore_gb300.workloads import beamlet_field, build_model, gaussian_rays
