@@ -245,6 +245,26 @@ int tg_field_prep(const tg_model *model, const tg_beams *beams, const tg_pixel_m
 int tg_field_eval(int32_t method, int64_t n_beams, const tg_pixel_map *pm, float *out,
                   void *workspace, size_t ws_bytes, void *stream);
 
+/*
+ * tg_field_direct_noalloc - tg_field_prep + tg_field_eval(TG_FIELD_DIRECT)
+ * in one call that allocates nothing.  No counterpart in the reference: it
+ * exists for callers that cannot call cudaMalloc (an allocator owned by
+ * another framework, a pre-sized memory pool, a host that forbids device
+ * allocation after start-up).  Its scratch (beam records + partial images) is
+ * a fixed 32 MiB array inside the library, held by every GPU that loads the
+ * library until the process exits.  Limits: at most 32768 beams, and the
+ * records plus one h*w complex64 partial image must fit the 32 MiB (about
+ * 3.2 million pixels at 32768 beams, 4.1 million with few beams); larger
+ * requests return
+ * TG_ERR_TOO_LARGE.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress); make that first call before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU (other
+ * streams, other threads) race and must be serialised by the caller.
+ * out: device complex64 [h][w], overwritten.
+ */
+int tg_field_direct_noalloc(const tg_model *model, const tg_beams *beams,
+                            const tg_pixel_map *pm, float *out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

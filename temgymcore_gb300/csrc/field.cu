@@ -751,3 +751,77 @@ extern "C" int tg_field_eval(int32_t method, int64_t n_beams, const tg_pixel_map
   }
   return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
 }
+
+// ---------------------------------------------------------------- no-alloc
+// tg_field_direct_noalloc: the direct field sum for callers that cannot
+// allocate device memory.  Its scratch (beam records and per-chunk partial
+// images) lives in one file-scope device array of fixed size, so the call
+// itself never allocates.  Every GPU that loads this library holds the array
+// until the process exits.
+#include <mutex>
+
+namespace tg {
+
+constexpr size_t kNoAllocBytes = (size_t)32 << 20;  // 32 MiB per device
+constexpr int64_t kNoAllocMaxBeams = 32768;
+static __device__ __align__(256) unsigned char g_field_noalloc[kNoAllocBytes];
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_addr[256];  // device address of g_field_noalloc, per device ordinal
+
+// Device address of the scratch array on the current device.  Host code may
+// not use the symbol itself as a pointer (it is a host-side stand-in), so the
+// address is fetched once per device with that device current.
+static int noalloc_scratch(void** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) return TG_ERR_CUDA;
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_field_noalloc) != cudaSuccess || !p) return TG_ERR_CUDA;
+    g_noalloc_addr[dev] = p;
+  }
+  *out = g_noalloc_addr[dev];
+  return TG_OK;
+}
+
+}  // namespace tg
+
+extern "C" int tg_field_direct_noalloc(const tg_model* model, const tg_beams* beams,
+                                       const tg_pixel_map* pm, float* out, void* stream) {
+  if (!model || !beams || !pm) return TG_ERR_INVALID;
+  if (beams->n < 0 || pm->h <= 0 || pm->w <= 0) return TG_ERR_INVALID;
+  if (beams->n > kNoAllocMaxBeams) return TG_ERR_TOO_LARGE;
+  const FieldLayout L = field_layout(beams->n, pm->h, pm->w, TG_FIELD_DIRECT);
+  const size_t per_chunk = (size_t)pm->h * pm->w * sizeof(float2);
+  if (L.part > kNoAllocBytes || kNoAllocBytes - L.part < per_chunk) return TG_ERR_TOO_LARGE;
+  if (!out) return TG_ERR_INVALID;
+  void* scratch = nullptr;
+  int st = noalloc_scratch(&scratch);
+  if (st != TG_OK) return st;
+  st = tg_field_prep(model, beams, pm, scratch, L.part, nullptr, stream);
+  if (st != TG_OK) return st;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  const int64_t n = beams->n, npx = (int64_t)pm->h * pm->w;
+  float2* o = reinterpret_cast<float2*>(out);
+  if (n == 0)
+    return cudaMemsetAsync(out, 0, (size_t)npx * sizeof(float2), s) == cudaSuccess ? TG_OK : TG_ERR_CUDA;
+  int64_t chunks = L.chunks;
+  const int64_t fit = (int64_t)((kNoAllocBytes - L.part) / per_chunk);
+  if (chunks > fit) chunks = fit;
+  char* ws = reinterpret_cast<char*>(scratch);
+  DirArgs A;
+  A.beams = reinterpret_cast<const BeamFast*>(ws + L.fast);
+  A.n = n;
+  A.chunk = ((n + chunks - 1) / chunks + kBeamBatch - 1) / kBeamBatch * kBeamBatch;
+  A.h = pm->h;
+  A.w = pm->w;
+  A.tile_rows = kDirTileRows;
+  A.strips_x = kDirStrips;
+  A.out = reinterpret_cast<float2*>(ws + L.part);  // every in-range pixel is overwritten
+  const int tiles = ((pm->h + kDirTileRows - 1) / kDirTileRows) *
+                    ((pm->w + kDirStrips * kDirL - 1) / (kDirStrips * kDirL));
+  const int used = (int)((n + A.chunk - 1) / A.chunk);
+  k_field_direct<kDirL><<<dim3(tiles, used), kDirThreads, 0, s>>>(A);
+  k_field_reduce<<<(int)((npx + 255) / 256), 256, 0, s>>>(A.out, used, npx, o);
+  return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
+}

@@ -1,0 +1,77 @@
+"""tg_field_direct_noalloc: the direct beamlet-field sum for callers that
+cannot allocate device memory (their allocator belongs to another framework,
+or the device is pre-sized and allocation after start-up is not allowed).
+The entry point keeps its scratch in a fixed array inside the library.
+
+Called through the C ABI twice in a row; each result must match the regular
+entry points (tg_field_prep + tg_field_eval, direct method) to the direct
+kernel's tolerance, and requests beyond the stated limits are rejected.
+This file sorts last so a failure here does not hide any other test."""
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5  # normwise relative; the two paths only differ in beam chunking
+
+
+def _lib():
+    from temgymcore_gb300 import _native as N
+    from temgymcore_gb300 import gaussian as G
+    N.register("tg_field_direct_noalloc", C.c_int,
+               [C.POINTER(N.TgModel), C.POINTER(G.TgBeams), C.POINTER(G.TgPixelMap), C.c_void_p,
+                C.c_void_p])
+    return N.lib()
+
+
+def test_noalloc_matches_regular_direct_path(cuda):
+    import temgymcore_gb300 as t
+    from temgymcore_gb300 import _native as N
+    from temgymcore_gb300.gaussian import BeamSet, pixel_map
+    from temgymcore_gb300.run import pack_model
+    from temgymcore_gb300.workloads import beamlet_field, build_model, gaussian_rays
+    lib = _lib()
+    w = beamlet_field(seed=3, n_beams=3000, det_shape=(96, 160), det_px=3e-5, astigmatic=True)
+    rays, comps = gaussian_rays(w["rays"]), build_model(w["model"])
+    ref = t.FieldPlan(rays, comps, method="direct").evaluate("direct").clone()
+    beams = BeamSet(rays, cuda)
+    pm = pixel_map(comps[-1])
+    m, keep = pack_model(comps)
+    outs = []
+    for _ in range(2):
+        o = torch.full((96, 160), complex(np.nan, np.nan), dtype=torch.complex64, device=cuda)
+        st = lib.tg_field_direct_noalloc(C.byref(m), C.byref(beams.struct()), C.byref(pm),
+                                         torch.view_as_real(o).data_ptr(), N.stream_ptr())
+        assert st == 0, st
+        outs.append(o)
+    torch.cuda.synchronize()
+    r = ref.cpu().numpy()
+    for o in outs:
+        g = o.cpu().numpy()
+        assert np.isfinite(g).all()
+        assert np.max(np.abs(g - r)) / np.max(np.abs(r)) <= TOL
+    assert torch.equal(outs[0], outs[1])
+    assert N.error_word() == 0
+    del keep
+
+
+def test_noalloc_rejects_sizes_beyond_its_limits(cuda):
+    from temgymcore_gb300 import _native as N
+    from temgymcore_gb300 import gaussian as G
+    lib = _lib()
+    m = N.TgModel()
+    m.n_components = 0
+    b = G.TgBeams()
+    b.n = 32769  # beyond the 32768-beam maximum
+    pm = G.TgPixelMap()
+    pm.h, pm.w = 64, 64
+    out = torch.empty((64, 64), dtype=torch.complex64, device=cuda)
+    assert lib.tg_field_direct_noalloc(C.byref(m), C.byref(b), C.byref(pm),
+                                       torch.view_as_real(out).data_ptr(), None) == -5
+    b.n = 16
+    pm.h, pm.w = 4096, 4096  # one partial image alone exceeds the scratch
+    assert lib.tg_field_direct_noalloc(C.byref(m), C.byref(b), C.byref(pm),
+                                       torch.view_as_real(out).data_ptr(), None) == -5
