@@ -316,6 +316,117 @@ def secondary_field(torch, dev, hbm, bf16):
     return res
 
 
+def secondary_fit(torch, dev):
+    """Adjoint fit: 32x32 scan x 1,024 rays, 21 parameters; fused loss +
+    gradient + Adam replayed as a CUDA graph, 200 steps; versus the plain
+    per-model path (one generic forward + adjoint launch pair per probe)."""
+    import ctypes as C
+
+    import temgymcore_gb300 as t
+    from temgymcore_gb300 import _native as N
+    from temgymcore_gb300.fit import StemFit
+    from temgymcore_gb300.run import _rays_struct, pack_model
+    from temgymcore_gb300.workloads import stem_fit
+    w = stem_fit(seed=0)
+    ray = t.Ray(x=w["x"], y=w["y"], dx=w["dx"], dy=w["dy"], z=0.0, pathlength=0.0)
+    fit = StemFit(ray, w["rows"], w["cols"], w["gap"], w["theta0"])
+    fit.set_targets(w["theta_true"])
+    sc = np.abs(w["theta0"])
+    sc[sc < 1e-2] = 1e-3
+    fit.scale.copy_(torch.as_tensor(sc))
+    n_probes, n = fit.n_probes, fit.n
+    ms_lg = _time(torch, fit.loss_grad, 50)
+    fit.capture(1e-3)
+    a, b = _events(torch)
+    l0 = float(fit.loss_grad()[0])
+    torch.cuda.synchronize()
+    a.record()
+    for _ in range(200):
+        fit.graph.replay()
+    b.record()
+    torch.cuda.synchronize()
+    ms_step = a.elapsed_time(b) / 200
+    l1 = float(fit.loss_grad()[0])
+    th = fit.theta.cpu().numpy()
+    rel = np.abs(th[:3] - w["theta_true"][:3]) / np.abs(w["theta_true"][:3])
+    # plain per-model path on a sample of probes: tg_trace_fwd + residual + tg_trace_vjp
+    sample = 64
+    sp = t.scan_positions(fit.model_at(w["theta0"])[1])
+    models = [pack_model(fit.model_at(w["theta0"], *sp[p])) for p in range(sample)]
+    xs = [as_t.contiguous() for as_t in (fit.x, fit.y, fit.dx, fit.dy)]
+    outs = [torch.empty(n, dtype=torch.float32, device=dev) for _ in range(4)]
+    opl = torch.empty(n, dtype=torch.float64, device=dev)
+    g = [torch.empty(n, dtype=torch.float32, device=dev) for _ in range(4)]
+    ws = torch.empty(1 << 20, dtype=torch.uint8, device=dev)
+    raw = torch.zeros((12, 4), dtype=torch.float64, device=dev)
+    rin = _rays_struct(n, *xs, None, 0.0, None, 0.0)
+    rout = _rays_struct(n, *outs, None, 0.0, opl, 0.0)
+    gout = _rays_struct(n, *g, None, 0.0, None, 0.0)
+    lib = N.lib()
+
+    def plain():
+        for p in range(sample):
+            m, _ = models[p]
+            lib.tg_trace_fwd(C.byref(m), C.byref(rin), C.byref(rout), None, None, None, None, None, 0,
+                             N.stream_ptr())
+            torch.sub(outs[0], fit.tx[p], out=g[0]).mul_(2.0)
+            torch.sub(outs[1], fit.ty[p], out=g[1]).mul_(2.0)
+            g[2].zero_()
+            g[3].zero_()
+            lib.tg_trace_vjp(C.byref(m), C.byref(rin), C.byref(gout), None, raw.data_ptr(), ws.data_ptr(),
+                             ws.numel(), N.stream_ptr())
+    ms_plain = _time(torch, plain, 3) * n_probes / sample
+    return {"workload": "adjoint fit: 32x32 scan x 1,024 rays (1,048,576 rays), 21 parameters, "
+                        "loss = sum of squared detector residuals",
+            "loss_grad_ms": ms_lg, "adam_step_graph_ms": ms_step,
+            "grad_evals_per_s": 1e3 / ms_step,
+            "ray_component_steps_per_s": n_probes * n * 5 / (ms_step * 1e-3),
+            "achieved_gbs": n_probes * n * 8 / (ms_step * 1e-3) / 1e9,
+            "loss_before_after_200": [l0, l1], "rel_err_f_defocus_cl": rel.tolist(),
+            "plain_per_probe_path_ms_per_grad_eval": ms_plain,
+            "speedup_vs_plain_per_probe": ms_plain / ms_step}
+
+
+def run_only(args):
+    """One workload alone (for profiler captures): W warm-up + K timed calls."""
+    import torch
+
+    import temgymcore_gb300 as t
+    dev = torch.device("cuda", torch.cuda.current_device())
+    if args.only.startswith("field"):
+        from temgymcore_gb300.workloads import beamlet_field, build_model, gaussian_rays
+        beams = args.beams or 16384
+        w = beamlet_field(seed=0, n_beams=beams, astigmatic=args.only == "field-astig")
+        plan = t.FieldPlan(gaussian_rays(w["rays"]), build_model(w["model"]))
+        meth = {"field-separable": "separable", "field-direct": "direct", "field-astig": "direct",
+                "field-fp64": "fp64"}[args.only]
+        fn = lambda: plan.evaluate(meth)  # noqa: E731
+    elif args.only == "fit":
+        from temgymcore_gb300.fit import StemFit
+        from temgymcore_gb300.workloads import stem_fit
+        w = stem_fit(seed=0)
+        fit = StemFit(t.Ray(x=w["x"], y=w["y"], dx=w["dx"], dy=w["dy"], z=0.0, pathlength=0.0),
+                      w["rows"], w["cols"], w["gap"], w["theta0"])
+        fit.set_targets(w["theta_true"])
+        fn = fit.loss_grad
+    elif args.only == "plain":
+        from temgymcore_gb300.workloads import build_model, plain_trace
+        w = plain_trace(seed=0, n=args.rays or 65536)
+        model = build_model(w["model"])
+        ray = t.Ray(x=torch.tensor(w["x"], device=dev), y=torch.tensor(w["y"], device=dev),
+                    dx=torch.tensor(w["dx"], device=dev), dy=torch.tensor(w["dy"], device=dev),
+                    z=0.0, pathlength=0.0)
+        acc = torch.zeros((256, 256), dtype=torch.int64, device=dev)
+        fn = lambda: t.trace_to_image(ray, model, acc=acc)  # noqa: E731
+    else:
+        raise SystemExit(f"unknown --only {args.only}")
+    for _ in range(args.warmup):
+        fn()
+    ms = _time(torch, fn, args.steps)
+    print(json.dumps({"only": args.only, "ms_per_call": ms, "steps": args.steps,
+                      "error_word": t._native.error_word()}))
+
+
 def run_gpu(args, world, rank, local):
     import torch
 
@@ -401,6 +512,10 @@ def run_gpu(args, world, rank, local):
             secondary["beamlet_field"] = secondary_field(torch, dev, hbm, bf16)
         except Exception as e:
             secondary["beamlet_field"] = {"error": repr(e)}
+        try:
+            secondary["adjoint_fit"] = secondary_fit(torch, dev)
+        except Exception as e:
+            secondary["adjoint_fit"] = {"error": repr(e)}
     cpu = cpu_baseline() if (rank == 0 and world == 1) else None
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -427,11 +542,19 @@ def main():
                     help="smaller scan for profiling captures (default 64 64)")
     ap.add_argument("--headline-only", action="store_true",
                     help="skip the secondary workloads, e2e and CPU baseline")
+    ap.add_argument("--only", default=None,
+                    help="profile one workload alone: field-separable, field-direct, field-astig, "
+                         "field-fp64, fit, plain")
+    ap.add_argument("--beams", type=int, default=None)
+    ap.add_argument("--rays", type=int, default=None)
     args = ap.parse_args()
     if args.scan:
         global SCAN
         SCAN = tuple(args.scan)
     world, rank, local = _setup_dist(args)
+    if args.only:
+        run_only(args)
+        return
     if args.impl == "reference":
         run_reference(args, world, rank)
     else:

@@ -192,6 +192,48 @@ typedef struct tg_scan {
 int tg_scan_hist(const tg_model *model, const tg_rays *bundle, const tg_scan *scan,
                  const tg_grid *grid, int32_t *hist, float *probe_xy, void *stream);
 
+/* ---- 4D-STEM calibration fit (device-resident parameters) -------------- */
+/* Model: bundle at z = 0 -> Scanner + Descanner at z = defocus with the
+ * probe's scan position (ScanGrid of rows x cols, centre 0) -> Lens(f) at
+ * z = defocus + lens_gap -> Detector at z = defocus + camera_length.
+ * theta (device float64 [21]): f, defocus, camera_length, scan rotation
+ * (degrees), scan step, then the 4x4 descan matrix M row-major (rows x, y,
+ * dx, dy; columns scan x, scan y, tilt x, tilt y).  Probe p sits at scan
+ * pixel (p / cols, p % cols). */
+typedef struct tg_stem_fit {
+  int32_t n_rays, rows, cols;
+  const float *x, *y, *dx, *dy;      /* device bundle [n_rays] */
+  const float *target_x, *target_y;  /* device [rows*cols][n_rays] */
+  double lens_gap;
+} tg_stem_fit;
+
+/* Detector positions of every (probe, ray) at theta (device float32
+ * [rows*cols][n_rays] each).  Replaces the per-probe run_to_end loop. */
+int tg_stem_fit_forward(const tg_stem_fit *cfg, const double *theta, float *det_x,
+                        float *det_y, void *stream);
+
+/* Workspace bytes of tg_stem_fit_loss_grad. */
+size_t tg_stem_fit_workspace(int32_t n_probes);
+
+/*
+ * tg_stem_fit_loss_grad - out (device float64 [22]): out[0] = sum over probes
+ * and rays of the squared detector-position residual, out[1..21] = d out[0] /
+ * d theta.  One fused forward + adjoint pass per ray, deterministic
+ * reductions.  Replaces jax.value_and_grad of a loss over run_to_end
+ * (README.md:113-160).
+ */
+int tg_stem_fit_loss_grad(const tg_stem_fit *cfg, const double *theta, double *out,
+                          void *workspace, size_t ws_bytes, void *stream);
+
+/* One Adam update of theta (device float64 [n], n <= 1024) from grad; m, v
+ * (device float64 [n]) and the step counter t (device int64) persist across
+ * calls so the update replays inside a CUDA graph.  scale (optional, device
+ * float64 [n]) runs Adam in units of scale[i]; mask (optional, device uint8)
+ * freezes entries with 0. */
+int tg_adam_step(double *theta, const double *grad, double *m, double *v, int64_t *t, int32_t n,
+                 double lr, double beta1, double beta2, double eps, const double *scale,
+                 const uint8_t *mask, void *stream);
+
 /* ---- Gaussian-beamlet detector field ----------------------------------- */
 /* Beamlets (GaussianRay, gaussian.py:113-177): central rays and beam shape,
  * all device arrays.  amplitude is complex64 (re, im pairs); waist_xy and

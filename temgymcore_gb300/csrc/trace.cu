@@ -62,6 +62,7 @@ k_trace_fwd(const __grid_constant__ Program P, const __grid_constant__ FwdArgs A
             const __grid_constant__ BinCoef B) {
   const int64_t n = A.n;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x * R;
+  const double pl_uniform = A.pl_scalar + P.pl_const;
   // block-uniform loop: every lane of every warp takes the same trip count,
   // so warp-collective histogram aggregation below is always legal.
   for (int64_t blk = (int64_t)blockIdx.x * blockDim.x * R; blk < n; blk += stride) {
@@ -99,11 +100,14 @@ k_trace_fwd(const __grid_constant__ Program P, const __grid_constant__ FwdArgs A
     store4<R>(A.odx, i0, n, dx, vec);
     store4<R>(A.ody, i0, n, dy, vec);
     if (A.opl) {
+      // float64 adds per ray kept to the minimum (one, plus one per per-ray
+      // input): GB300 issues float64 at ~1/60 of the float32 rate
 #pragma unroll
       for (int k = 0; k < R; ++k) {
         if (i0 + k < n) {
-          double p0 = A.pl ? A.pl[i0 + k] : A.pl_scalar;
-          A.opl[i0 + k] = ((p0 + P.pl_const) + dvar[k]) + (double)r[k].plv;
+          double base = A.pl ? (A.pl[i0 + k] + P.pl_const) : pl_uniform;
+          if (A.z) base += dvar[k];
+          A.opl[i0 + k] = base + (double)r[k].plv;
         }
       }
     }

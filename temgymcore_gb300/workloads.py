@@ -81,7 +81,9 @@ def stem_4d(seed: int = 0, scan=(64, 64), rays_per_probe: int = 1024, scan_step:
 
 
 def descan_error_from_matrix(m) -> dict:
-    m = np.asarray(m, dtype=np.float64)
+    m = np.asarray(m)
+    if not np.iscomplexobj(m):  # complex entries pass through (complex-step derivatives)
+        m = m.astype(np.float64)
     return {"pxo_pxi": m[0, 0], "pxo_pyi": m[0, 1], "pyo_pxi": m[1, 0], "pyo_pyi": m[1, 1],
             "sxo_pxi": m[2, 0], "sxo_pyi": m[2, 1], "syo_pxi": m[3, 0], "syo_pyi": m[3, 1],
             "pxo_sxi": m[0, 2], "pxo_syi": m[0, 3], "pyo_sxi": m[1, 2], "pyo_syi": m[1, 3],
@@ -156,3 +158,42 @@ def gaussian_rays(d: dict):
                        pathlength=d["pathlength"], amplitude=d["amplitude"],
                        waist_xy=d["waist_xy"], radii_of_curv=d["radii_of_curv"],
                        wavelength=d["wavelength"], theta=d["theta"])
+
+
+def stem_fit(seed: int = 0, scan=(32, 32), rays_per_probe: int = 1024, rel_sigma: float = 0.01):
+    """Adjoint-fit workload in the plain-trace geometry.
+
+    Bundle at z = 0 with the plain-trace distributions (x, y ~ U(+-1e-3) m,
+    dx, dy ~ N(0, 1e-3) rad); scan/descan plane at z = defocus = 0.05 m
+    (32 x 32 scan, step 1e-5 m, rotation 37 deg, descan I + N(0, 1e-3));
+    Lens(f = 0.2 m) at z = 0.5 m (gap 0.45 m after the scan plane); detector
+    at z = 1.0 m (camera length 0.95 m from the scan plane).  The target
+    parameters are the nominal ones perturbed by N(0, rel_sigma) relative.
+    """
+    rng = np.random.default_rng(seed)
+    n = rays_per_probe
+    x = rng.uniform(-1e-3, 1e-3, n).astype(np.float32)
+    y = rng.uniform(-1e-3, 1e-3, n).astype(np.float32)
+    dx = rng.normal(0.0, 1e-3, n).astype(np.float32)
+    dy = rng.normal(0.0, 1e-3, n).astype(np.float32)
+    descan = np.eye(4) + rng.normal(0.0, 1e-3, (4, 4))
+    theta0 = np.concatenate([[0.2, 0.05, 0.95, 37.0, 1e-5], descan.reshape(16)])
+    theta_true = theta0 * (1.0 + rng.normal(0.0, rel_sigma, theta0.size))
+    return {"x": x, "y": y, "dx": dx, "dy": dy, "rows": scan[0], "cols": scan[1], "gap": 0.45,
+            "theta0": theta0, "theta_true": theta_true}
+
+
+def stem_fit_probe_spec(w: dict, theta, p: int):
+    """Model description (oracle form) of ``stem_fit`` at probe p for theta."""
+    th = np.asarray(theta)
+    f, dfc, cl, rot, step = th[:5]
+    m = th[5:].reshape(4, 4)
+    rows, cols = w["rows"], w["cols"]
+    sg = {"kind": "scangrid", "z": dfc, "pixel_size": (step, step), "shape": (rows, cols),
+          "rotation": rot}
+    return sg, [{"kind": "source", "z": 0.0}, sg,
+                {"kind": "scanner", "z": dfc, "scan_pos_x": None, "scan_pos_y": None},
+                {"kind": "descanner", "z": dfc, "scan_pos_x": None, "scan_pos_y": None,
+                 "descan_error": descan_error_from_matrix(m)},
+                {"kind": "lens", "z": dfc + w["gap"], "focal_length": f},
+                {"kind": "detector", "z": dfc + cl, "pixel_size": (1e-5, 1e-5), "shape": (256, 256)}]
