@@ -409,6 +409,15 @@ def run_only(args):
                       w["rows"], w["cols"], w["gap"], w["theta0"])
         fit.set_targets(w["theta_true"])
         fn = fit.loss_grad
+    elif args.only == "batched":
+        from temgymcore_gb300.batched import BatchedTrace
+        from temgymcore_gb300.workloads import batched_sweep, build_model
+        w = batched_sweep(seed=0, n_models=args.models or 512)
+        bt = BatchedTrace([build_model(s) for s in w["specs"]], w["counts"], tile_rays=4096)
+        bt.block, bt.rpt = 256, 4
+        x, y, dx, dy, tx, ty = (torch.tensor(w[k], device=dev) for k in ("x", "y", "dx", "dy", "tx", "ty"))
+        out, raw = bt.alloc_outputs(), bt.alloc_raw()
+        fn = lambda: bt.run(x, y, dx, dy, out, (tx, ty), raw)  # noqa: E731
     elif args.only == "plain":
         from temgymcore_gb300.workloads import build_model, plain_trace
         w = plain_trace(seed=0, n=args.rays or 65536)
@@ -425,6 +434,66 @@ def run_only(args):
     ms = _time(torch, fn, args.steps)
     print(json.dumps({"only": args.only, "ms_per_call": ms, "steps": args.steps,
                       "error_word": t._native.error_word()}))
+
+
+def secondary_batched(torch, dev, hbm):
+    """Batched sweep: 512 models (U{2..12} components), ~2.4e7 rays, forward +
+    adjoint in one persistent launch replayed as a CUDA graph (autotuned launch
+    shape), versus per-model plain launches on the same GPU."""
+    import ctypes as C
+
+    from temgymcore_gb300 import _native as N
+    from temgymcore_gb300.batched import BatchedTrace
+    from temgymcore_gb300.run import _rays_struct
+    from temgymcore_gb300.workloads import batched_sweep, build_model
+    w = batched_sweep(seed=0)
+    models = [build_model(s) for s in w["specs"]]
+    bt = BatchedTrace(models, w["counts"])
+    x, y, dx, dy, tx, ty = (torch.tensor(w[k], device=dev) for k in ("x", "y", "dx", "dy", "tx", "ty"))
+    out = bt.alloc_outputs()
+    raw = bt.alloc_raw()
+    best, results = bt.autotune(x, y, dx, dy, out, (tx, ty), raw)
+    g = bt.capture(x, y, dx, dy, out, (tx, ty), raw)
+    ms = _time(torch, g.replay, 10)
+    steps = int(sum(c * len(m) for c, m in zip(w["counts"], models)))
+    total = int(w["counts"].sum())
+    alg = total * (16 + 24 + 8)
+    # per-model plain launches: forward, residual, generic adjoint per model
+    packed = bt._packed
+    outs = bt.alloc_outputs()
+    gxy = [torch.empty(total, dtype=torch.float32, device=dev) for _ in range(2)]
+    zeros = torch.zeros(total, dtype=torch.float32, device=dev)
+    ws = torch.empty(64 << 20, dtype=torch.uint8, device=dev)
+    raws = [torch.zeros((2 * len(m), 4), dtype=torch.float64, device=dev) for m in models]
+    lib = N.lib()
+    structs = []
+    for m in range(len(models)):
+        a, b = int(bt.offsets[m]), int(bt.offsets[m + 1])
+        n = b - a
+        rin = _rays_struct(n, x[a:b], y[a:b], dx[a:b], dy[a:b], None, 0.0, None, 0.0)
+        rout = _rays_struct(n, outs[0][a:b], outs[1][a:b], outs[2][a:b], outs[3][a:b], None, 0.0,
+                            outs[4][a:b], 0.0)
+        gout = _rays_struct(n, gxy[0][a:b], gxy[1][a:b], zeros[a:b], zeros[a:b], None, 0.0, None, 0.0)
+        structs.append((a, b, rin, rout, gout))
+
+    def plain():
+        for m, (a, b, rin, rout, gout) in enumerate(structs):
+            mm = packed[m][0]
+            lib.tg_trace_fwd(C.byref(mm), C.byref(rin), C.byref(rout), None, None, None, None, None, 0,
+                             N.stream_ptr())
+            torch.sub(outs[0][a:b], tx[a:b], out=gxy[0][a:b]).mul_(2.0)
+            torch.sub(outs[1][a:b], ty[a:b], out=gxy[1][a:b]).mul_(2.0)
+            lib.tg_trace_vjp(C.byref(mm), C.byref(rin), C.byref(gout), None, raws[m].data_ptr(),
+                             ws.data_ptr(), ws.numel(), N.stream_ptr())
+    ms_plain = _time(torch, plain, 2)
+    return {"workload": f"batched sweep: {len(models)} models, U{{2..12}} components, {total} rays, "
+                        "forward + adjoint (squared-residual loss)",
+            "ms": ms, "ray_component_steps_per_s": steps / (ms * 1e-3), "rays_per_s": total / (ms * 1e-3),
+            "algorithmic_bytes": alg, "achieved_gbs": alg / (ms * 1e-3) / 1e9,
+            "frac_of_hbm": alg / (ms * 1e-3) / 1e9 / hbm,
+            "autotuned": {"tile_rays": best[0], "block": best[1], "rays_per_thread": best[2]},
+            "autotune_ms": None if results is None else [[r[1], r[2], r[3], r[0]] for r in results],
+            "plain_per_model_ms": ms_plain, "speedup_vs_plain_per_model": ms_plain / ms}
 
 
 def run_gpu(args, world, rank, local):
@@ -516,6 +585,10 @@ def run_gpu(args, world, rank, local):
             secondary["adjoint_fit"] = secondary_fit(torch, dev)
         except Exception as e:
             secondary["adjoint_fit"] = {"error": repr(e)}
+        try:
+            secondary["batched_sweep"] = secondary_batched(torch, dev, hbm)
+        except Exception as e:
+            secondary["batched_sweep"] = {"error": repr(e)}
     cpu = cpu_baseline() if (rank == 0 and world == 1) else None
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -544,9 +617,10 @@ def main():
                     help="skip the secondary workloads, e2e and CPU baseline")
     ap.add_argument("--only", default=None,
                     help="profile one workload alone: field-separable, field-direct, field-astig, "
-                         "field-fp64, fit, plain")
+                         "field-fp64, fit, batched, plain")
     ap.add_argument("--beams", type=int, default=None)
     ap.add_argument("--rays", type=int, default=None)
+    ap.add_argument("--models", type=int, default=None)
     args = ap.parse_args()
     if args.scan:
         global SCAN

@@ -192,6 +192,50 @@ typedef struct tg_scan {
 int tg_scan_hist(const tg_model *model, const tg_rays *bundle, const tg_scan *scan,
                  const tg_grid *grid, int32_t *hist, float *probe_xy, void *stream);
 
+/* ---- many models in one persistent launch ------------------------------ */
+typedef struct tg_batch_info {
+  size_t plan_bytes;       /* bytes of the packed plan (copy it to the device) */
+  size_t workspace_bytes;  /* device workspace for tg_batch_run              */
+  int32_t n_tiles;
+  int32_t total_steps;     /* sum over models of 2 * n_components           */
+  int64_t total_rays;
+} tg_batch_info;
+
+/* Rays of all models concatenated in model order (device float32).  With
+ * target_x/target_y (device float32, may be NULL = forward only) the adjoint
+ * of loss = sum |(x, y)_out - target|^2 runs too and raw (device float64
+ * [total_steps][4], OVERWRITTEN) receives each model's per-step sums (the
+ * quantities of tg_trace_vjp), model m's steps starting at
+ * 2 * (components of models 0..m-1). */
+typedef struct tg_batch_io {
+  const float *x, *y, *dx, *dy;
+  float *out_x, *out_y, *out_dx, *out_dy;
+  double *out_pathlength;
+  const float *target_x, *target_y;
+  double *raw;
+} tg_batch_io;
+
+/*
+ * tg_batch_plan - pack n_models models (host) with n_rays[m] rays each and
+ * input z z_in[m] (NULL = 0) into one plan of tiles of tile_rays rays.  Host
+ * only: with plan == NULL fills *info (sizes); otherwise writes the plan into
+ * the host buffer plan (info->plan_bytes) for the caller to copy to the
+ * device.  Replaces a Python loop of run_to_end (run.py:85-116) per model.
+ */
+int tg_batch_plan(int32_t n_models, const tg_model *models, const int64_t *n_rays,
+                  const double *z_in, int32_t tile_rays, void *plan, size_t plan_bytes,
+                  tg_batch_info *info);
+
+/*
+ * tg_batch_run - one persistent launch over every tile of the plan (device
+ * copy), forward and (with targets) adjoint, plus a deterministic per-model
+ * reduction.  block in {128, 256, 512}; rays_per_thread in {1, 2, 4}.
+ * workspace: device, info->workspace_bytes, 256-byte aligned.
+ */
+int tg_batch_run(const void *plan_dev, const tg_batch_info *info, const tg_batch_io *io,
+                 int32_t block, int32_t rays_per_thread, void *workspace, size_t ws_bytes,
+                 void *stream);
+
 /* ---- 4D-STEM calibration fit (device-resident parameters) -------------- */
 /* Model: bundle at z = 0 -> Scanner + Descanner at z = defocus with the
  * probe's scan position (ScanGrid of rows x cols, centre 0) -> Lens(f) at

@@ -274,6 +274,7 @@ extern "C" int tg_internal_err_scan(uint32_t*, int);
 extern "C" int tg_internal_err_field(uint32_t*, int);
 extern "C" int tg_internal_err_gemm(uint32_t*, int);
 extern "C" int tg_internal_err_fit(uint32_t*, int);
+extern "C" int tg_internal_err_batch(uint32_t*, int);
 
 extern "C" int tg_get_error_word(uint32_t* out, int clear) {
   if (!out) return TG_ERR_INVALID;
@@ -284,5 +285,6 @@ extern "C" int tg_get_error_word(uint32_t* out, int clear) {
   if (s == TG_OK) s = tg_internal_err_field(out, clear);
   if (s == TG_OK) s = tg_internal_err_gemm(out, clear);
   if (s == TG_OK) s = tg_internal_err_fit(out, clear);
+  if (s == TG_OK) s = tg_internal_err_batch(out, clear);
   return s;
 }

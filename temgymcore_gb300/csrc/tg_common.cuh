@@ -221,4 +221,82 @@ __device__ __forceinline__ void op_forward(const Op& op, const float4* pshift,
   }
 }
 
+// ---------------------------------------------------------------- adjoint
+struct Adj {
+  float lx, ly, ldx, ldy, lpl;
+};
+
+// Reverse one step: on entry r is the state after the step and a the adjoint
+// after it; on exit both describe the state before it.  c receives the step's
+// parameter sensitivities for this ray.  gz receives dL/dz_in (OP_FREE_VARZ).
+__device__ __forceinline__ void op_reverse(const Op& op, const float4* pshift, RayS& r,
+                                           Adj& a, uint64_t sbits, double dvar,
+                                           float c[4], float& gz) {
+  switch (op.kind) {
+    case OP_FREE:
+    case OP_FREE_VARZ: {
+      float d = (op.kind == OP_FREE) ? op.c[0] : (float)dvar;
+      float g = a.lx * r.dx + a.ly * r.dy + a.lpl;
+      c[0] = g;
+      if (op.kind == OP_FREE_VARZ) gz = -g;
+      r.x = fmaf(-r.dx, d, r.x);
+      r.y = fmaf(-r.dy, d, r.y);
+      a.ldx = fmaf(a.lx, d, a.ldx);
+      a.ldy = fmaf(a.ly, d, a.ldy);
+    } break;
+    case OP_LENS: {
+      float k = op.c[0], h = op.c[1];
+      float x = r.x, y = r.y;
+      r.dx = fmaf(x, k, r.dx);
+      r.dy = fmaf(y, k, r.dy);
+      c[0] = (a.ldx * x + a.ldy * y) * (k * k) + a.lpl * (x * x + y * y) * (k * h);
+      a.lx = a.lx - a.ldx * k - a.lpl * 2.f * x * h;
+      a.ly = a.ly - a.ldy * k - a.lpl * 2.f * y * h;
+    } break;
+    case OP_SHIFT:
+    case OP_PROBE_SHIFT: {
+      float4 s = (op.kind == OP_SHIFT) ? make_float4(op.c[0], op.c[1], op.c[2], op.c[3])
+                                       : pshift[op.aux];
+      r.x -= s.x; r.y -= s.y; r.dx -= s.z; r.dy -= s.w;
+      c[0] = a.lx; c[1] = a.ly; c[2] = a.ldx; c[3] = a.ldy;
+    } break;
+    case OP_DEFLECT: {
+      c[0] = a.ldx;
+      c[1] = a.ldy;
+      r.dx -= op.c[0];
+      r.dy -= op.c[1];
+      a.lx = fmaf(a.lpl, r.dx, a.lx);
+      a.ly = fmaf(a.lpl, r.dy, a.ly);
+      a.ldx = fmaf(a.lpl, r.x, a.ldx);
+      a.ldy = fmaf(a.lpl, r.y, a.ldy);
+    } break;
+    case OP_BIPRISM: {
+      uint32_t b = (uint32_t)(sbits >> (2 * op.aux)) & 3u;
+      float s = b == 1u ? 1.f : (b == 2u ? -1.f : 0.f);
+      c[0] = a.ldx * s;
+      r.dx = fmaf(-op.c[0], s, r.dx);
+      a.lx = fmaf(a.lpl, r.dx, a.lx);
+      a.ly = fmaf(a.lpl, r.dy, a.ly);
+      a.ldx = fmaf(a.lpl, r.x, a.ldx);
+      a.ldy = fmaf(a.lpl, r.y, a.ldy);
+    } break;
+    case OP_ROTATE: {
+      float cs = op.c[0], sn = op.c[1];
+      c[0] = -a.lx * r.y + a.ly * r.x - a.ldx * r.dy + a.ldy * r.dx;
+      float x = r.x, y = r.y, dx = r.dx, dy = r.dy;
+      r.x = x * cs + y * sn;
+      r.y = -x * sn + y * cs;
+      r.dx = dx * cs + dy * sn;
+      r.dy = -dx * sn + dy * cs;
+      float lx = a.lx, ly = a.ly, ldx = a.ldx, ldy = a.ldy;
+      a.lx = lx * cs + ly * sn;
+      a.ly = -lx * sn + ly * cs;
+      a.ldx = ldx * cs + ldy * sn;
+      a.ldy = -ldx * sn + ldy * cs;
+    } break;
+    default:
+      break;
+  }
+}
+
 }  // namespace tg

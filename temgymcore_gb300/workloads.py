@@ -197,3 +197,40 @@ def stem_fit_probe_spec(w: dict, theta, p: int):
                  "descan_error": descan_error_from_matrix(m)},
                 {"kind": "lens", "z": dfc + w["gap"], "focal_length": f},
                 {"kind": "detector", "z": dfc + cl, "pixel_size": (1e-5, 1e-5), "shape": (256, 256)}]
+
+
+def batched_sweep(seed: int = 0, n_models: int = 512, n_components=(2, 12),
+                  rays=(1e3, 2.6e5)):
+    """Batched sweep: n_models independent models with U{2..12} components
+    drawn from lens / deflector / biprism / aperture (log-uniform f in
+    [0.01, 1] m, spacings U(0.01, 0.1) m), ray counts log-uniform in
+    [1e3, 2.6e5] (~2.4e7 rays at 512 models); plain-trace ray distributions;
+    targets N(0, 1e-3) m for the adjoint's squared-residual loss."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for _ in range(n_models):
+        nc = int(rng.integers(n_components[0], n_components[1] + 1))
+        z = 0.0
+        comps = []
+        for _ in range(nc):
+            z += float(rng.uniform(0.01, 0.1))
+            kind = ("lens", "deflector", "biprism", "aperture")[int(rng.integers(0, 4))]
+            if kind == "lens":
+                comps.append({"kind": "lens", "z": z, "focal_length": float(10 ** rng.uniform(-2, 0))})
+            elif kind == "deflector":
+                comps.append({"kind": "deflector", "z": z, "def_x": float(rng.normal(0, 1e-3)),
+                              "def_y": float(rng.normal(0, 1e-3))})
+            elif kind == "biprism":
+                comps.append({"kind": "biprism", "z": z, "def_x": float(rng.normal(0, 1e-3))})
+            else:
+                comps.append({"kind": "aperture", "z": z, "radius": float(rng.uniform(5e-4, 5e-3))})
+        specs.append(comps)
+    counts = np.round(10 ** rng.uniform(np.log10(rays[0]), np.log10(rays[1]), n_models)).astype(np.int64)
+    total = int(counts.sum())
+    x = rng.uniform(-1e-3, 1e-3, total).astype(np.float32)
+    y = rng.uniform(-1e-3, 1e-3, total).astype(np.float32)
+    dx = rng.normal(0.0, 1e-3, total).astype(np.float32)
+    dy = rng.normal(0.0, 1e-3, total).astype(np.float32)
+    tx = rng.normal(0.0, 1e-3, total).astype(np.float32)
+    ty = rng.normal(0.0, 1e-3, total).astype(np.float32)
+    return {"specs": specs, "counts": counts, "x": x, "y": y, "dx": dx, "dy": dy, "tx": tx, "ty": ty}
