@@ -199,6 +199,7 @@ typedef struct tg_batch_info {
   int32_t n_tiles;
   int32_t total_steps;     /* sum over models of 2 * n_components           */
   int64_t total_rays;
+  int32_t max_steps;       /* largest 2 * n_components of one model         */
 } tg_batch_info;
 
 /* Rays of all models concatenated in model order (device float32).  With

@@ -64,9 +64,11 @@ template <int R>
 __global__ void __launch_bounds__(512)
 k_batch(const uint8_t* __restrict__ plan, const __grid_constant__ BatchIO io,
         int32_t* __restrict__ counter, double* __restrict__ partial) {
+  extern __shared__ float wacc[];  // [warps][n_steps * 4] per-warp float32 sums of this tile
   __shared__ Op sops[kMaxSteps];
-  __shared__ double acc[kMaxSteps * 4];
   __shared__ int s_tile;
+  const int nwarps = blockDim.x >> 5;
+  const int warp = threadIdx.x >> 5;
   const BHeader H = *reinterpret_cast<const BHeader*>(plan);
   const BModel* models = reinterpret_cast<const BModel*>(plan + H.models_off);
   const BTile* tiles = reinterpret_cast<const BTile*>(plan + H.tiles_off);
@@ -88,7 +90,7 @@ k_batch(const uint8_t* __restrict__ plan, const __grid_constant__ BatchIO io,
     const int ns = M.n_steps;
     for (int i = threadIdx.x; i < ns; i += blockDim.x) sops[i] = ops[M.op_off + i];
     if (adj)
-      for (int i = threadIdx.x; i < ns * 4; i += blockDim.x) acc[i] = 0.0;
+      for (int i = threadIdx.x; i < nwarps * ns * 4; i += blockDim.x) wacc[i] = 0.f;
     __syncthreads();
     const int64_t end = T.start + T.count;
     for (int64_t blk = T.start; blk < end; blk += (int64_t)blockDim.x * R) {
@@ -142,17 +144,23 @@ k_batch(const uint8_t* __restrict__ plan, const __grid_constant__ BatchIO io,
           op_reverse(op, nullptr, r[k], ad[k], sb[k], dv[k], ck, gz);
           c[0] += ck[0]; c[1] += ck[1]; c[2] += ck[2]; c[3] += ck[3];
         }
+        // warp sums accumulate in float32 in the warp's own shared row (no
+        // atomics, no float64: GB300 issues float64 at ~1/60 of float32)
         const int nsum = bt_nsums(op.kind);
         for (int j = 0; j < nsum; ++j) {
           const float v = bt_warp_sum(c[j]);
-          if (lane == 0) atomicAdd(&acc[4 * s + j], (double)v);
+          if (lane == 0) wacc[warp * ns * 4 + 4 * s + j] += v;
         }
       }
     }
     __syncthreads();
     if (adj) {
       double* dst = partial + M.part_off + (int64_t)(t - M.tile_off) * ns * 4;
-      for (int i = threadIdx.x; i < ns * 4; i += blockDim.x) dst[i] = acc[i];
+      for (int i = threadIdx.x; i < ns * 4; i += blockDim.x) {
+        double a = 0.0;
+        for (int w = 0; w < nwarps; ++w) a += (double)wacc[w * ns * 4 + i];
+        dst[i] = a;
+      }
     }
     __syncthreads();
   }
@@ -201,6 +209,7 @@ extern "C" int tg_batch_plan(int32_t n_models, const tg_model* models, const int
   std::vector<Op> ops;
   std::vector<int32_t> step_model;
   int64_t ray_off = 0, part_off = 0;
+  int32_t max_steps = 0;
   for (int m = 0; m < n_models; ++m) {
     if (n_rays[m] < 0) return TG_ERR_INVALID;
     Program P;
@@ -210,6 +219,7 @@ extern "C" int tg_batch_plan(int32_t n_models, const tg_model* models, const int
     BModel& M = bm[m];
     M.op_off = (int32_t)ops.size();
     M.n_steps = P.n_steps;
+    if (P.n_steps > max_steps) max_steps = P.n_steps;
     M.tile_off = (int32_t)bt.size();
     M.ray_off = ray_off;
     M.n_rays = n_rays[m];
@@ -249,6 +259,7 @@ extern "C" int tg_batch_plan(int32_t n_models, const tg_model* models, const int
   info->n_tiles = H.n_tiles;
   info->total_steps = H.total_steps;
   info->total_rays = ray_off;
+  info->max_steps = max_steps;
   info->workspace_bytes = 256 + (size_t)part_off * sizeof(double);
   if (!plan) return TG_OK;  // size query
   if (plan_bytes < (size_t)off) return TG_ERR_WORKSPACE;
@@ -288,16 +299,19 @@ extern "C" int tg_batch_run(const void* plan_dev, const tg_batch_info* info, con
   A.tx = io->target_x; A.ty = io->target_y;
   A.raw = io->raw;
   const uint8_t* plan = reinterpret_cast<const uint8_t*>(plan_dev);
+  // per-warp float32 step sums: warps x max steps x 4 (max steps <= kMaxSteps)
+  const size_t dyn = (size_t)(block / 32) * (info->max_steps > 0 ? info->max_steps : 1) * 4 * sizeof(float);
+  if (dyn > 48 * 1024) return TG_ERR_TOO_LARGE;
   int per_sm = 1;
-  if (rays_per_thread == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<1>, block, 0);
-  else if (rays_per_thread == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<2>, block, 0);
-  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<4>, block, 0);
+  if (rays_per_thread == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<1>, block, dyn);
+  else if (rays_per_thread == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<2>, block, dyn);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<4>, block, dyn);
   if (per_sm < 1) per_sm = 1;
   int grid = sm_count_batch() * per_sm;
   if (grid > info->n_tiles) grid = info->n_tiles;
-  if (rays_per_thread == 1) k_batch<1><<<grid, block, 0, s>>>(plan, A, counter, partial);
-  else if (rays_per_thread == 2) k_batch<2><<<grid, block, 0, s>>>(plan, A, counter, partial);
-  else k_batch<4><<<grid, block, 0, s>>>(plan, A, counter, partial);
+  if (rays_per_thread == 1) k_batch<1><<<grid, block, dyn, s>>>(plan, A, counter, partial);
+  else if (rays_per_thread == 2) k_batch<2><<<grid, block, dyn, s>>>(plan, A, counter, partial);
+  else k_batch<4><<<grid, block, dyn, s>>>(plan, A, counter, partial);
   if (adj && info->total_steps > 0) {
     const int64_t nel = (int64_t)info->total_steps * 4;
     k_batch_reduce<<<(int)((nel + 255) / 256), 256, 0, s>>>(plan, partial, io->raw);
