@@ -5,12 +5,14 @@
 // (field.cu, k_field_operands).  Each complex operand is stored as bf16 planes
 // re_hi, re_lo, im_hi, im_lo (value ~= hi + lo to ~2^-17 relative), K-major
 // (beam index contiguous).  Per 16-deep K slice the CTA issues 12 MMAs
-// (hi*hi + hi*lo + lo*hi for each real product) into three float32
-// accumulators held in tensor memory:
-//   D0 = Vr Ur,  D1 = Vi Ui,  D2 = Vr Ui + Vi Ur;   Fr = D0 - D1, Fi = D2.
-// Tile 128 x 128 (UMMA M = N = 128, K = 16), K blocks of 32 bf16 (64-byte rows,
-// 64-byte swizzle), a 3-stage TMA -> MMA pipeline on mbarriers, split-K over
-// beams across CTAs (partials reduced deterministically in field.cu).
+// (hi*hi + hi*lo + lo*hi) into two float32 accumulators held in tensor
+// memory, each 128 x 256 with the U operand stacked as [Ur | Ui]:
+//   D0 = Vr [Ur | Ui],  D1 = Vi [Ur | Ui];
+//   Fr = D0[:, :128] - D1[:, 128:],  Fi = D0[:, 128:] + D1[:, :128].
+// Output tile 128 x 128 complex (UMMA M = 128, N = 256, K = 16: six MMAs per
+// K slice), K blocks of 32 bf16 (64-byte rows, 64-byte swizzle), a 3-stage
+// TMA -> MMA pipeline on mbarriers, split-K over beams across CTAs (partials
+// reduced deterministically in field.cu).
 // Roles: warp 0 lane 0 issues TMA loads, warp 1 lane 0 issues MMAs, all four
 // warps drain TMEM in the epilogue.  Every wait is bounded: on timeout the
 // kernel records TG_EW_MMA, drains its own copies (bounded) and frees TMEM.
@@ -28,9 +30,11 @@ namespace tg {
 
 constexpr int kGStages = 3;
 constexpr int kTileBytes = 128 * 64;            // 128 lines x 32 bf16
-constexpr int kStageBytes = 8 * kTileBytes;     // 4 V planes + 4 U planes
+constexpr int kStageBytes = 8 * kTileBytes;     // 4 V planes + [Ur;Ui] hi and lo
 constexpr int kGemmSmem = kGStages * kStageBytes + 1024 /*align*/ + 256 /*barriers*/;
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
+// kind::f16 instruction descriptor: f32 accumulate, bf16 A and B, both
+// K-major, N = 256, M = 128.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((256u >> 3) << 17) | ((128u >> 4) << 24);
 constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -172,12 +176,16 @@ k_field_gemm(const __grid_constant__ GemmMaps maps, const __grid_constant__ Gemm
       mbar_expect_tx(full0 + 8 * s, kStageBytes);
       const int kc = (kb0 + i) * 32;
       for (int p = 0; p < 4; ++p) tma_load_2d(base + p * kTileBytes, &maps.v[p], kc, mt * 128, full0 + 8 * s);
-      for (int p = 0; p < 4; ++p) tma_load_2d(base + (4 + p) * kTileBytes, &maps.u[p], kc, nt * 128, full0 + 8 * s);
+      // U planes: re_hi, re_lo, im_hi, im_lo -> [re_hi; im_hi] at tile 4-5, [re_lo; im_lo] at 6-7
+      tma_load_2d(base + 4 * kTileBytes, &maps.u[0], kc, nt * 128, full0 + 8 * s);
+      tma_load_2d(base + 5 * kTileBytes, &maps.u[2], kc, nt * 128, full0 + 8 * s);
+      tma_load_2d(base + 6 * kTileBytes, &maps.u[1], kc, nt * 128, full0 + 8 * s);
+      tma_load_2d(base + 7 * kTileBytes, &maps.u[3], kc, nt * 128, full0 + 8 * s);
       ++loads_issued;
     }
   } else if (warp == 1 && lane == 0) {
     // ---------------- MMA issuer
-    const uint32_t d0 = tmem, d1 = tmem + 128, d2 = tmem + 256;
+    const uint32_t d0 = tmem, d1 = tmem + 256;
     bool first = true;
     for (int i = 0; i < A.nkb; ++i) {
       const int s = i % kGStages;
@@ -188,15 +196,12 @@ k_field_gemm(const __grid_constant__ GemmMaps maps, const __grid_constant__ Gemm
 #pragma unroll
       for (int kk = 0; kk < 2; ++kk) {
         const uint32_t ko = kk * 32;  // bytes: 16 bf16
-        const uint64_t a0 = sdesc(base + 0 * kTileBytes + ko), a1 = sdesc(base + 1 * kTileBytes + ko);
-        const uint64_t a2 = sdesc(base + 2 * kTileBytes + ko), a3 = sdesc(base + 3 * kTileBytes + ko);
-        const uint64_t b0 = sdesc(base + 4 * kTileBytes + ko), b1 = sdesc(base + 5 * kTileBytes + ko);
-        const uint64_t b2 = sdesc(base + 6 * kTileBytes + ko), b3 = sdesc(base + 7 * kTileBytes + ko);
+        const uint64_t vrh = sdesc(base + 0 * kTileBytes + ko), vrl = sdesc(base + 1 * kTileBytes + ko);
+        const uint64_t vih = sdesc(base + 2 * kTileBytes + ko), vil = sdesc(base + 3 * kTileBytes + ko);
+        const uint64_t bh = sdesc(base + 4 * kTileBytes + ko), bl = sdesc(base + 6 * kTileBytes + ko);
         const uint32_t acc = first ? 0u : 1u;
-        umma(d0, a0, b0, acc); umma(d0, a0, b1, 1u); umma(d0, a1, b0, 1u);
-        umma(d1, a2, b2, acc); umma(d1, a2, b3, 1u); umma(d1, a3, b2, 1u);
-        umma(d2, a0, b2, acc); umma(d2, a0, b3, 1u); umma(d2, a1, b2, 1u);
-        umma(d2, a2, b0, 1u); umma(d2, a2, b1, 1u); umma(d2, a3, b0, 1u);
+        umma(d0, vrh, bh, acc); umma(d0, vrh, bl, 1u); umma(d0, vrl, bh, 1u);
+        umma(d1, vih, bh, acc); umma(d1, vih, bl, 1u); umma(d1, vil, bh, 1u);
         first = false;
       }
       umma_commit(empty0 + 8 * s);  // smem stage free once these MMAs finish
@@ -212,25 +217,28 @@ k_field_gemm(const __grid_constant__ GemmMaps maps, const __grid_constant__ Gemm
   float2* out = A.part + (size_t)sp * A.h * A.w + (size_t)row * A.w;
   const uint32_t lane_base = ((uint32_t)(warp * 32)) << 16;
   for (int c = 0; c < 4; ++c) {
-    uint32_t r0[32], r1[32], r2[32];
-    tmem_ld32(tmem + lane_base + 0 + c * 32, r0);
-    tmem_ld32(tmem + lane_base + 128 + c * 32, r1);
-    tmem_ld32(tmem + lane_base + 256 + c * 32, r2);
+    uint32_t a_re[32], a_im[32], b_re[32], b_im[32];
+    tmem_ld32(tmem + lane_base + 0 + c * 32, a_re);    // D0: Vr Ur
+    tmem_ld32(tmem + lane_base + 128 + c * 32, a_im);  // D0: Vr Ui
+    tmem_ld32(tmem + lane_base + 256 + c * 32, b_re);  // D1: Vi Ur
+    tmem_ld32(tmem + lane_base + 384 + c * 32, b_im);  // D1: Vi Ui
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
     const int col0 = nt * 128 + c * 32;
     if (got && row < A.h) {
       if (col0 + 32 <= A.w && (A.w & 1) == 0) {
 #pragma unroll
         for (int j = 0; j < 32; j += 2) {
-          float4 v = make_float4(__uint_as_float(r0[j]) - __uint_as_float(r1[j]), __uint_as_float(r2[j]),
-                                 __uint_as_float(r0[j + 1]) - __uint_as_float(r1[j + 1]),
-                                 __uint_as_float(r2[j + 1]));
+          float4 v = make_float4(__uint_as_float(a_re[j]) - __uint_as_float(b_im[j]),
+                                 __uint_as_float(a_im[j]) + __uint_as_float(b_re[j]),
+                                 __uint_as_float(a_re[j + 1]) - __uint_as_float(b_im[j + 1]),
+                                 __uint_as_float(a_im[j + 1]) + __uint_as_float(b_re[j + 1]));
           *reinterpret_cast<float4*>(out + col0 + j) = v;
         }
       } else {
         for (int j = 0; j < 32; ++j)
           if (col0 + j < A.w)
-            out[col0 + j] = make_float2(__uint_as_float(r0[j]) - __uint_as_float(r1[j]), __uint_as_float(r2[j]));
+            out[col0 + j] = make_float2(__uint_as_float(a_re[j]) - __uint_as_float(b_im[j]),
+                                        __uint_as_float(a_im[j]) + __uint_as_float(b_re[j]));
       }
     }
   }
