@@ -200,6 +200,10 @@ typedef struct tg_batch_info {
   int32_t total_steps;     /* sum over models of 2 * n_components           */
   int64_t total_rays;
   int32_t max_steps;       /* largest 2 * n_components of one model         */
+  int32_t max_moments;     /* largest adjoint moment count of one model     */
+  int32_t n_models;
+  int64_t partial_doubles; /* workspace layout: per-tile moment partials    */
+  int64_t moment_doubles;  /* per-model moments                             */
 } tg_batch_info;
 
 /* Rays of all models concatenated in model order (device float32).  With
@@ -207,7 +211,9 @@ typedef struct tg_batch_info {
  * of loss = sum |(x, y)_out - target|^2 runs too and raw (device float64
  * [total_steps][4], OVERWRITTEN) receives each model's per-step sums (the
  * quantities of tg_trace_vjp), model m's steps starting at
- * 2 * (components of models 0..m-1). */
+ * 2 * (components of models 0..m-1).  The adjoint is evaluated from per-model
+ * moments of the rays (the loss reaches every step through the chain's
+ * ray-independent linear part), so it costs a few multiply-adds per ray. */
 typedef struct tg_batch_io {
   const float *x, *y, *dx, *dy;
   float *out_x, *out_y, *out_dx, *out_dy;
@@ -252,13 +258,13 @@ typedef struct tg_stem_fit {
   double lens_gap;
 } tg_stem_fit;
 
+/* Workspace bytes of tg_stem_fit_forward / tg_stem_fit_loss_grad. */
+size_t tg_stem_fit_workspace(int32_t n_probes);
+
 /* Detector positions of every (probe, ray) at theta (device float32
  * [rows*cols][n_rays] each).  Replaces the per-probe run_to_end loop. */
 int tg_stem_fit_forward(const tg_stem_fit *cfg, const double *theta, float *det_x,
-                        float *det_y, void *stream);
-
-/* Workspace bytes of tg_stem_fit_loss_grad. */
-size_t tg_stem_fit_workspace(int32_t n_probes);
+                        float *det_y, void *workspace, size_t ws_bytes, void *stream);
 
 /*
  * tg_stem_fit_loss_grad - out (device float64 [22]): out[0] = sum over probes

@@ -64,7 +64,7 @@ from .components import (  # noqa: E402,F401
 )
 from .propagator import FreeSpaceParaxial, FreeSpaceDirCosine, Propagator, BasePropagator  # noqa: E402,F401
 from .run import (  # noqa: E402,F401
-    run_to_end, run_iter, solve_model, abcd_matrix, trace_to_image, pack_model,
+    run_to_end, run_iter, solve_model, abcd_matrix, trace_to_image, pack_model, TracePlan,
 )
 from .scan import scan_images, scan_positions, probe_model  # noqa: E402,F401
 from .gaussian import make_gaussian_image, FieldPlan, fibonacci_spiral  # noqa: E402,F401

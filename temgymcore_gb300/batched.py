@@ -24,7 +24,9 @@ from .run import _check_model, _device, pack_model
 
 class TgBatchInfo(C.Structure):
     _fields_ = [("plan_bytes", C.c_size_t), ("workspace_bytes", C.c_size_t), ("n_tiles", C.c_int32),
-                ("total_steps", C.c_int32), ("total_rays", C.c_int64), ("max_steps", C.c_int32)]
+                ("total_steps", C.c_int32), ("total_rays", C.c_int64), ("max_steps", C.c_int32),
+                ("max_moments", C.c_int32), ("n_models", C.c_int32), ("partial_doubles", C.c_int64),
+                ("moment_doubles", C.c_int64)]
 
 
 class TgBatchIO(C.Structure):

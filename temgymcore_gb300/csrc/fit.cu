@@ -35,7 +35,10 @@ struct FitArgs {
   float *ox, *oy;        // forward mode outputs [n_probes][n] (may be NULL)
   const double* theta;
   double gap;
-  double* partial;  // [gridDim.x][kFitOut]
+  float4* shift;         // [n_probes] per-probe combined scanner+descanner shift
+  double2* sp;           // [n_probes] scan position (x, y)
+  float* fpar;           // [4] D, Lp, 1/f, gap (float32 copies)
+  double* psum;          // [n_probes][8] per-probe sums
   int32_t forward_only;
 };
 
@@ -45,50 +48,43 @@ __device__ __forceinline__ float warp_sumf(float v) {
   return v;
 }
 
-__global__ void __launch_bounds__(kFitThreads)
-k_stem_fit(const __grid_constant__ FitArgs A) {
-  __shared__ double th[21];
-  __shared__ double acc[kFitOut];
-  __shared__ float wsum[kFitThreads / 32][8];
-  __shared__ float4 shift;  // per-probe combined scanner+descanner shift
-  __shared__ double sp[2];
-  __shared__ double trig[2];   // cos, sin of the scan rotation
-  __shared__ float fpar[4];    // D, Lp, 1/f (float32 copies)
-  // float64 set-up by one thread: GB300's float64 rate is ~1/60 of float32,
-  // so no per-thread float64 transcendental or division is issued.
-  if (threadIdx.x < 21) th[threadIdx.x] = A.theta[threadIdx.x];
-  if (threadIdx.x < kFitOut) acc[threadIdx.x] = 0.0;
-  __syncthreads();
+// Scan geometry in float64, once per probe (and the float32 copies of the
+// distances / focal power once): the streaming kernel then issues no float64.
+__global__ void __launch_bounds__(256) k_fit_setup(const __grid_constant__ FitArgs A) {
+  __shared__ double cs[2];
   if (threadIdx.x == 0) {
-    double sr_, cr_;
-    sincos(th[3] * (3.141592653589793 / 180.0), &sr_, &cr_);
-    trig[0] = cr_;
-    trig[1] = sr_;
-    fpar[0] = (float)th[1];
-    fpar[1] = (float)(th[2] - A.gap);
-    fpar[2] = (float)(1.0 / th[0]);
+    double sr, cr;
+    sincos(A.theta[3] * (3.141592653589793 / 180.0), &sr, &cr);
+    cs[0] = cr;
+    cs[1] = sr;
+    if (blockIdx.x == 0) {
+      A.fpar[0] = (float)A.theta[1];
+      A.fpar[1] = (float)(A.theta[2] - A.gap);
+      A.fpar[2] = (float)(1.0 / A.theta[0]);
+      A.fpar[3] = (float)A.gap;
+    }
   }
   __syncthreads();
-  const float D = fpar[0], Lp = fpar[1], invf = fpar[2];
-  const float G = (float)A.gap;
-  const double PI = 3.141592653589793;
-  const double cr = trig[0], sr = trig[1];
-  const double step = th[4];
-  const double r0 = 0.5 * (A.rows - 1), c0 = 0.5 * (A.cols - 1);
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= A.n_probes) return;
+  const double cr = cs[0], sr = cs[1], step = A.theta[4];
+  const double u = (double)(p / A.cols) - 0.5 * (A.rows - 1), v = (double)(p % A.cols) - 0.5 * (A.cols - 1);
+  const double spx = step * (-sr * u + cr * v);
+  const double spy = -step * (cr * u + sr * v);
+  A.sp[p] = make_double2(spx, spy);
+  const double* M = A.theta + 5;
+  A.shift[p] = make_float4((float)(M[0] * spx + M[1] * spy), (float)(M[4] * spx + M[5] * spy),
+                           (float)(M[8] * spx + M[9] * spy), (float)(M[12] * spx + M[13] * spy));
+}
+
+// One CTA per probe (grid-stride): the chain and its hand-derived adjoint per
+// ray in float32 registers; the probe's eight sums leave as float64.
+__global__ void __launch_bounds__(kFitThreads) k_stem_fit(const __grid_constant__ FitArgs A) {
+  __shared__ float wsum[kFitThreads / 32][8];
+  const float D = A.fpar[0], Lp = A.fpar[1], invf = A.fpar[2], G = A.fpar[3];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int p = blockIdx.x; p < A.n_probes; p += gridDim.x) {
-    if (threadIdx.x == 0) {
-      const double u = (double)(p / A.cols) - r0, v = (double)(p % A.cols) - c0;
-      const double spx = step * (-sr * u + cr * v);
-      const double spy = -step * (cr * u + sr * v);
-      sp[0] = spx;
-      sp[1] = spy;
-      const double* M = th + 5;
-      shift = make_float4((float)(M[0] * spx + M[1] * spy), (float)(M[4] * spx + M[5] * spy),
-                          (float)(M[8] * spx + M[9] * spy), (float)(M[12] * spx + M[13] * spy));
-    }
-    __syncthreads();
-    const float4 sh = shift;
+    const float4 sh = A.shift[p];
     // per-thread sums: loss, dL/dLp, dL/df, dL/dD, Gx, Gy, Gdx, Gdy
     float s[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     for (int i = threadIdx.x; i < A.n; i += blockDim.x) {
@@ -107,62 +103,80 @@ k_stem_fit(const __grid_constant__ FitArgs A) {
       const float rx = xd - A.tx[o], ry = yd - A.ty[o];
       s[0] += rx * rx + ry * ry;
       const float lxd = 2.f * rx, lyd = 2.f * ry;
-      s[1] += lxd * dx4 + lyd * dy4;              // dL/dLp
+      s[1] += lxd * dx4 + lyd * dy4;                    // dL/dLp
       const float ldx4 = lxd * Lp, ldy4 = lyd * Lp;
       s[2] += (ldx4 * x3 + ldy4 * y3) * (invf * invf);  // dL/df
       const float lx3 = lxd - ldx4 * invf, ly3 = lyd - ldy4 * invf;
       const float ldx2 = fmaf(lx3, G, ldx4), ldy2 = fmaf(ly3, G, ldy4);
-      s[3] += lx3 * dx0 + ly3 * dy0;              // dL/dD (lambda_x2 = lambda_x3)
+      s[3] += lx3 * dx0 + ly3 * dy0;                    // dL/dD (lambda_x2 = lambda_x3)
       s[4] += lx3;
       s[5] += ly3;
       s[6] += ldx2;
       s[7] += ldy2;
     }
-    if (!A.forward_only) {
+    if (A.forward_only) continue;
 #pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        float v = warp_sumf(s[k]);
-        if (lane == 0) wsum[warp][k] = v;
-      }
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        double t[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
-          for (int k = 0; k < 8; ++k) t[k] += (double)wsum[w][k];
-        const double* M = th + 5;
-        const double spx = sp[0], spy = sp[1];
-        const double u = (double)(p / A.cols) - r0, v = (double)(p % A.cols) - c0;
-        acc[0] += t[0];
-        acc[1] += t[2];                 // f
-        acc[2] += t[3];                 // defocus
-        acc[3] += t[1];                 // camera length (Lp = CL - gap)
-        const double gr[4] = {t[4], t[5], t[6], t[7]};
-        double gsx = 0.0, gsy = 0.0;
-        for (int r = 0; r < 4; ++r) {
-          gsx += gr[r] * M[4 * r + 0];
-          gsy += gr[r] * M[4 * r + 1];
-          acc[6 + 4 * r + 0] += gr[r] * spx;  // dL/dM[r][0]
-          acc[6 + 4 * r + 1] += gr[r] * spy;  // dL/dM[r][1]
-          // tilt columns multiply a zero scan tilt: zero gradient
-        }
-        const double k = PI / 180.0;
-        acc[4] += gsx * (step * k * (-cr * u - sr * v)) + gsy * (-step * k * (-sr * u + cr * v));  // rot
-        acc[5] += gsx * (-sr * u + cr * v) + gsy * (-(cr * u + sr * v));                         // step
-      }
+    for (int k = 0; k < 8; ++k) {
+      float v = warp_sumf(s[k]);
+      if (lane == 0) wsum[warp][k] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 8) {
+      double t = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += (double)wsum[w][threadIdx.x];
+      A.psum[(size_t)p * 8 + threadIdx.x] = t;
     }
     __syncthreads();
   }
-  if (!A.forward_only && threadIdx.x < kFitOut)
-    A.partial[(size_t)blockIdx.x * kFitOut + threadIdx.x] = acc[threadIdx.x];
 }
 
-// out[0] = loss, out[1..21] = dL/dtheta (sum of block partials in block order)
-__global__ void k_fit_reduce(const double* __restrict__ partial, int nblocks, double* __restrict__ out) {
-  const int i = threadIdx.x;
-  if (i >= kFitOut) return;
-  double s = 0.0;
-  for (int b = 0; b < nblocks; ++b) s += partial[(size_t)b * kFitOut + i];
-  out[i] = s;
+// out[j] for j = blockIdx.x: loss (j = 0) or dL/dtheta[j-1], from the
+// per-probe sums through the scan-geometry chain rule (float64), block tree
+// reduction in a fixed order.
+__global__ void __launch_bounds__(256) k_fit_reduce(const __grid_constant__ FitArgs A, double* __restrict__ out) {
+  __shared__ double red[256];
+  __shared__ double cs[2];
+  const int j = blockIdx.x;
+  if (threadIdx.x == 0) {
+    double sr, cr;
+    sincos(A.theta[3] * (3.141592653589793 / 180.0), &sr, &cr);
+    cs[0] = cr;
+    cs[1] = sr;
+  }
+  __syncthreads();
+  const double cr = cs[0], sr = cs[1], step = A.theta[4];
+  const double* M = A.theta + 5;
+  const double kdeg = 3.141592653589793 / 180.0;
+  double acc = 0.0;
+  for (int p = threadIdx.x; p < A.n_probes; p += blockDim.x) {
+    const double* t = A.psum + (size_t)p * 8;
+    double c = 0.0;
+    if (j == 0) c = t[0];
+    else if (j == 1) c = t[2];
+    else if (j == 2) c = t[3];
+    else if (j == 3) c = t[1];
+    else if (j == 4 || j == 5) {
+      const double u = (double)(p / A.cols) - 0.5 * (A.rows - 1), v = (double)(p % A.cols) - 0.5 * (A.cols - 1);
+      double gsx = 0.0, gsy = 0.0;
+      for (int r = 0; r < 4; ++r) {
+        gsx += t[4 + r] * M[4 * r + 0];
+        gsy += t[4 + r] * M[4 * r + 1];
+      }
+      if (j == 4) c = gsx * (step * kdeg * (-cr * u - sr * v)) + gsy * (-step * kdeg * (-sr * u + cr * v));
+      else c = gsx * (-sr * u + cr * v) + gsy * (-(cr * u + sr * v));
+    } else {
+      const int e = j - 6, r = e >> 2, col = e & 3;  // dL/dM[r][col]; tilt columns multiply zero tilt
+      if (col < 2) c = t[4 + r] * (col == 0 ? A.sp[p].x : A.sp[p].y);
+    }
+    acc += c;
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = blockDim.x >> 1; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[j] = red[0];
 }
 
 // Adam on float64 parameters; the step counter lives on the device so the
@@ -197,8 +211,14 @@ static int fit_grid(int n_probes) {
     cudaDeviceGetAttribute(&cached, cudaDevAttrMultiProcessorCount, dev);
     if (cached <= 0) cached = 148;
   }
-  int g = cached * 4;
+  // one probe per CTA up to eight CTAs per SM (all resident in one wave)
+  int g = cached * 8;
   return g < n_probes ? g : (n_probes > 0 ? n_probes : 1);
+}
+
+// workspace: shift [n_probes] float4 | sp [n_probes] double2 | psum [n_probes][8] | fpar[4]
+static size_t fit_ws(int32_t n_probes) {
+  return (size_t)n_probes * (16 + 16 + 64) + 256;
 }
 
 }  // namespace tg
@@ -207,10 +227,10 @@ using namespace tg;
 
 extern "C" size_t tg_stem_fit_workspace(int32_t n_probes) {
   if (n_probes <= 0) return 0;
-  return (size_t)fit_grid(n_probes) * kFitOut * sizeof(double);
+  return fit_ws(n_probes);
 }
 
-static int fit_args(const tg_stem_fit* c, const double* theta, FitArgs* A) {
+static int fit_args(const tg_stem_fit* c, const double* theta, void* ws, size_t ws_bytes, FitArgs* A) {
   if (!c || !theta) return TG_ERR_INVALID;
   if (c->n_rays < 0 || c->rows <= 0 || c->cols <= 0) return TG_ERR_INVALID;
   if (c->n_rays > 0 && (!c->x || !c->y || !c->dx || !c->dy)) return TG_ERR_INVALID;
@@ -219,24 +239,32 @@ static int fit_args(const tg_stem_fit* c, const double* theta, FitArgs* A) {
   A->rows = c->rows;
   A->cols = c->cols;
   A->n_probes = c->rows * c->cols;
+  if (!ws || ws_bytes < fit_ws(A->n_probes)) return TG_ERR_WORKSPACE;
+  if (((uintptr_t)ws & 15) != 0) return TG_ERR_ALIGN;
   A->x = c->x; A->y = c->y; A->dx = c->dx; A->dy = c->dy;
   A->tx = c->target_x;
   A->ty = c->target_y;
   A->theta = theta;
   A->gap = c->lens_gap;
+  char* w = reinterpret_cast<char*>(ws);
+  A->shift = reinterpret_cast<float4*>(w);
+  A->sp = reinterpret_cast<double2*>(w + (size_t)A->n_probes * 16);
+  A->psum = reinterpret_cast<double*>(w + (size_t)A->n_probes * 32);
+  A->fpar = reinterpret_cast<float*>(w + (size_t)A->n_probes * 96);
   return TG_OK;
 }
 
 extern "C" int tg_stem_fit_forward(const tg_stem_fit* cfg, const double* theta, float* det_x,
-                                   float* det_y, void* stream) {
+                                   float* det_y, void* workspace, size_t ws_bytes, void* stream) {
   FitArgs A;
-  int st = fit_args(cfg, theta, &A);
+  int st = fit_args(cfg, theta, workspace, ws_bytes, &A);
   if (st != TG_OK) return st;
   if (!det_x || !det_y) return TG_ERR_INVALID;
   A.forward_only = 1;
   A.ox = det_x;
   A.oy = det_y;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  k_fit_setup<<<(A.n_probes + 255) / 256, 256, 0, s>>>(A);
   k_stem_fit<<<fit_grid(A.n_probes), kFitThreads, 0, s>>>(A);
   return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
 }
@@ -244,15 +272,13 @@ extern "C" int tg_stem_fit_forward(const tg_stem_fit* cfg, const double* theta, 
 extern "C" int tg_stem_fit_loss_grad(const tg_stem_fit* cfg, const double* theta, double* out,
                                      void* workspace, size_t ws_bytes, void* stream) {
   FitArgs A;
-  int st = fit_args(cfg, theta, &A);
+  int st = fit_args(cfg, theta, workspace, ws_bytes, &A);
   if (st != TG_OK) return st;
   if (!out || (A.n > 0 && (!A.tx || !A.ty))) return TG_ERR_INVALID;
-  const int grid = fit_grid(A.n_probes);
-  if (!workspace || ws_bytes < (size_t)grid * kFitOut * sizeof(double)) return TG_ERR_WORKSPACE;
-  A.partial = reinterpret_cast<double*>(workspace);
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-  k_stem_fit<<<grid, kFitThreads, 0, s>>>(A);
-  k_fit_reduce<<<1, 32, 0, s>>>(A.partial, grid, out);
+  k_fit_setup<<<(A.n_probes + 255) / 256, 256, 0, s>>>(A);
+  k_stem_fit<<<fit_grid(A.n_probes), kFitThreads, 0, s>>>(A);
+  k_fit_reduce<<<kFitOut, 256, 0, s>>>(A, out);
   return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
 }
 

@@ -408,9 +408,15 @@ __global__ void k_reduce_partials(const double* __restrict__ partial, int nblock
                                   int width, double* __restrict__ raw) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= width) return;
-  double s = 0.0;
-  for (int b = 0; b < nblocks; ++b) s += partial[(size_t)b * width + i];
-  raw[i] += s;
+  // eight independent partial sums keep eight loads in flight (fixed order)
+  double a[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  int b = 0;
+  for (; b + 8 <= nblocks; b += 8) {
+#pragma unroll
+    for (int u = 0; u < 8; ++u) a[u] += partial[(size_t)(b + u) * width + i];
+  }
+  for (int u = 0; b < nblocks; ++b, ++u) a[u] += partial[(size_t)b * width + i];
+  raw[i] += ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
 }
 
 static int vjp_grid(int64_t n) {

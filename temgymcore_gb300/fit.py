@@ -28,7 +28,7 @@ class TgStemFit(C.Structure):
 
 
 N.register("tg_stem_fit_forward", C.c_int, [C.POINTER(TgStemFit), C.c_void_p, C.c_void_p,
-                                            C.c_void_p, C.c_void_p])
+                                            C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p])
 N.register("tg_stem_fit_workspace", C.c_size_t, [C.c_int32])
 N.register("tg_stem_fit_loss_grad", C.c_int, [C.POINTER(TgStemFit), C.c_void_p, C.c_void_p,
                                               C.c_void_p, C.c_size_t, C.c_void_p])
@@ -86,7 +86,8 @@ class StemFit:
         ox = torch.empty((self.n_probes, self.n), dtype=torch.float32, device=self.dev)
         oy = torch.empty_like(ox)
         N.check(N.lib().tg_stem_fit_forward(C.byref(self._cfg()), th.data_ptr(), ox.data_ptr(),
-                                            oy.data_ptr(), N.stream_ptr()), "tg_stem_fit_forward")
+                                            oy.data_ptr(), self.ws.data_ptr(), self.ws.numel(),
+                                            N.stream_ptr()), "tg_stem_fit_forward")
         return ox, oy
 
     def set_targets(self, theta_true):

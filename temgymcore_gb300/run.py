@@ -419,3 +419,72 @@ def trace_to_image(ray: Ray, components: Sequence[Component], detector: Grid | N
     from . import PixelsYX
     pix = PixelsYX(y=py.reshape(shape), x=px.reshape(shape)) if want_pixels else None
     return out, pix, acc
+
+
+class TracePlan:
+    """A compiled trace for repeated launches on the same device buffers.
+
+    Packs the model once, allocates the outputs once and keeps the C-ABI
+    structures, so ``run()`` is a single C call (no Python allocation) and
+    ``capture()`` records it as a CUDA graph.  ``x, y, dx, dy`` are float32
+    CUDA tensors of equal length whose contents may change between runs;
+    ``z`` and ``pathlength`` are uniform inputs.  With a detector the launch
+    also bins the rays and adds them to ``self.image``.
+    """
+
+    def __init__(self, components, x, y, dx, dy, z=0.0, pathlength=0.0, detector: Grid | None = None,
+                 pixels: bool = False, hist_dtype=torch.int64):
+        N.require_cuda(x)
+        self.comps = _check_model(components)
+        for t in (x, y, dx, dy):
+            if t.dtype != torch.float32 or not t.is_contiguous() or t.numel() != x.numel():
+                raise ValueError("x, y, dx, dy must be contiguous float32 tensors of equal length")
+        self.n = x.numel()
+        self.inputs = (x, y, dx, dy)
+        dev = x.device
+        self.out = tuple(torch.empty(self.n, dtype=torch.float32, device=dev) for _ in range(4))
+        self.pathlength = torch.empty(self.n, dtype=torch.float64, device=dev)
+        self._m, self._keep = pack_model(self.comps)
+        self._in = _rays_struct(self.n, x, y, dx, dy, None, float(z), None, float(pathlength))
+        self._o = _rays_struct(self.n, *self.out, None, 0.0, self.pathlength, 0.0)
+        self._zout = C.c_double(0.0)
+        self.detector = detector
+        self.image = None
+        self.pix = None
+        self._g = None
+        if detector is not None:
+            self._g = detector._tg_grid()
+            h, w = int(detector.shape[0]), int(detector.shape[1])
+            self.image = torch.zeros((h, w), dtype=hist_dtype, device=dev)
+            if pixels:
+                self.pix = (torch.empty(self.n, dtype=torch.int32, device=dev),
+                            torch.empty(self.n, dtype=torch.int32, device=dev))
+        self._lib = N.lib()
+        self.graph = None
+
+    def run(self):
+        pix = self.pix or (None, None)
+        st = self._lib.tg_trace_fwd(C.byref(self._m), C.byref(self._in), C.byref(self._o),
+                                    C.byref(self._zout), C.byref(self._g) if self._g is not None else None,
+                                    N.ptr(pix[0]), N.ptr(pix[1]), N.ptr(self.image),
+                                    1 if (self.image is not None and self.image.dtype == torch.int64) else 0,
+                                    N.stream_ptr())
+        N.check(st, "tg_trace_fwd")
+        return self
+
+    def capture(self):
+        """Record one run as a CUDA graph (``self.graph.replay()``)."""
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            self.run()
+        torch.cuda.current_stream().wait_stream(s)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.run()
+        self.graph = g
+        return g
+
+    def ray(self) -> Ray:
+        return Ray(x=self.out[0], y=self.out[1], dx=self.out[2], dy=self.out[3], z=self._zout.value,
+                   pathlength=self.pathlength)

@@ -296,3 +296,23 @@ def test_readme_gradients_gpu(kats, cuda):
                        [t.Lens(z=0.5, focal_length=1.0), det])
     out.dx.backward()
     assert abs(float(x.grad) - kats["readme_grads"]["ddx_out_dx_in"]) < 1e-6
+
+
+def test_trace_plan_and_graph_match_api(cuda):
+    t = T()
+    from temgymcore_gb300.workloads import build_model, plain_trace
+    w = plain_trace(seed=3, n=10000)
+    model = build_model(w["model"])
+    xs = [torch.tensor(w[k], device=cuda) for k in ("x", "y", "dx", "dy")]
+    out, pix, img = t.trace_to_image(t.Ray(x=xs[0], y=xs[1], dx=xs[2], dy=xs[3], z=0.0, pathlength=0.0),
+                                     model)
+    plan = t.TracePlan(model, *xs, detector=model[-1], pixels=True)
+    plan.run()
+    assert torch.equal(plan.out[0], out.x) and torch.equal(plan.pathlength, out.pathlength)
+    assert torch.equal(plan.image, img) and torch.equal(plan.pix[1], pix.x)
+    g = plan.capture()
+    plan.image.zero_()
+    g.replay()
+    g.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(plan.image, 2 * img)
