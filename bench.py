@@ -412,7 +412,7 @@ def run_only(args):
         from temgymcore_gb300.workloads import batched_sweep, build_model
         w = batched_sweep(seed=0, n_models=args.models or 512)
         bt = BatchedTrace([build_model(s) for s in w["specs"]], w["counts"], tile_rays=4096)
-        bt.block, bt.rpt = 256, 4
+        bt.block, bt.rpt = 256, 2
         x, y, dx, dy, tx, ty = (torch.tensor(w[k], device=dev) for k in ("x", "y", "dx", "dy", "tx", "ty"))
         out, raw = bt.alloc_outputs(), bt.alloc_raw()
         fn = lambda: bt.run(x, y, dx, dy, out, (tx, ty), raw)  # noqa: E731

@@ -196,7 +196,7 @@ int tg_scan_hist(const tg_model *model, const tg_rays *bundle, const tg_scan *sc
 typedef struct tg_batch_info {
   size_t plan_bytes;       /* bytes of the packed plan (copy it to the device) */
   size_t workspace_bytes;  /* device workspace for tg_batch_run              */
-  int32_t n_tiles;
+  int32_t n_tiles;         /* >= 1 per model (an empty model has one empty tile) */
   int32_t total_steps;     /* sum over models of 2 * n_components           */
   int64_t total_rays;
   int32_t max_steps;       /* largest 2 * n_components of one model         */
@@ -235,9 +235,13 @@ int tg_batch_plan(int32_t n_models, const tg_model *models, const int64_t *n_ray
 
 /*
  * tg_batch_run - one persistent launch over every tile of the plan (device
- * copy), forward and (with targets) adjoint, plus a deterministic per-model
- * reduction.  block in {128, 256, 512}; rays_per_thread in {1, 2, 4}.
- * workspace: device, info->workspace_bytes, 256-byte aligned.
+ * copy), forward and (with targets) adjoint; the CTA that completes a model's
+ * last tile reduces that model's tile partials in tile order (deterministic)
+ * and writes its per-step sums, so nothing else is launched besides one
+ * memset of the work counters.  block in {128, 256, 512}; rays_per_thread in
+ * {1, 2, 4}.  workspace: device, info->workspace_bytes, 256-byte aligned.
+ * An aperture does not change the traced state here (the outputs carry no
+ * mask) and the loss covers every ray.
  */
 int tg_batch_run(const void *plan_dev, const tg_batch_info *info, const tg_batch_io *io,
                  int32_t block, int32_t rays_per_thread, void *workspace, size_t ws_bytes,

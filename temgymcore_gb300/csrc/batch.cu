@@ -17,8 +17,9 @@
 //   W[a][c] = sum_i l_a,i v_c,i     (v = input x, y, dx, dy, 1; a = x, y)
 //   S_b[a]  = sum_i sign_b,i l_a,i  (one pair per biprism b)
 // k_batch accumulates the moments next to the forward pass (no reverse walk
-// per ray) and k_batch_steps turns them into the per-step sums with float64
-// 5x5 algebra, one thread per model.
+// per ray); the CTA that finishes a model's last tile reduces its moments and
+// turns them into the per-step sums with 5x5 algebra (batch_model_tail), so
+// one launch does the whole forward + adjoint.
 #include <cstring>
 #include <vector>
 
@@ -62,258 +63,135 @@ __device__ __forceinline__ float bt_warp_sum(float v) {
   return v;
 }
 
-template <int R>
-__global__ void __launch_bounds__(512)
-k_batch(const uint8_t* __restrict__ plan, const __grid_constant__ BatchIO io,
-        int32_t* __restrict__ counter, double* __restrict__ partial) {
-  extern __shared__ float wacc[];  // [warps][n_mom] per-warp float32 moments of this tile
-  __shared__ Op sops[kMaxSteps];
-  __shared__ int s_tile;
-  const int nwarps = blockDim.x >> 5;
-  const int warp = threadIdx.x >> 5;
-  const BHeader H = *reinterpret_cast<const BHeader*>(plan);
-  const BModel* models = reinterpret_cast<const BModel*>(plan + H.models_off);
-  const BTile* tiles = reinterpret_cast<const BTile*>(plan + H.tiles_off);
-  const Op* ops = reinterpret_cast<const Op*>(plan + H.ops_off);
-  const bool adj = io.tx != nullptr;
-  const int lane = threadIdx.x & 31;
-  for (;;) {
-    if (threadIdx.x == 0) s_tile = atomicAdd(counter, 1);
-    __syncthreads();
-    const int t = s_tile;
-    if (t >= H.n_tiles) break;
-    const BTile T = tiles[t];
-    if (T.model < 0 || T.model >= H.n_models) {  // corrupt plan: flag and skip
-      if (threadIdx.x == 0) atomicOr(&g_tg_err, TG_EW_TABLE);
-      __syncthreads();
-      continue;
-    }
-    const BModel M = models[T.model];
-    const int ns = M.n_steps, nm = M.n_mom, nb = M.n_bip;
-    for (int i = threadIdx.x; i < ns; i += blockDim.x) sops[i] = ops[M.op_off + i];
-    if (adj)
-      for (int i = threadIdx.x; i < nwarps * nm; i += blockDim.x) wacc[i] = 0.f;
-    __syncthreads();
-    float mw[10];
-#pragma unroll
-    for (int j = 0; j < 10; ++j) mw[j] = 0.f;
-    const int64_t end = T.start + T.count;
-    for (int64_t blk = T.start; blk < end; blk += (int64_t)blockDim.x * R) {
-      RayS r[R];
-      float v0[R][4];
-      uint64_t sb[R];
-      bool alive[R];
-      double dv[R];
-      int64_t idx[R];
-      bool inr[R];
-#pragma unroll
-      for (int k = 0; k < R; ++k) {
-        idx[k] = blk + (int64_t)threadIdx.x + (int64_t)k * blockDim.x;  // coalesced per k
-        inr[k] = idx[k] < end;
-        const int64_t i = inr[k] ? idx[k] : T.start;
-        v0[k][0] = io.x[i]; v0[k][1] = io.y[i]; v0[k][2] = io.dx[i]; v0[k][3] = io.dy[i];
-        r[k] = RayS{v0[k][0], v0[k][1], v0[k][2], v0[k][3], 0.f};
-        sb[k] = 0;
-        alive[k] = true;
-        dv[k] = 0.0;
-      }
-      for (int s = 0; s < ns; ++s) {
-        const Op op = sops[s];
-#pragma unroll
-        for (int k = 0; k < R; ++k) op_forward(op, nullptr, r[k], 0.0, 0.0, dv[k], sb[k], alive[k]);
-      }
-#pragma unroll
-      for (int k = 0; k < R; ++k) {
-        if (inr[k]) {
-          const int64_t i = idx[k];
-          io.ox[i] = r[k].x;
-          io.oy[i] = r[k].y;
-          io.odx[i] = r[k].dx;
-          io.ody[i] = r[k].dy;
-          if (io.opl) io.opl[i] = M.pl_const + (double)r[k].plv;
-        }
-      }
-      if (!adj) continue;
-      float lx[R], ly[R];
-#pragma unroll
-      for (int k = 0; k < R; ++k) {
-        lx[k] = inr[k] ? 2.f * (r[k].x - io.tx[idx[k]]) : 0.f;
-        ly[k] = inr[k] ? 2.f * (r[k].y - io.ty[idx[k]]) : 0.f;
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          mw[c] = fmaf(lx[k], v0[k][c], mw[c]);
-          mw[5 + c] = fmaf(ly[k], v0[k][c], mw[5 + c]);
-        }
-        mw[4] += lx[k];
-        mw[9] += ly[k];
-      }
-      // biprism sign moments (few per model): warp sums into the warp's row
-      for (int b2 = 0; b2 < nb; ++b2) {
-        float sx = 0.f, sy = 0.f;
-#pragma unroll
-        for (int k = 0; k < R; ++k) {
-          const uint32_t bits = (uint32_t)(sb[k] >> (2 * b2)) & 3u;
-          const float sg = bits == 1u ? 1.f : (bits == 2u ? -1.f : 0.f);
-          sx = fmaf(sg, lx[k], sx);
-          sy = fmaf(sg, ly[k], sy);
-        }
-        sx = bt_warp_sum(sx);
-        sy = bt_warp_sum(sy);
-        if (lane == 0) {
-          wacc[warp * nm + 10 + 2 * b2] += sx;
-          wacc[warp * nm + 11 + 2 * b2] += sy;
-        }
-      }
-    }
-    if (adj) {
-#pragma unroll
-      for (int j = 0; j < 10; ++j) {
-        const float v = bt_warp_sum(mw[j]);
-        if (lane == 0) wacc[warp * nm + j] += v;
-      }
-    }
-    __syncthreads();
-    if (adj) {
-      double* dst = partial + M.part_off + (int64_t)(t - M.tile_off) * nm;
-      for (int i = threadIdx.x; i < nm; i += blockDim.x) {
-        double a = 0.0;
-        for (int w = 0; w < nwarps; ++w) a += (double)wacc[w * nm + i];
-        dst[i] = a;
-      }
-    }
-    __syncthreads();
-  }
-}
+// One component with the free-space step in front of it (the compiled
+// program always alternates the two), 32 bytes: two float4 broadcasts from
+// shared memory per component and one kind test for all of a thread's rays.
+struct FOp {
+  int32_t kind;  // component op (OP_NOP for a plane / detector)
+  int32_t aux;   // OP_BIPRISM: sign slot
+  float d;       // propagation distance before the component
+  float c[5];
+};
+static_assert(sizeof(FOp) == 32, "FOp is two float4");
 
-// moments[e] = sum over the model's tiles of the tile partials, in tile order.
-__global__ void k_batch_reduce(const uint8_t* __restrict__ plan, const double* __restrict__ partial,
-                               double* __restrict__ moments) {
-  const BHeader H = *reinterpret_cast<const BHeader*>(plan);
-  const BModel* models = reinterpret_cast<const BModel*>(plan + H.models_off);
-  const int32_t* mom_model = reinterpret_cast<const int32_t*>(plan + H.mom_model_off);
-  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= H.moment_doubles) return;
-  const BModel M = models[mom_model[e]];
-  const int j = (int)(e - M.mom_off);
-  // eight independent partial sums keep eight loads in flight; the summation
-  // order is fixed, so the result is deterministic
-  double a[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-  const double* src = partial + M.part_off + j;
-  int tt = 0;
-  for (; tt + 8 <= M.n_tiles; tt += 8) {
-#pragma unroll
-    for (int u = 0; u < 8; ++u) a[u] += src[(int64_t)(tt + u) * M.n_mom];
-  }
-  for (int u = 0; tt < M.n_tiles; ++tt, ++u) a[u] += src[(int64_t)tt * M.n_mom];
-  moments[e] = ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
-}
+// Biprism sign moments kept in registers for the first kRegBip biprisms of a
+// model; any further ones are warp-reduced per iteration into shared memory.
+constexpr int kRegBip = 4;
 
-// 5x5 step matrix (linear part + non-biprism offsets) of one compiled step,
-// in the float32 values the forward pass used.
-__device__ void step_matrix(const Op& op, float T[5][5]) {
-  for (int i = 0; i < 5; ++i)
-    for (int j = 0; j < 5; ++j) T[i][j] = (i == j) ? 1.f : 0.f;
+// Entry (i, j) of the 5x5 step matrix of one compiled step (linear part +
+// non-biprism offsets, in the float32 values the forward pass used; 0 outside
+// the 5x5 range).  A biprism's offset enters through its sign moment; the
+// other kinds are the identity.
+__device__ __forceinline__ float t_entry(const Op& op, int i, int j) {
+  if (i > 4 || j > 4) return 0.f;
+  float v = (i == j) ? 1.f : 0.f;
   switch (op.kind) {
-    case OP_FREE: T[0][2] = op.c[0]; T[1][3] = op.c[0]; break;
-    case OP_LENS: T[2][0] = -op.c[0]; T[3][1] = -op.c[0]; break;
-    case OP_SHIFT: T[0][4] = op.c[0]; T[1][4] = op.c[1]; T[2][4] = op.c[2]; T[3][4] = op.c[3]; break;
-    case OP_DEFLECT: T[2][4] = op.c[0]; T[3][4] = op.c[1]; break;
-    case OP_ROTATE: {
-      const float c = op.c[0], sn = op.c[1];
-      T[0][0] = c; T[0][1] = -sn; T[1][0] = sn; T[1][1] = c;
-      T[2][2] = c; T[2][3] = -sn; T[3][2] = sn; T[3][3] = c;
-    } break;
-    default: break;  // biprism offset enters through its sign moment; others are identity
+    case OP_FREE: if ((i == 0 && j == 2) || (i == 1 && j == 3)) v = op.c[0]; break;
+    case OP_LENS: if ((i == 2 && j == 0) || (i == 3 && j == 1)) v = -op.c[0]; break;
+    case OP_SHIFT:  // register selects, not a dynamic index into op.c
+      if (j == 4 && i < 4) v = i == 0 ? op.c[0] : (i == 1 ? op.c[1] : (i == 2 ? op.c[2] : op.c[3]));
+      break;
+    case OP_DEFLECT: if (j == 4 && (i == 2 || i == 3)) v = i == 2 ? op.c[0] : op.c[1]; break;
+    case OP_ROTATE:
+      if (i < 4 && j < 4 && (i >> 1) == (j >> 1)) {
+        const int ii = i & 1, jj = j & 1;
+        v = (ii == jj) ? op.c[0] : (ii == 0 ? -op.c[1] : op.c[1]);
+      }
+      break;
+    default: break;
   }
+  return v;
 }
 
-// One warp per model: per-step sums (the quantities of the generic adjoint)
-// from the moments.  Every lane walks the chain once (the 5x5 prefix/suffix
-// products are short, independent multiply-adds, run in float32 - the
-// precision of the traced rays) and leaves, per step, the adjoint map G_s,
-// the first four rows of the prefix C_s and the moment-weighted biprism
-// offsets E_s in shared memory; then the lanes split the steps and contract
-// them with the moments in float64.
-//   E_{s,a} = sum_b S_b[a] (effect at step s of biprism b's offset), so the
-//   bilinear sum of a step is sum_a (G_s Q C_s)[a] . W[a] + (G_s Q E_{s,a})[a].
+// Step s of the compiled program (propagator, component, propagator, ...)
+// rebuilt from the fused per-component records staged in shared memory.
+__device__ __forceinline__ Op fused_step(const FOp* f, int s) {
+  Op o;
+  const FOp& c = f[s >> 1];
+  if ((s & 1) == 0) {
+    o.kind = OP_FREE;
+    o.aux = 0;
+    o.c[0] = c.d;
+    for (int j = 1; j < 6; ++j) o.c[j] = 0.f;
+  } else {
+    o.kind = c.kind;
+    o.aux = c.aux;
+    for (int j = 0; j < 5; ++j) o.c[j] = c.c[j];
+    o.c[5] = 0.f;
+  }
+  return o;
+}
+
+// Adjoint tail of one model, run by the CTA that stored the model's last tile
+// partial (all threads of the CTA call it).  Per-step sums, the quantities of
+// the generic adjoint, follow from the moments:
+//  1. moments = sum of the tile partials in tile order (each warp takes a
+//     moment; its lanes stride over tiles; a fixed shuffle tree combines them,
+//     so the result is deterministic);
+//  2. warp 0 walks the chain backwards for G_s = linear part of
+//     (T_{ns-1} ... T_{s+1}) and warp 1 walks it forwards for the first four
+//     rows of the prefix C_s and the moment-weighted biprism offsets E_s
+//     (E_{s,a} = sum_b S_b[a] (effect at step s of biprism b's offset)); the
+//     5x5 products run in float32, the precision of the traced rays;
+//  3. every thread contracts steps with the moments in float64:
+//     sum_a (G_s Q C_s)[a] . W[a] + (G_s Q E_{s,a})[a].
 constexpr int kStepFloats = 16 + 20 + 8;  // G_s, C_s rows 0..3, E_s (a = x, y)
 
-__global__ void __launch_bounds__(32)
-k_batch_steps(const uint8_t* __restrict__ plan, const double* __restrict__ moments,
-              double* __restrict__ raw) {
-  extern __shared__ float st[];  // [n_steps][kStepFloats]
-  const BHeader H = *reinterpret_cast<const BHeader*>(plan);
-  const int m = blockIdx.x;
-  if (m >= H.n_models) return;
-  const BModel M = reinterpret_cast<const BModel*>(plan + H.models_off)[m];
-  const Op* ops = reinterpret_cast<const Op*>(plan + H.ops_off) + M.op_off;
-  const double* mo = moments + M.mom_off;
-  const int ns = M.n_steps;
-  const int lane = threadIdx.x;
-  {  // backward: G_s = linear part of (T_{ns-1} ... T_{s+1}); lambda after s = G_s^T l
-    float Rm[4][4];
-    for (int i = 0; i < 4; ++i)
-      for (int j = 0; j < 4; ++j) Rm[i][j] = (i == j) ? 1.f : 0.f;
+__device__ void batch_model_tail(const BModel& M, const FOp* fops, const double* partial,
+                                 double* moments_g, double* raw, float* smem) {
+  const int nm = M.n_mom, ns = M.n_steps;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  double* mo = reinterpret_cast<double*>(smem);                // [nm]
+  float* st = reinterpret_cast<float*>(mo + ((nm + 1) & ~1));  // [ns][kStepFloats]
+  const double* src = partial + M.part_off;
+  for (int j = warp; j < nm; j += nwarps) {
+    double a = 0.0;
+    for (int t = lane; t < M.n_tiles; t += 32) a += __ldcg(src + (int64_t)t * nm + j);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if (lane == 0) {
+      mo[j] = a;
+      moments_g[M.mom_off + j] = a;
+    }
+  }
+  __syncthreads();
+  // The chain walks keep one matrix element per lane and combine them with
+  // shuffles (same multiply-add order as a row-by-column product).
+  if (warp == 0) {  // backward: G_s, lanes 0..15 own Rm[i][j], i = lane / 4, j = lane % 4
+    const int i = lane >> 2, j = lane & 3;
+    float rm = (i == j && lane < 16) ? 1.f : 0.f;
     for (int s = ns - 1; s >= 0; --s) {
-      if (lane == 0)
-        for (int i = 0; i < 16; ++i) st[s * kStepFloats + i] = Rm[i >> 2][i & 3];
-      float T[5][5];
-      step_matrix(ops[s], T);
-      float N2[4][4];
-      for (int i = 0; i < 4; ++i)
-        for (int j = 0; j < 4; ++j) {
-          float v = 0.f;
-          for (int k = 0; k < 4; ++k) v = fmaf(Rm[i][k], T[k][j], v);
-          N2[i][j] = v;
-        }
-      for (int i = 0; i < 4; ++i)
-        for (int j = 0; j < 4; ++j) Rm[i][j] = N2[i][j];
+      if (lane < 16) st[s * kStepFloats + lane] = rm;
+      const Op op = fused_step(fops, s);
+      float v = 0.f;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) v = fmaf(__shfl_sync(0xffffffffu, rm, (i * 4 + k) & 31), t_entry(op, k, j), v);
+      rm = v;
     }
-  }
-  {  // forward: C_s and E_s
-    float Cm[5][5], E[2][4];
-    for (int i = 0; i < 5; ++i)
-      for (int j = 0; j < 5; ++j) Cm[i][j] = (i == j) ? 1.f : 0.f;
-    for (int a = 0; a < 2; ++a)
-      for (int j = 0; j < 4; ++j) E[a][j] = 0.f;
+  } else if (warp == 1) {  // forward: lanes 0..24 own Cm[i][j] (i = lane / 5); lanes 0..7 own E[a][ie]
+    const int i = lane / 5, j = lane % 5;
+    const int a = lane >> 2, ie = lane & 3;
+    float cm = (i == j && lane < 25) ? 1.f : 0.f;
+    float e = 0.f;
     for (int s = 0; s < ns; ++s) {
-      const Op op = ops[s];
-      float T[5][5];
-      step_matrix(op, T);
-      float N5[5][5];
-      for (int i = 0; i < 5; ++i)
-        for (int j = 0; j < 5; ++j) {
-          float v = 0.f;
-          for (int k = 0; k < 5; ++k) v = fmaf(T[i][k], Cm[k][j], v);
-          N5[i][j] = v;
-        }
-      for (int i = 0; i < 5; ++i)
-        for (int j = 0; j < 5; ++j) Cm[i][j] = N5[i][j];
-      for (int a = 0; a < 2; ++a) {
-        float ne[4];
-        for (int i = 0; i < 4; ++i) {
-          float v = 0.f;
-          for (int k = 0; k < 4; ++k) v = fmaf(T[i][k], E[a][k], v);
-          ne[i] = v;
-        }
-        for (int i = 0; i < 4; ++i) E[a][i] = ne[i];
-      }
-      if (op.kind == OP_BIPRISM) {  // this biprism's offset def * sign * e_dx, weighted by S_b
-        E[0][2] += (float)(op.c[0] * mo[10 + 2 * op.aux]);
-        E[1][2] += (float)(op.c[0] * mo[11 + 2 * op.aux]);
-      }
-      if (lane == 0) {
-        float* o = st + s * kStepFloats + 16;
-        for (int i = 0; i < 4; ++i)
-          for (int j = 0; j < 5; ++j) o[5 * i + j] = Cm[i][j];
-        for (int a = 0; a < 2; ++a)
-          for (int j = 0; j < 4; ++j) o[20 + 4 * a + j] = E[a][j];
-      }
+      const Op op = fused_step(fops, s);
+      float v = 0.f;
+#pragma unroll
+      for (int k = 0; k < 5; ++k) v = fmaf(t_entry(op, i, k), __shfl_sync(0xffffffffu, cm, (k * 5 + j) & 31), v);
+      float ve = 0.f;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) ve = fmaf(t_entry(op, ie, k), __shfl_sync(0xffffffffu, e, (a * 4 + k) & 31), ve);
+      cm = v;
+      e = ve;
+      if (op.kind == OP_BIPRISM && lane < 8 && ie == 2)  // this biprism's offset def * sign * e_dx, weighted by S_b
+        e += (float)(op.c[0] * mo[10 + 2 * op.aux + a]);
+      if (lane < 20) st[s * kStepFloats + 16 + lane] = cm;  // rows 0..3
+      if (lane < 8) st[s * kStepFloats + 36 + lane] = e;
     }
   }
-  __syncwarp();
-  for (int s = lane; s < ns; s += 32) {
-    const Op op = ops[s];
+  __syncthreads();
+  for (int s = threadIdx.x; s < ns; s += blockDim.x) {
+    const Op op = fused_step(fops, s);
     const float* Gs = st + s * kStepFloats;       // Gs[4*i+j]
     const float* Cs = Gs + 16;                    // Cs[5*i+j], rows 0..3
     const float* Es = Gs + 36;                    // Es[4*a+j]
@@ -338,35 +216,265 @@ k_batch_steps(const uint8_t* __restrict__ plan, const double* __restrict__ momen
       }
       return acc;
     };
-    double r4[4] = {0.0, 0.0, 0.0, 0.0};
+    double r0 = 0.0, r1 = 0.0, r2 = 0.0, r3 = 0.0;
     switch (op.kind) {
       case OP_FREE: {
         const float Q[4][4] = {{0, 0, 1, 0}, {0, 0, 0, 1}, {0, 0, 0, 0}, {0, 0, 0, 0}};
-        r4[0] = bil(Q);
+        r0 = bil(Q);
       } break;
       case OP_LENS: {
         const float k2 = op.c[0] * op.c[0];
         const float Q[4][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}, {k2, 0, 0, 0}, {0, k2, 0, 0}};
-        r4[0] = bil(Q);
+        r0 = bil(Q);
       } break;
       case OP_ROTATE: {
         const float Q[4][4] = {{0, -1, 0, 0}, {1, 0, 0, 0}, {0, 0, 0, -1}, {0, 0, 1, 0}};
-        r4[0] = bil(Q);
+        r0 = bil(Q);
       } break;
       case OP_SHIFT:
-        r4[0] = lin(0); r4[1] = lin(1); r4[2] = lin(2); r4[3] = lin(3);
+        r0 = lin(0); r1 = lin(1); r2 = lin(2); r3 = lin(3);
         break;
       case OP_DEFLECT:
-        r4[0] = lin(2); r4[1] = lin(3);
+        r0 = lin(2); r1 = lin(3);
         break;
       case OP_BIPRISM: {
         const int b = op.aux;
-        r4[0] = (double)Gs[0 * 4 + 2] * mo[10 + 2 * b] + (double)Gs[1 * 4 + 2] * mo[11 + 2 * b];
+        r0 = (double)Gs[0 * 4 + 2] * mo[10 + 2 * b] + (double)Gs[1 * 4 + 2] * mo[11 + 2 * b];
       } break;
       default: break;
     }
     double* out = raw + (int64_t)(M.op_off + s) * 4;
-    out[0] = r4[0]; out[1] = r4[1]; out[2] = r4[2]; out[3] = r4[3];
+    out[0] = r0; out[1] = r1; out[2] = r2; out[3] = r3;
+  }
+}
+
+template <int R>
+__global__ void __launch_bounds__(512, (R == 4 ? 1 : 2))  // R = 1, 2: <= 64 registers (32 warps per SM)
+k_batch(const uint8_t* __restrict__ plan, const __grid_constant__ BatchIO io,
+        int32_t* __restrict__ counter, int32_t* __restrict__ done, double* __restrict__ partial,
+        double* __restrict__ moments) {
+  // dynamic shared memory: [warps][n_mom] per-warp float32 moments of the tile,
+  // reused by the model's adjoint tail (moments + per-step products)
+  extern __shared__ __align__(16) float wacc[];
+  __shared__ int s_last;
+  __shared__ __align__(16) FOp sops[TG_MAX_COMPONENTS];
+  __shared__ int s_tile;
+  const int nwarps = blockDim.x >> 5;
+  const int warp = threadIdx.x >> 5;
+  const BHeader H = *reinterpret_cast<const BHeader*>(plan);
+  const BModel* models = reinterpret_cast<const BModel*>(plan + H.models_off);
+  const BTile* tiles = reinterpret_cast<const BTile*>(plan + H.tiles_off);
+  const Op* ops = reinterpret_cast<const Op*>(plan + H.ops_off);
+  const bool adj = io.tx != nullptr;
+  const int lane = threadIdx.x & 31;
+  const float4* sf4 = reinterpret_cast<const float4*>(sops);
+  for (;;) {
+    if (threadIdx.x == 0) s_tile = atomicAdd(counter, 1);
+    __syncthreads();
+    const int t = s_tile;
+    if (t >= H.n_tiles) break;
+    const BTile T = tiles[t];
+    if (T.model < 0 || T.model >= H.n_models) {  // corrupt plan: flag and skip
+      if (threadIdx.x == 0) atomicOr(&g_tg_err, TG_EW_TABLE);
+      __syncthreads();
+      continue;
+    }
+    const BModel M = models[T.model];
+    const int nc = M.n_steps >> 1, nm = M.n_mom, nb = M.n_bip;
+    for (int i = threadIdx.x; i < nc; i += blockDim.x) {
+      const Op fr = ops[M.op_off + 2 * i], co = ops[M.op_off + 2 * i + 1];
+      FOp f;
+      f.kind = co.kind;
+      f.aux = co.aux;
+      f.d = fr.c[0];
+      for (int j = 0; j < 5; ++j) f.c[j] = co.c[j];
+      if (fr.kind != OP_FREE) {  // the batched plan only holds uniform propagators
+        atomicOr(&g_tg_err, TG_EW_TABLE);
+        f.d = 0.f;
+      }
+      sops[i] = f;
+    }
+    if (adj)
+      for (int i = threadIdx.x; i < nwarps * nm; i += blockDim.x) wacc[i] = 0.f;
+    __syncthreads();
+    // tile-local 32-bit indexing from per-tile base pointers
+    const float* __restrict__ gx = io.x + T.start;
+    const float* __restrict__ gy = io.y + T.start;
+    const float* __restrict__ gdx = io.dx + T.start;
+    const float* __restrict__ gdy = io.dy + T.start;
+    float mw[10];
+#pragma unroll
+    for (int j = 0; j < 10; ++j) mw[j] = 0.f;
+    float bsx[kRegBip], bsy[kRegBip];
+#pragma unroll
+    for (int j = 0; j < kRegBip; ++j) bsx[j] = bsy[j] = 0.f;
+    const int cnt = T.count;
+    for (int it = 0; it < cnt; it += blockDim.x * R) {
+      float x[R], y[R], dx[R], dy[R], pl[R], v0[R][4], tx[R], ty[R];
+      uint32_t spos[R], sneg[R];  // biprism b: bit b set when sign(x) > 0 / < 0
+      int idx[R];
+      bool inr[R];
+#pragma unroll
+      for (int k = 0; k < R; ++k) {
+        idx[k] = it + (int)threadIdx.x + k * (int)blockDim.x;  // coalesced per k
+        inr[k] = idx[k] < cnt;
+        const int i = inr[k] ? idx[k] : 0;
+        v0[k][0] = gx[i]; v0[k][1] = gy[i]; v0[k][2] = gdx[i]; v0[k][3] = gdy[i];
+        if (adj) {
+          tx[k] = io.tx[T.start + i];
+          ty[k] = io.ty[T.start + i];
+        }
+        x[k] = v0[k][0]; y[k] = v0[k][1]; dx[k] = v0[k][2]; dy[k] = v0[k][3];
+        pl[k] = 0.f;
+        spos[k] = sneg[k] = 0u;
+      }
+      for (int s = 0; s < nc; ++s) {
+        const float4 A = sf4[2 * s], B = sf4[2 * s + 1];  // {kind, aux, d, c0}, {c1..c4}
+        const int kind = __float_as_int(A.x);
+        const float d = A.z;
+#pragma unroll
+        for (int k = 0; k < R; ++k) {
+          x[k] = fmaf(dx[k], d, x[k]);
+          y[k] = fmaf(dy[k], d, y[k]);
+        }
+        if (kind == OP_LENS) {
+          const float k1 = A.w, h = B.x;
+#pragma unroll
+          for (int k = 0; k < R; ++k) {
+            const float xx = x[k], yy = y[k];
+            pl[k] -= (xx * xx + yy * yy) * h;
+            dx[k] = fmaf(-xx, k1, dx[k]);
+            dy[k] = fmaf(-yy, k1, dy[k]);
+          }
+        } else if (kind == OP_BIPRISM) {
+          const uint32_t bit = 1u << __float_as_int(A.y);  // slot < 32
+#pragma unroll
+          for (int k = 0; k < R; ++k) {
+            pl[k] += dx[k] * x[k] + dy[k] * y[k];
+            const float sg = sgnf(x[k]);
+            spos[k] |= sg > 0.f ? bit : 0u;
+            sneg[k] |= sg < 0.f ? bit : 0u;
+            dx[k] = fmaf(A.w, sg, dx[k]);
+          }
+        } else if (kind == OP_DEFLECT) {
+#pragma unroll
+          for (int k = 0; k < R; ++k) {
+            pl[k] += dx[k] * x[k] + dy[k] * y[k];
+            dx[k] += A.w;
+            dy[k] += B.x;
+          }
+        } else if (kind == OP_SHIFT) {
+#pragma unroll
+          for (int k = 0; k < R; ++k) {
+            x[k] += A.w; y[k] += B.x; dx[k] += B.y; dy[k] += B.z;
+          }
+        } else if (kind == OP_ROTATE) {
+          const float c = A.w, sn = B.x;
+#pragma unroll
+          for (int k = 0; k < R; ++k) {
+            const float xx = x[k], yy = y[k], ddx = dx[k], ddy = dy[k];
+            x[k] = xx * c - yy * sn;
+            y[k] = xx * sn + yy * c;
+            dx[k] = ddx * c - ddy * sn;
+            dy[k] = ddx * sn + ddy * c;
+          }
+        }
+        // OP_APERTURE / OP_NOP: no change to the traced state (the batched
+        // outputs carry no mask; the loss covers every ray)
+      }
+#pragma unroll
+      for (int k = 0; k < R; ++k) {
+        if (inr[k]) {
+          const int64_t i = T.start + idx[k];
+          io.ox[i] = x[k];
+          io.oy[i] = y[k];
+          io.odx[i] = dx[k];
+          io.ody[i] = dy[k];
+          if (io.opl) io.opl[i] = M.pl_const + (double)pl[k];
+        }
+      }
+      if (!adj) continue;
+      float lx[R], ly[R];
+#pragma unroll
+      for (int k = 0; k < R; ++k) {
+        lx[k] = inr[k] ? 2.f * (x[k] - tx[k]) : 0.f;
+        ly[k] = inr[k] ? 2.f * (y[k] - ty[k]) : 0.f;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          mw[c] = fmaf(lx[k], v0[k][c], mw[c]);
+          mw[5 + c] = fmaf(ly[k], v0[k][c], mw[5 + c]);
+        }
+        mw[4] += lx[k];
+        mw[9] += ly[k];
+      }
+      // biprism sign moments: registers for the first kRegBip, warp sums beyond
+#pragma unroll
+      for (int b2 = 0; b2 < kRegBip; ++b2) {
+        if (b2 < nb) {
+#pragma unroll
+          for (int k = 0; k < R; ++k) {
+            const float sg = (spos[k] >> b2) & 1u ? 1.f : ((sneg[k] >> b2) & 1u ? -1.f : 0.f);
+            bsx[b2] = fmaf(sg, lx[k], bsx[b2]);
+            bsy[b2] = fmaf(sg, ly[k], bsy[b2]);
+          }
+        }
+      }
+      for (int b2 = kRegBip; b2 < nb; ++b2) {
+        float sx = 0.f, sy = 0.f;
+#pragma unroll
+        for (int k = 0; k < R; ++k) {
+          const float sg = (spos[k] >> b2) & 1u ? 1.f : ((sneg[k] >> b2) & 1u ? -1.f : 0.f);
+          sx = fmaf(sg, lx[k], sx);
+          sy = fmaf(sg, ly[k], sy);
+        }
+        sx = bt_warp_sum(sx);
+        sy = bt_warp_sum(sy);
+        if (lane == 0) {
+          wacc[warp * nm + 10 + 2 * b2] += sx;
+          wacc[warp * nm + 11 + 2 * b2] += sy;
+        }
+      }
+    }
+    if (adj) {
+#pragma unroll
+      for (int j = 0; j < 10; ++j) {
+        const float v = bt_warp_sum(mw[j]);
+        if (lane == 0) wacc[warp * nm + j] += v;
+      }
+#pragma unroll
+      for (int b2 = 0; b2 < kRegBip; ++b2) {
+        if (b2 < nb) {
+          const float sx = bt_warp_sum(bsx[b2]), sy = bt_warp_sum(bsy[b2]);
+          if (lane == 0) {
+            wacc[warp * nm + 10 + 2 * b2] += sx;
+            wacc[warp * nm + 11 + 2 * b2] += sy;
+          }
+        }
+      }
+    }
+    __syncthreads();
+    if (adj) {
+      // warp 0 stores the tile partial and counts the tile; the CTA that
+      // counts a model's last tile runs its adjoint tail (only warp 0 waits
+      // for the fence, the other warps' ray stores are not ordered with it)
+      if (warp == 0) {
+        double* dst = partial + M.part_off + (int64_t)(t - M.tile_off) * nm;
+        for (int i = lane; i < nm; i += 32) {
+          double a = 0.0;
+          for (int w = 0; w < nwarps; ++w) a += (double)wacc[w * nm + i];
+          dst[i] = a;
+        }
+        __threadfence();
+        __syncwarp();
+        if (lane == 0) s_last = atomicAdd(done + T.model, 1) == M.n_tiles - 1;
+      }
+      __syncthreads();
+      if (s_last) {
+        __threadfence();
+        batch_model_tail(M, sops, partial, moments, io.raw, wacc);
+      }
+    }
+    __syncthreads();
   }
 }
 
@@ -382,6 +490,7 @@ static int sm_count_batch() {
 }
 
 static inline int64_t al16(int64_t v) { return (v + 15) & ~(int64_t)15; }
+static inline int64_t al256(int64_t v) { return (v + 255) & ~(int64_t)255; }
 
 }  // namespace tg
 
@@ -422,7 +531,9 @@ extern "C" int tg_batch_plan(int32_t n_models, const tg_model* models, const int
     for (int s = 0; s < P.n_steps; ++s) ops.push_back(P.op[s]);
     for (int j = 0; j < M.n_mom; ++j) mom_model.push_back(m);
     int32_t nt = 0;
-    for (int64_t r = 0; r < n_rays[m]; r += tile_rays, ++nt) {
+    // at least one tile per model: an empty model's tile (count 0) still runs
+    // the model's adjoint tail, which then writes zero sums
+    for (int64_t r = 0; r < n_rays[m] || nt == 0; r += tile_rays, ++nt) {
       BTile T;
       T.model = m;
       T.start = ray_off + r;
@@ -457,8 +568,8 @@ extern "C" int tg_batch_plan(int32_t n_models, const tg_model* models, const int
   info->n_models = n_models;
   info->partial_doubles = part_off;
   info->moment_doubles = mom_off;
-  // workspace: counter | tile partials | moments
-  info->workspace_bytes = 256 + (size_t)(part_off + mom_off) * sizeof(double);
+  // workspace: tile counter + per-model done counters | tile partials | moments
+  info->workspace_bytes = (size_t)al256(4 + 4 * (int64_t)n_models) + (size_t)(part_off + mom_off) * sizeof(double);
   if (!plan) return TG_OK;  // size query
   if (plan_bytes < (size_t)off) return TG_ERR_WORKSPACE;
   uint8_t* p = reinterpret_cast<uint8_t*>(plan);
@@ -487,8 +598,11 @@ extern "C" int tg_batch_run(const void* plan_dev, const tg_batch_info* info, con
   if (((uintptr_t)workspace & 255) != 0) return TG_ERR_ALIGN;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   int32_t* counter = reinterpret_cast<int32_t*>(workspace);
-  double* partial = reinterpret_cast<double*>(reinterpret_cast<uint8_t*>(workspace) + 256);
-  if (cudaMemsetAsync(counter, 0, sizeof(int32_t), s) != cudaSuccess) return TG_ERR_CUDA;
+  int32_t* done = counter + 1;
+  const size_t head = (size_t)al256(4 + 4 * (int64_t)info->n_models);
+  double* partial = reinterpret_cast<double*>(reinterpret_cast<uint8_t*>(workspace) + head);
+  double* moments = partial + info->partial_doubles;
+  if (cudaMemsetAsync(counter, 0, 4 + 4 * (size_t)info->n_models, s) != cudaSuccess) return TG_ERR_CUDA;
   if (info->n_tiles == 0) return TG_OK;
   BatchIO A;
   A.x = io->x; A.y = io->y; A.dx = io->dx; A.dy = io->dy;
@@ -497,8 +611,14 @@ extern "C" int tg_batch_run(const void* plan_dev, const tg_batch_info* info, con
   A.tx = io->target_x; A.ty = io->target_y;
   A.raw = io->raw;
   const uint8_t* plan = reinterpret_cast<const uint8_t*>(plan_dev);
-  // per-warp float32 moments: warps x max moments (10 + 2 per biprism)
-  const size_t dyn = (size_t)(block / 32) * (info->max_moments > 0 ? info->max_moments : 10) * sizeof(float);
+  // dynamic shared memory: per-warp float32 moments (warps x max moments),
+  // reused by the adjoint tail for the moments (float64) and the per-step products
+  const size_t mom = (size_t)(info->max_moments > 0 ? info->max_moments : 10);
+  const size_t tail = adj ? ((mom + 1) & ~(size_t)1) * sizeof(double) +
+                                (size_t)(info->max_steps > 0 ? info->max_steps : 1) * kStepFloats * sizeof(float)
+                          : 0;
+  size_t dyn = (size_t)(block / 32) * mom * sizeof(float);
+  if (tail > dyn) dyn = tail;
   if (dyn > 48 * 1024) return TG_ERR_TOO_LARGE;
   int per_sm = 1;
   if (rays_per_thread == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<1>, block, dyn);
@@ -507,16 +627,8 @@ extern "C" int tg_batch_run(const void* plan_dev, const tg_batch_info* info, con
   if (per_sm < 1) per_sm = 1;
   int grid = sm_count_batch() * per_sm;
   if (grid > info->n_tiles) grid = info->n_tiles;
-  if (rays_per_thread == 1) k_batch<1><<<grid, block, dyn, s>>>(plan, A, counter, partial);
-  else if (rays_per_thread == 2) k_batch<2><<<grid, block, dyn, s>>>(plan, A, counter, partial);
-  else k_batch<4><<<grid, block, dyn, s>>>(plan, A, counter, partial);
-  if (adj && info->total_steps > 0) {
-    // moments then per-step sums; sizes come from the plan header on the device
-    double* moments = partial + info->partial_doubles;
-    const int64_t nmom = info->moment_doubles;
-    k_batch_reduce<<<(int)((nmom + 255) / 256), 256, 0, s>>>(plan, partial, moments);
-    const size_t sm_steps = (size_t)(info->max_steps > 0 ? info->max_steps : 1) * kStepFloats * sizeof(float);
-    k_batch_steps<<<info->n_models, 32, sm_steps, s>>>(plan, moments, io->raw);
-  }
+  if (rays_per_thread == 1) k_batch<1><<<grid, block, dyn, s>>>(plan, A, counter, done, partial, moments);
+  else if (rays_per_thread == 2) k_batch<2><<<grid, block, dyn, s>>>(plan, A, counter, done, partial, moments);
+  else k_batch<4><<<grid, block, dyn, s>>>(plan, A, counter, done, partial, moments);
   return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
 }
