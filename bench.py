@@ -30,7 +30,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "fwd+grad ray·component steps/s; field beam·px/s at stated err vs FP64 oracle"
+METRIC = "fwd+grad ray·component steps/s; field beam·px/s at stated err vs the float64 kernel"
 UNIT = "ray·component steps/s"
 SCAN = (64, 64)
 RAYS = 1024
@@ -262,11 +262,52 @@ def _time(torch, fn, reps):
     return a.elapsed_time(b) / reps
 
 
+def _field_errors(plan, ref, methods, into):
+    """Normwise field error and the phase error at bright pixels (> 25% of the
+    peak) of each method against a reference image."""
+    scale = np.max(np.abs(ref))
+    bright = np.abs(ref) > 0.25 * scale
+    for name in methods:
+        g = plan.evaluate(name).cpu().numpy().astype(np.complex128)
+        ph = float(np.max(np.abs(np.angle(g[bright] * np.conj(ref[bright]))))) if bright.any() else None
+        into[name].update({"field_rel_err_vs_fp64_kernel": float(np.max(np.abs(g - ref)) / scale),
+                           "phase_err_rad_bright": ph})
+
+
+def secondary_input_field(torch, dev, bf16):
+    """Input-plane beamlet field (evaluate_gaussian_input_image): 16,384
+    overlapping beams on 512 x 512 pixels; separable split-BF16 GEMM and the
+    fast direct kernel (astigmatic beams), errors against the float64 kernel."""
+    import temgymcore_gb300 as t
+    from temgymcore_gb300.workloads import build_model, gaussian_rays, input_field
+    w = input_field(seed=0)
+    grid = build_model([w["grid"]])[0]
+    pairs = 16384 * 512 * 512
+    plan = t.FieldPlan(gaussian_rays(w["rays"]), None, grid=grid)
+    res = {"workload": f"16,384 beams on a golden-angle spiral (waist {w['waist']:.3g} m, lambda 500 nm, "
+                       "slopes N(0,1e-4)), their own plane sampled on 512x512 pixels of 1e-5 m",
+           "separable": plan.separable}
+    ms_sep = _time(torch, lambda: plan.evaluate("separable"), 20)
+    ms_dir = _time(torch, lambda: plan.evaluate("direct"), 3)
+    gemm_flops = 12 * 2 * 512 * 512 * 16416
+    res["separable_gemm"] = {"ms": ms_sep, "beam_px_per_s": pairs / (ms_sep * 1e-3),
+                             "frac_of_bf16_peak": gemm_flops / (ms_sep * 1e-3) / 1e12 / bf16}
+    res["direct_fast"] = {"ms": ms_dir, "beam_px_per_s": pairs / (ms_dir * 1e-3)}
+    ref = plan.evaluate("fp64").clone().cpu().numpy().astype(np.complex128)
+    _field_errors(plan, ref, ("separable", "direct"),
+                  {"separable": res["separable_gemm"], "direct": res["direct_fast"]})
+    wa = input_field(seed=0, astigmatic=True)
+    pa = t.FieldPlan(gaussian_rays(wa["rays"]), None, grid=grid)
+    ms_a = _time(torch, lambda: pa.evaluate("direct"), 3)
+    res["astigmatic_direct"] = {"ms": ms_a, "beam_px_per_s": pairs / (ms_a * 1e-3), "separable": pa.separable}
+    return res
+
+
 def secondary_field(torch, dev, hbm, bf16):
     """Gaussian-beamlet field, 16,384 beams on 512 x 512 pixels: separable
     split-BF16 tensor-core GEMM, fast direct kernel (astigmatic beams) and the
-    all-float64 direct kernel, with errors against the float64 oracle on a
-    pixel sample (exact k*pl reduction)."""
+    all-float64 direct kernel; errors of the fast paths against the float64
+    kernel's image (exact k*pl reduction)."""
     import temgymcore_gb300 as t
     from temgymcore_gb300.workloads import beamlet_field, build_model, gaussian_rays
     res = {"workload": "16,384 beamlets (aperture decomposition, waist 1e-9 m, lambda 1.97e-12 m, "
@@ -290,22 +331,11 @@ def secondary_field(torch, dev, hbm, bf16):
     res["direct_fp64"] = {"ms": ms_f64, "beam_px_per_s": pairs / (ms_f64 * 1e-3)}
     res["speedup_separable_vs_fp64"] = ms_f64 / ms_sep
     res["prep_plan_ms"] = ms_prep
-    # errors against the float64 oracle on a pixel sample
-    try:
-        from oracle import field as OF
-        rng = np.random.default_rng(1)
-        idx = rng.choice(512 * 512, 48, replace=False)
-        ref = OF.make_gaussian_image(w["rays"], w["model"], pixel_index=idx, chunk=2048)
-        scale = np.max(np.abs(ref))
-        for name in ("separable", "direct", "fp64"):
-            g = plan.evaluate(name).reshape(-1)[torch.as_tensor(idx, device=dev)].cpu().numpy()
-            err = np.max(np.abs(g - ref)) / scale
-            bright = np.abs(ref) > 0.25 * scale
-            ph = float(np.max(np.abs(np.angle(g[bright] * np.conj(ref[bright]))))) if bright.any() else None
-            res[{"separable": "separable_gemm", "direct": "direct_fast", "fp64": "direct_fp64"}[name]].update(
-                {"field_rel_err": float(err), "phase_err_rad_bright": ph})
-    except Exception as e:
-        res["oracle_error"] = repr(e)
+    # errors against the all-float64 kernel's image (that kernel is held to
+    # 5e-7 of the float64 oracle by the tests; the bench itself runs no oracle)
+    ref = plan.evaluate("fp64").clone().cpu().numpy().astype(np.complex128)
+    _field_errors(plan, ref, ("separable", "direct"),
+                  {"separable": res["separable_gemm"], "direct": res["direct_fast"]})
     # astigmatic case (direct kernel only)
     wa = beamlet_field(seed=0, astigmatic=True)
     pa = t.FieldPlan(gaussian_rays(wa["rays"]), build_model(wa["model"]))
@@ -391,7 +421,13 @@ def run_only(args):
 
     import temgymcore_gb300 as t
     dev = torch.device("cuda", torch.cuda.current_device())
-    if args.only.startswith("field"):
+    if args.only in ("field-input", "field-input-astig"):
+        from temgymcore_gb300.workloads import build_model, gaussian_rays, input_field
+        w = input_field(seed=0, n_beams=args.beams or 16384, astigmatic=args.only == "field-input-astig")
+        plan = t.FieldPlan(gaussian_rays(w["rays"]), None, grid=build_model([w["grid"]])[0])
+        meth = "direct" if args.only == "field-input-astig" else "separable"
+        fn = lambda: plan.evaluate(meth)  # noqa: E731
+    elif args.only.startswith("field"):
         from temgymcore_gb300.workloads import beamlet_field, build_model, gaussian_rays
         beams = args.beams or 16384
         w = beamlet_field(seed=0, n_beams=beams, astigmatic=args.only == "field-astig")
@@ -489,6 +525,11 @@ def secondary_batched(torch, dev, hbm):
             "ms": ms, "ray_component_steps_per_s": steps / (ms * 1e-3), "rays_per_s": total / (ms * 1e-3),
             "algorithmic_bytes": alg, "achieved_gbs": alg / (ms * 1e-3) / 1e9,
             "frac_of_hbm": alg / (ms * 1e-3) / 1e9 / hbm,
+            # separate forward and adjoint passes would move 64 B/ray (forward
+            # 16 in + 24 out, adjoint 16 in + 8 targets); the fused launch reads
+            # the inputs once, 48 B/ray
+            "bytes_separate_passes": total * 64,
+            "frac_of_hbm_separate_passes": total * 64 / (ms * 1e-3) / 1e9 / hbm,
             "autotuned": {"tile_rays": best[0], "block": best[1], "rays_per_thread": best[2]},
             "autotune_ms": None if results is None else [[r[1], r[2], r[3], r[0]] for r in results],
             "plain_per_model_ms": ms_plain, "speedup_vs_plain_per_model": ms_plain / ms}
@@ -580,6 +621,10 @@ def run_gpu(args, world, rank, local):
         except Exception as e:
             secondary["beamlet_field"] = {"error": repr(e)}
         try:
+            secondary["input_field"] = secondary_input_field(torch, dev, bf16)
+        except Exception as e:
+            secondary["input_field"] = {"error": repr(e)}
+        try:
             secondary["adjoint_fit"] = secondary_fit(torch, dev)
         except Exception as e:
             secondary["adjoint_fit"] = {"error": repr(e)}
@@ -615,7 +660,7 @@ def main():
                     help="skip the secondary workloads, e2e and CPU baseline")
     ap.add_argument("--only", default=None,
                     help="profile one workload alone: field-separable, field-direct, field-astig, "
-                         "field-fp64, fit, batched, plain")
+                         "field-fp64, field-input, field-input-astig, fit, batched, plain")
     ap.add_argument("--beams", type=int, default=None)
     ap.add_argument("--rays", type=int, default=None)
     ap.add_argument("--models", type=int, default=None)

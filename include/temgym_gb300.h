@@ -333,6 +333,17 @@ int tg_field_prep(const tg_model *model, const tg_beams *beams, const tg_pixel_m
                   void *workspace, size_t ws_bytes, int32_t *flags, void *stream);
 
 /*
+ * tg_field_prep_input - the same records for the field of the beams in their
+ * own plane, sampled on the pixel map (evaluate_gaussian_input_image,
+ * gaussian.py:372-427): per pixel r1 and beam,
+ *   amplitude * exp(i (k/2) ((r1 - r1m)^T Q1^-1 (r1 - r1m) + 2 (r1 - r1m).theta1m)) * exp(i k pl).
+ * No model and no ABCD; tg_field_eval then sums the beams exactly as for the
+ * detector field (the separable method applies when Q1^-1 has no xy term).
+ */
+int tg_field_prep_input(const tg_beams *beams, const tg_pixel_map *pm, void *workspace,
+                        size_t ws_bytes, int32_t *flags, void *stream);
+
+/*
  * tg_field_eval - the field sum over beams at every detector pixel into out
  * (device complex64 [h][w], overwritten).  Replaces gaussian.py:319-369
  * propagate_misaligned_gaussian_jax_scan + map_reduce (and the reshape in

@@ -8,6 +8,8 @@ Follows:
   - ``_beam_field``                              gaussian.py:276-316
   - ``propagate_misaligned_gaussian_jax_scan``   gaussian.py:319-337
   - ``map_reduce`` (a plain sum over beams)      gaussian.py:340-369
+  - ``evaluate_gaussian_input_image``            gaussian.py:372-400
+  - ``_input_beam_field``                        gaussian.py:403-409
   - ``fibonacci_spiral``                         utils.py:297-325
 
 2x2 inverses are written out explicitly (the reference calls
@@ -164,6 +166,52 @@ def make_gaussian_image(rays: dict, model, pixel_index=None, chunk=64, phase_mod
         acc += beam_field_pixels(amp[sl], phase_offset[sl], q1inv[sl], q2inv[sl], r1m[sl],
                                  t1m[sl], A[sl], B[sl], e[sl], f[sl], k[sl], r2,
                                  None if po is None else po[sl]).sum(0)
+    if pixel_index is not None:
+        return acc
+    return acc.reshape(grid["shape"])
+
+
+def _beams(rays: dict):
+    x = np.asarray(rays["x"], np.float64).ravel()
+    n = x.size
+    bc = lambda v: np.broadcast_to(np.asarray(v, np.float64), (n,)).copy()  # noqa: E731
+    return dict(
+        x=x, y=bc(rays["y"]), dx=bc(rays["dx"]), dy=bc(rays["dy"]), pl=bc(rays["pathlength"]),
+        wl=bc(rays["wavelength"]), theta=bc(rays["theta"]),
+        amp=np.broadcast_to(np.asarray(rays["amplitude"], np.complex128), (n,)).copy(),
+        waist=np.broadcast_to(np.asarray(rays["waist_xy"], np.float64), (n, 2)),
+        radii=np.broadcast_to(np.asarray(rays["radii_of_curv"], np.float64), (n, 2)), n=n)
+
+
+def input_beam_field_pixels(amp, q1inv, r1m, t1m, k, r1, po):
+    """gaussian.py:403-409 for a chunk of beams over pixels r1 (P, 2):
+    a * exp(i (k/2) (d^T Q1 d + 2 d.t1m)) * exp(i p), d = r1 - r1m."""
+    d = r1[None, :, :] - r1m[:, None, :]
+    quad = np.einsum("npi,nij,npj->np", d, q1inv, d)
+    tilt = 2 * np.einsum("npi,ni->np", d, t1m)
+    phase = (k[:, None] / 2) * (quad + tilt)
+    return amp[:, None] * np.exp(1j * phase) * np.exp(1j * po[:, None])
+
+
+def evaluate_gaussian_input_image(rays: dict, grid: dict, pixel_index=None, chunk=64,
+                                  phase_mode="exact"):
+    """gaussian.py:372-400: the beams' field in their own plane sampled on
+    ``grid`` (no model).  Same ``rays`` keys and ``phase_mode`` as
+    ``make_gaussian_image``."""
+    b = _beams(rays)
+    q1inv = Q_inv(b["waist"], b["radii"], b["wl"], b["theta"])
+    r1 = grid_coords(grid)
+    if pixel_index is not None:
+        r1 = r1[np.asarray(pixel_index).ravel()]
+    k = 2 * np.pi / b["wl"]
+    po = phase_offset_exact(k, b["pl"]) if phase_mode == "exact" else k * b["pl"]
+    r1m = np.stack([b["x"], b["y"]], -1)
+    t1m = np.stack([b["dx"], b["dy"]], -1)
+    acc = np.zeros(r1.shape[0], dtype=np.complex128)
+    for s in range(0, b["n"], chunk):
+        sl = slice(s, s + chunk)
+        acc += input_beam_field_pixels(b["amp"][sl], q1inv[sl], r1m[sl], t1m[sl], k[sl], r1,
+                                       po[sl]).sum(0)
     if pixel_index is not None:
         return acc
     return acc.reshape(grid["shape"])

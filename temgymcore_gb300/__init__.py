@@ -67,6 +67,7 @@ from .run import (  # noqa: E402,F401
     run_to_end, run_iter, solve_model, abcd_matrix, trace_to_image, pack_model, TracePlan,
 )
 from .scan import scan_images, scan_positions, probe_model  # noqa: E402,F401
-from .gaussian import make_gaussian_image, FieldPlan, fibonacci_spiral  # noqa: E402,F401
+from .gaussian import (  # noqa: E402,F401
+    make_gaussian_image, evaluate_gaussian_input_image, FieldPlan, fibonacci_spiral)
 
 __version__ = "0.1.0"

@@ -127,6 +127,7 @@ struct PrepArgs {
   BeamFast* fast;
   BeamF64* f64;
   int32_t* flags;  // [0]: non-separable beams seen
+  int32_t input_plane;  // 1: field of the beams in their own plane (no model)
 };
 
 __global__ void __launch_bounds__(128)
@@ -209,33 +210,48 @@ k_field_prep(const __grid_constant__ DModel M, const __grid_constant__ PrepArgs 
   // R D R^T with R = [[c, -s], [s, c]]
   cm2 Q1i{cth * cth * qx + sth * sth * qy, cth * sth * qx - sth * cth * qy,
           sth * cth * qx - cth * sth * qy, sth * sth * qx + cth * cth * qy};
-  // ---- Q2^-1 = (A + B Q1i)^-1 (C + D Q1i)   (gaussian.py:92-96)
-  const cm2 denom = madd(Am, mm(Bm, Q1i));
-  const cm2 Q2 = mm(inv2c(denom), madd(Cm, mm(Dm, Q1i)));
-  const cm2 Binv = nan_to_num(inv2c(Bm));
-  const cm2 Q1 = nan_to_num(inv2c(Q1i));
-  // central ray at output: r2m = A r1m + B theta1m
-  const double r2mx = m[0][0] * x0 + m[0][1] * y0 + m[0][2] * dx0 + m[0][3] * dy0;
-  const double r2my = m[1][0] * x0 + m[1][1] * y0 + m[1][2] * dx0 + m[1][3] * dy0;
-  const cd det = denom.a * denom.d - denom.b * denom.c;
   const cd amp = C((double)A.amp[2 * b], (double)A.amp[2 * b + 1]);
-  const cd pref = cdiv(amp, csqrt_(det));
-  const cm2 ABinv = mm(Am, Binv);
-  const cm2 P = mm(Q1, inv2c(mm(Bm, madd(mm(Am, Q1), Bm))));
   const double k = 2.0 * PI / wl;
   const double hk = 0.5 * k;
-  // quadratic (symmetric part), linear and constant terms in s = r2 - e
-  const cd Sxx = Q2.a, Syy = Q2.d, Sxy = 0.5 * (Q2.b + Q2.c);
-  // Binv^T r1m and P^T r2m
-  const cd bx = Binv.a * C(x0) + Binv.c * C(y0), by = Binv.b * C(x0) + Binv.d * C(y0);
-  const cd px_ = P.a * C(r2mx) + P.c * C(r2my), py_ = P.b * C(r2mx) + P.d * C(r2my);
-  const cd Lx = C(2.0 * fx) - 2.0 * bx + 2.0 * px_;
-  const cd Ly = C(2.0 * fy) - 2.0 * by + 2.0 * py_;
-  const cd q1 = C(x0) * (ABinv.a * C(x0) + ABinv.b * C(y0)) + C(y0) * (ABinv.c * C(x0) + ABinv.d * C(y0));
-  const cd q2 = C(r2mx) * (P.a * C(r2mx) + P.b * C(r2my)) + C(r2my) * (P.c * C(r2mx) + P.d * C(r2my));
-  const cd c0 = q1 - q2;
+  // Phase polynomial (k/2) (s^T S s + L.s + c0) of the pixel position r,
+  // s = r - origin, and the prefactor pref:
+  cd Sxx, Syy, Sxy, Lx, Ly, c0, pref;
+  double ox, oy;
+  if (A.input_plane) {
+    // the beams in their own plane (gaussian.py:402-409): s = r1 - r1m,
+    // S = Q1^-1, L = 2 theta1m, no constant, pref = amplitude
+    Sxx = Q1i.a; Syy = Q1i.d; Sxy = 0.5 * (Q1i.b + Q1i.c);
+    Lx = C(2.0 * dx0); Ly = C(2.0 * dy0);
+    c0 = C(0.0);
+    pref = amp;
+    ox = x0; oy = y0;
+  } else {
+    // ---- Q2^-1 = (A + B Q1i)^-1 (C + D Q1i)   (gaussian.py:92-96)
+    const cm2 denom = madd(Am, mm(Bm, Q1i));
+    const cm2 Q2 = mm(inv2c(denom), madd(Cm, mm(Dm, Q1i)));
+    const cm2 Binv = nan_to_num(inv2c(Bm));
+    const cm2 Q1 = nan_to_num(inv2c(Q1i));
+    // central ray at output: r2m = A r1m + B theta1m
+    const double r2mx = m[0][0] * x0 + m[0][1] * y0 + m[0][2] * dx0 + m[0][3] * dy0;
+    const double r2my = m[1][0] * x0 + m[1][1] * y0 + m[1][2] * dx0 + m[1][3] * dy0;
+    const cd det = denom.a * denom.d - denom.b * denom.c;
+    pref = cdiv(amp, csqrt_(det));
+    const cm2 ABinv = mm(Am, Binv);
+    const cm2 P = mm(Q1, inv2c(mm(Bm, madd(mm(Am, Q1), Bm))));
+    // quadratic (symmetric part), linear and constant terms in s = r2 - e
+    Sxx = Q2.a; Syy = Q2.d; Sxy = 0.5 * (Q2.b + Q2.c);
+    // Binv^T r1m and P^T r2m
+    const cd bx = Binv.a * C(x0) + Binv.c * C(y0), by = Binv.b * C(x0) + Binv.d * C(y0);
+    const cd px_ = P.a * C(r2mx) + P.c * C(r2my), py_ = P.b * C(r2mx) + P.d * C(r2my);
+    Lx = C(2.0 * fx) - 2.0 * bx + 2.0 * px_;
+    Ly = C(2.0 * fy) - 2.0 * by + 2.0 * py_;
+    const cd q1 = C(x0) * (ABinv.a * C(x0) + ABinv.b * C(y0)) + C(y0) * (ABinv.c * C(x0) + ABinv.d * C(y0));
+    const cd q2 = C(r2mx) * (P.a * C(r2mx) + P.b * C(r2my)) + C(r2my) * (P.c * C(r2mx) + P.d * C(r2my));
+    c0 = q1 - q2;
+    ox = e0x; oy = e0y;
+  }
   // pixel map: s = s0 + row*u + col*v
-  const double s0x = A.pm.t[5] - e0x, s0y = A.pm.t[2] - e0y;
+  const double s0x = A.pm.t[5] - ox, s0y = A.pm.t[2] - oy;
   const double ux = A.pm.t[3], uy = A.pm.t[0], vx = A.pm.t[4], vy = A.pm.t[1];
   auto quad = [&](double ax, double ay, double bx2, double by2) -> cd {  // a^T S b
     return C(ax * bx2) * Sxx + C(ay * by2) * Syy + C(ax * by2 + ay * bx2) * Sxy;
@@ -664,18 +680,16 @@ extern "C" size_t tg_field_workspace(int64_t n_beams, int32_t h, int32_t w, int3
   return field_layout(n_beams, h, w, method).total;
 }
 
-extern "C" int tg_field_prep(const tg_model* model, const tg_beams* beams,
-                             const tg_pixel_map* pm, void* workspace, size_t ws_bytes,
-                             int32_t* flags, void* stream) {
-  if (!model || !beams || !pm || pm->h <= 0 || pm->w <= 0 || beams->n < 0) return TG_ERR_INVALID;
+namespace tg {
+static int field_prep_launch(const DModel& dm, const tg_beams* beams, const tg_pixel_map* pm,
+                             void* workspace, size_t ws_bytes, int32_t* flags, void* stream,
+                             int input_plane) {
+  if (!beams || !pm || pm->h <= 0 || pm->w <= 0 || beams->n < 0) return TG_ERR_INVALID;
   if (beams->n > 0 && (!beams->x || !beams->y || !beams->dx || !beams->dy || !beams->pathlength ||
                        !beams->amplitude || !beams->waist_xy || !beams->radii))
     return TG_ERR_INVALID;
   FieldLayout L = field_layout(beams->n, pm->h, pm->w, TG_FIELD_DIRECT);
   if (!workspace || ws_bytes < L.part) return TG_ERR_WORKSPACE;
-  DModel dm;
-  int st = build_dmodel(model, beams->z, &dm);
-  if (st != TG_OK) return st;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   char* ws = reinterpret_cast<char*>(workspace);
   int32_t* fl = flags ? flags : reinterpret_cast<int32_t*>(ws + L.flags);
@@ -699,9 +713,28 @@ extern "C" int tg_field_prep(const tg_model* model, const tg_beams* beams,
   A.fast = reinterpret_cast<BeamFast*>(ws + L.fast);
   A.f64 = reinterpret_cast<BeamF64*>(ws + L.f64);
   A.flags = fl;
+  A.input_plane = input_plane;
   int blocks = (int)((beams->n + 127) / 128);
   k_field_prep<<<blocks, 128, 0, s>>>(dm, A);
   return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
+}
+}  // namespace tg
+
+extern "C" int tg_field_prep(const tg_model* model, const tg_beams* beams,
+                             const tg_pixel_map* pm, void* workspace, size_t ws_bytes,
+                             int32_t* flags, void* stream) {
+  if (!model || !beams) return TG_ERR_INVALID;
+  DModel dm;
+  int st = build_dmodel(model, beams->z, &dm);
+  if (st != TG_OK) return st;
+  return field_prep_launch(dm, beams, pm, workspace, ws_bytes, flags, stream, 0);
+}
+
+extern "C" int tg_field_prep_input(const tg_beams* beams, const tg_pixel_map* pm, void* workspace,
+                                   size_t ws_bytes, int32_t* flags, void* stream) {
+  DModel dm;
+  std::memset(&dm, 0, sizeof(dm));
+  return field_prep_launch(dm, beams, pm, workspace, ws_bytes, flags, stream, 1);
 }
 
 extern "C" int tg_field_eval(int32_t method, int64_t n_beams, const tg_pixel_map* pm,

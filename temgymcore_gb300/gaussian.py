@@ -13,6 +13,10 @@ beams x pixels run in the C-ABI kernels of ``csrc/field.cu`` and
   method="fp64"       every (beam, pixel) term in float64 (comparator);
   method="auto"       "separable" when every beam qualifies, else "direct".
 
+``evaluate_gaussian_input_image(gaussian_rays, grid)`` (gaussian.py:372-427)
+is the beams' field in their own plane: the same records and sum, with the
+per-beam polynomial taken from Q1^-1 and the central ray directly (no model).
+
 ``batch_size`` is accepted for signature compatibility; the GPU path needs no
 (batch, npix) temporary.
 """
@@ -48,6 +52,8 @@ class TgPixelMap(C.Structure):
 N.register("tg_field_workspace", C.c_size_t, [C.c_int64, C.c_int32, C.c_int32, C.c_int32])
 N.register("tg_field_prep", C.c_int, [C.POINTER(N.TgModel), C.POINTER(TgBeams), C.POINTER(TgPixelMap),
                                       C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p])
+N.register("tg_field_prep_input", C.c_int, [C.POINTER(TgBeams), C.POINTER(TgPixelMap), C.c_void_p,
+                                            C.c_size_t, C.c_void_p, C.c_void_p])
 N.register("tg_field_eval", C.c_int, [C.c_int32, C.c_int64, C.POINTER(TgPixelMap), C.c_void_p,
                                       C.c_void_p, C.c_size_t, C.c_void_p])
 
@@ -124,13 +130,24 @@ class BeamSet:
 
 
 class FieldPlan:
-    """Prepared beams + workspace for repeated field evaluations."""
+    """Prepared beams + workspace for repeated field evaluations.
 
-    def __init__(self, gaussian_rays: GaussianRay, model, method: str = "auto"):
-        comps = _check_model(model)
-        grid = comps[-1]
-        if not isinstance(grid, Grid):
-            raise ValueError("the last model element must be a Detector grid (gaussian.py:231-232)")
+    ``model``: component list ending in the detector Grid (the detector field,
+    gaussian.py:225-273); or ``model=None`` with ``grid=`` for the field of
+    the beams in their own plane (gaussian.py:372-427)."""
+
+    def __init__(self, gaussian_rays: GaussianRay, model, method: str = "auto", *, grid=None):
+        if not isinstance(gaussian_rays, GaussianRay):
+            raise TypeError("gaussian_rays must be a GaussianRay (gaussian.py:228)")
+        comps = None
+        if model is None:
+            if not isinstance(grid, Grid):
+                raise ValueError("the input-plane field needs a Grid (gaussian.py:377-381)")
+        else:
+            comps = _check_model(model)
+            grid = comps[-1]
+            if not isinstance(grid, Grid):
+                raise ValueError("the last model element must be a Detector grid (gaussian.py:231-232)")
         self.dev = _device()
         self.beams = BeamSet(gaussian_rays, self.dev)
         self.pm = pixel_map(grid)
@@ -141,11 +158,16 @@ class FieldPlan:
         self.ws_ptr = self.ws.data_ptr() + off
         self.ws_bytes = self.ws.numel() - off
         self.flags = torch.zeros(1, dtype=torch.int32, device=self.dev)
-        m, keep = pack_model(comps)
-        st = N.lib().tg_field_prep(C.byref(m), C.byref(self.beams.struct()), C.byref(self.pm),
-                                   self.ws_ptr, self.ws_bytes, self.flags.data_ptr(), N.stream_ptr())
-        del keep
-        N.check(st, "tg_field_prep")
+        if comps is None:
+            st = N.lib().tg_field_prep_input(C.byref(self.beams.struct()), C.byref(self.pm), self.ws_ptr,
+                                             self.ws_bytes, self.flags.data_ptr(), N.stream_ptr())
+            N.check(st, "tg_field_prep_input")
+        else:
+            m, keep = pack_model(comps)
+            st = N.lib().tg_field_prep(C.byref(m), C.byref(self.beams.struct()), C.byref(self.pm),
+                                       self.ws_ptr, self.ws_bytes, self.flags.data_ptr(), N.stream_ptr())
+            del keep
+            N.check(st, "tg_field_prep")
         if method == "auto":
             method = "separable" if int(self.flags.item()) == 0 else "direct"
         if method not in _METHODS:
@@ -172,6 +194,14 @@ def make_gaussian_image(gaussian_rays: GaussianRay, model, batch_size: int = 128
     """Complex64 detector field (H, W) of the Gaussian beamlets after ``model``
     (gaussian.py:225-273)."""
     plan = FieldPlan(gaussian_rays, model, method)
+    return plan.evaluate().clone()
+
+
+def evaluate_gaussian_input_image(gaussian_rays: GaussianRay, grid, batch_size: int = 128,
+                                  method: str = "auto") -> torch.Tensor:
+    """Complex64 field (H, W) of the Gaussian beamlets in their own plane,
+    sampled at the pixel centres of ``grid`` (gaussian.py:372-400)."""
+    plan = FieldPlan(gaussian_rays, None, method, grid=grid)
     return plan.evaluate().clone()
 
 

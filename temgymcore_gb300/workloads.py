@@ -151,6 +151,37 @@ def beamlet_field(seed: int = 0, n_beams: int = 16384, det_shape=(512, 512), det
     return {"rays": rays, "model": spec}
 
 
+def input_field(seed: int = 0, n_beams: int = 16384, grid_shape=(512, 512), px: float = 1e-5,
+                wavelength: float = 500e-9, astigmatic: bool = False):
+    """Input-plane beamlet field (an image decomposed into Gaussians, the use
+    of evaluate_gaussian_input_image, gaussian.py:372-427).
+
+    ``n_beams`` beams on a golden-angle spiral filling a disc of 0.4 of the
+    grid half-width; waist = the mean beam spacing (so neighbours overlap),
+    flat wavefront; slopes N(0, 1e-4) rad; amplitudes |a| ~ U(0.5, 1), phase
+    U(0, 2 pi); pathlength N(0, 1e-6) m; wavelength 500 nm.  Grid: a detector
+    of ``grid_shape`` pixels of ``px`` m at z = 0.  ``astigmatic``: waist_y =
+    waist * U(0.5, 1.5), theta ~ U(0, pi).
+    """
+    from .gaussian import fibonacci_spiral
+    rng = np.random.default_rng(seed)
+    radius = 0.4 * 0.5 * min(grid_shape) * px
+    x, y = fibonacci_spiral(n_beams, radius, alpha=0)
+    waist = float(np.sqrt(np.pi * radius ** 2 / n_beams))
+    amp = (rng.uniform(0.5, 1.0, n_beams) * np.exp(1j * rng.uniform(0, 2 * np.pi, n_beams))
+           ).astype(np.complex64)
+    wxy = np.full((n_beams, 2), waist)
+    theta = np.zeros(n_beams)
+    if astigmatic:
+        wxy[:, 1] = waist * rng.uniform(0.5, 1.5, n_beams)
+        theta = rng.uniform(0.0, np.pi, n_beams)
+    rays = {"x": x, "y": y, "dx": rng.normal(0.0, 1e-4, n_beams), "dy": rng.normal(0.0, 1e-4, n_beams),
+            "z": 0.0, "pathlength": rng.normal(0.0, 1e-6, n_beams), "amplitude": amp, "waist_xy": wxy,
+            "radii_of_curv": np.full((n_beams, 2), np.inf), "wavelength": wavelength, "theta": theta}
+    grid = {"kind": "detector", "z": 0.0, "pixel_size": (px, px), "shape": tuple(grid_shape)}
+    return {"rays": rays, "grid": grid, "waist": waist}
+
+
 def gaussian_rays(d: dict):
     """GaussianRay from a ``beamlet_field`` ray dict."""
     from .ray import GaussianRay

@@ -198,3 +198,60 @@ def test_phase_reduction_exact():
     # the literal float64 product is off by up to ~ulp(3e12) / 2 ~ 2.4e-4 rad
     lit = np.angle(np.exp(1j * (k * pl)))
     assert np.abs(np.angle(np.exp(1j * (lit - red)))).max() > 1e-6
+
+
+def _one_beam(x0, y0, dx, dy, wavelength=500e-9, w0=1e-4, theta=0.0, waist=None):
+    return {"x": np.array([x0]), "y": np.array([y0]), "dx": np.array([dx]), "dy": np.array([dy]),
+            "z": 0.0, "pathlength": np.array([0.0]), "amplitude": np.array([1.0 + 0j]),
+            "waist_xy": np.array([[w0, w0]] if waist is None else [waist]),
+            "radii_of_curv": np.array([[np.inf, np.inf]]), "wavelength": wavelength,
+            "theta": np.array([theta])}
+
+
+def test_oracle_input_field_phase_ramp():
+    """tests/test_gaussians.py:736-786: the input-plane field of a tilted beam
+    has zero phase at its centre and a phase slope k * tilt."""
+    from oracle import field as OF
+    from oracle.grid import grid_coords
+    det = {"kind": "detector", "z": 0.0, "pixel_size": (1e-5, 1e-5), "shape": (512, 512)}
+    xy = grid_coords(det).reshape(512, 512, 2)
+    det_x, det_y = xy[0, :, 0], xy[:, 0, 1]
+    ix = iy = 256
+    wl = 500e-9
+    k = 2 * np.pi / wl
+    for dx, dy in ((2e-4, 0.0), (0.0, -1e-4), (1.5e-4, -1.0e-4)):
+        img = OF.evaluate_gaussian_input_image(_one_beam(det_x[ix], det_y[iy], dx, dy, wl), det)
+        assert abs(np.angle(img[iy, ix])) < 1e-6
+        rp = np.unwrap(np.angle(img[iy, :]))
+        cp = np.unwrap(np.angle(img[:, ix]))
+        sx = (rp[ix + 8] - rp[ix - 8]) / (det_x[ix + 8] - det_x[ix - 8])
+        sy = (cp[iy + 8] - cp[iy - 8]) / (det_y[iy + 8] - det_y[iy - 8])
+        np.testing.assert_allclose(sx, k * dx, rtol=2e-2, atol=1e-3)
+        np.testing.assert_allclose(sy, k * dy, rtol=2e-2, atol=1e-3)
+
+
+def _principal_axis_angle(field, X, Y):
+    intensity = np.abs(field) ** 2
+    w = intensity.sum() + 1e-30
+    xb, yb = (intensity * X).sum() / w, (intensity * Y).sum() / w
+    cxx = (intensity * (X - xb) ** 2).sum() / w
+    cyy = (intensity * (Y - yb) ** 2).sum() / w
+    cxy = (intensity * (X - xb) * (Y - yb)).sum() / w
+    vals, vecs = np.linalg.eigh(np.array([[cxx, cxy], [cxy, cyy]]))
+    v = vecs[:, np.argmax(vals)]
+    return (np.arctan2(v[1], v[0]) + np.pi / 2) % np.pi - np.pi / 2
+
+
+def test_oracle_input_field_astigmatic_rotation():
+    """tests/test_gaussians.py:818-877: the major axis of an astigmatic input
+    beam follows theta."""
+    from oracle import field as OF
+    from oracle.grid import grid_coords
+    det = {"kind": "detector", "z": 0.0, "pixel_size": (1e-5, 1e-5), "shape": (512, 512)}
+    xy = grid_coords(det).reshape(512, 512, 2)
+    X, Y = xy[..., 0], xy[..., 1]
+    for th in (np.pi / 3, np.pi / 6, 0.0, -np.pi / 6, -np.pi / 3, -np.pi / 2 + 0.1):
+        img = OF.evaluate_gaussian_input_image(_one_beam(0.0, 0.0, 0.0, 0.0, theta=th,
+                                                         waist=[2e-4, 1e-4]), det)
+        phi = _principal_axis_angle(img, X, Y)
+        assert abs(np.arctan2(np.sin(phi - th), np.cos(phi - th))) < 0.1
