@@ -342,6 +342,13 @@ __device__ __forceinline__ float2 cexpf_turn(float logamp, uint64_t turns) {
   return make_float2(a * c, a * s);
 }
 
+// Per (beam, strip) the log-amplitude decides how the strip is summed: skip
+// when it stays below kDirSkipLog (e^-60 of a unit amplitude), the geometric
+// recurrence while its start and per-step ratios stay inside float32 range
+// (|log| < 80), otherwise a per-pixel evaluation.
+constexpr float kDirSkipLog = -60.f;
+constexpr float kDirRecurMax = 80.f;
+
 template <int L>
 __global__ void __launch_bounds__(kDirThreads)
 k_field_direct(const __grid_constant__ DirArgs A) {
@@ -378,19 +385,43 @@ k_field_direct(const __grid_constant__ DirArgs A) {
       const float dr = (float)row - B.r0, dc = (float)col0 - B.c0;
       const float la = B.e0 - (B.b_cc * dc * dc + B.b_rr * dr * dr + B.b_rc * dr * dc + B.l_c * dc + B.l_r * dr);
       const float dla = -(B.b_cc * (2.f * dc + 1.f) + B.b_rc * dr + B.l_c);
-      float2 z = cexpf_turn(la, th);
-      float2 w = cexpf_turn(dla, dth);
-      const float rr = B.rho_re, ri = B.rho_im;
+      // log-amplitude along the strip: la(j) = la + j dla - b_cc j (j - 1)
+      const float jl = (float)(L - 1);
+      const float la_end = la + jl * dla - B.b_cc * jl * (jl - 1.f);
+      const float dla_end = dla - 2.f * B.b_cc * (jl - 1.f);
+      float jv = B.b_cc > 0.f ? 0.5f + dla / (2.f * B.b_cc) : (dla > 0.f ? jl : 0.f);
+      jv = fminf(fmaxf(jv, 0.f), jl);
+      const float la_max = fmaxf(fmaxf(la, la_end), la + jv * dla - B.b_cc * jv * (jv - 1.f));
+      if (!(la_max > kDirSkipLog)) continue;  // below e^-60 of unit amplitude everywhere (or NaN)
+      if (la > -kDirRecurMax && fabsf(dla) < kDirRecurMax && fabsf(dla_end) < kDirRecurMax) {
+        // the geometric recurrence stays inside float32 range: z_j+1 = z_j w_j, w_j+1 = w_j rho
+        float2 z = cexpf_turn(la, th);
+        float2 w = cexpf_turn(dla, dth);
+        const float rr = B.rho_re, ri = B.rho_im;
 #pragma unroll
-      for (int j = 0; j < L; ++j) {
-        are[j] += z.x;
-        aim[j] += z.y;
-        float zr = z.x * w.x - z.y * w.y;
-        float zi = z.x * w.y + z.y * w.x;
-        z = make_float2(zr, zi);
-        float wr = w.x * rr - w.y * ri;
-        float wi = w.x * ri + w.y * rr;
-        w = make_float2(wr, wi);
+        for (int j = 0; j < L; ++j) {
+          are[j] += z.x;
+          aim[j] += z.y;
+          float zr = z.x * w.x - z.y * w.y;
+          float zi = z.x * w.y + z.y * w.x;
+          z = make_float2(zr, zi);
+          float wr = w.x * rr - w.y * ri;
+          float wi = w.x * ri + w.y * rr;
+          w = make_float2(wr, wi);
+        }
+      } else {
+        // a beam narrow against the strip: every pixel evaluated directly
+        // (exact fixed-point phase stepped by integer differences)
+        const uint64_t ddth = 2 * B.p_cc;
+#pragma unroll
+        for (int j = 0; j < L; ++j) {
+          const float fj = (float)j;
+          const float2 z = cexpf_turn(la + fj * dla - B.b_cc * fj * (fj - 1.f), th);
+          are[j] += z.x;
+          aim[j] += z.y;
+          th += dth;
+          dth += ddth;
+        }
       }
     }
   }
