@@ -59,7 +59,14 @@ enum tg_kind {
   TG_BIPRISM = 5,   /* p[0] = def_x                                        */
   TG_ROTATOR = 6,   /* p[0] = angle in degrees                             */
   TG_THICKLENS = 7, /* z = z_po; p[0] = focal_length; p[1] = z_pi          */
-  TG_APERTURE = 8   /* p[0] = radius; p[1..2] = centre x, y (extension)    */
+  TG_APERTURE = 8,  /* p[0] = radius; p[1..2] = centre x, y (extension)    */
+  TG_ABERLENS = 9   /* AberratedLensKrivanek: p[0] = focal_length;        */
+                    /* p[1..25] = C10, C12, phi12, C21, phi21, C23, phi23, */
+                    /* C30, C32, phi32, C34, phi34, C41, phi41, C43, phi43,*/
+                    /* C45, phi45, C50, C52, phi52, C54, phi54, C56, phi56 */
+                    /* (aberrations.py:5-31 order).  Forward trace, scan,  */
+                    /* ABCD and field prep only (adjoint, batched: status  */
+                    /* TG_ERR_UNSUPPORTED); at most 4 per model.           */
 };
 
 /* component flag: scan position comes from the probe (tg_scan_*) */
@@ -69,7 +76,7 @@ typedef struct tg_component {
   int32_t kind;  /* enum tg_kind */
   int32_t flags; /* TG_FLAG_* */
   double z;      /* axial position in metres (ThickLens: z_po) */
-  double p[24];  /* kind-specific parameters, see enum tg_kind */
+  double p[32];  /* kind-specific parameters, see enum tg_kind */
 } tg_component;
 
 typedef struct tg_model {

@@ -28,7 +28,8 @@ import numpy as np
 
 from .grid import grid_coords
 from .phase import phase_offset_exact
-from .rays import ORay, comp_z, propagate, apply_component, component_matrix, free_matrix
+from .rays import (ORay, aberrated_lens_matrix, apply_component, comp_z, component_matrix,  # noqa: F401
+                   free_matrix, propagate)
 
 
 def q_inv(waist_xy, radii, wavelength):
@@ -90,6 +91,8 @@ def beam_abcd(x, y, dx, dy, z, model):
         if c["kind"] == "biprism":
             cm = np.broadcast_to(np.eye(5), (n, 5, 5)).copy()
             cm[:, 2, 4] = c.get("def_x", 0.0) * np.sign(r.x)
+        elif c["kind"] == "aberrated_lens":
+            cm = np.stack([aberrated_lens_matrix(c, r.x[i], r.y[i], r.dx[i], r.dy[i]) for i in range(n)])
         else:
             cm = np.broadcast_to(component_matrix(c), (n, 5, 5))
         total = cm @ total

@@ -6,6 +6,10 @@ Follows, operation by operation:
   - ``run_iter`` / ``run_to_end``    run.py:47-116 (a propagator is inserted
     before EVERY component, with per-ray distance ``component.z - ray.z``)
   - components                       components.py:137-559
+  - ``AberratedLensKrivanek``        components.py:177-215 with
+    ``W_krivanek`` / ``grad_W_krivanek`` aberrations.py:42-108 (polar form,
+    atan2 / hypot / cos(m phi) exactly as written there); its Jacobian for the
+    ABCD by central differences of that gradient
   - ``custom_jacobian_matrix``       utils.py:7-43 (rows/cols x, y, dx, dy, _one)
   - ``solve_model``                  run.py:150-179
   - ``accumulate_matrices``          transfer.py:126-147 (M_last @ ... @ M_0)
@@ -133,7 +137,101 @@ def apply_component(c: dict, r: ORay) -> ORay:
         ok = rr < c["radius"] ** 2
         alive = ok if r.alive is None else (r.alive & ok)
         return r.copy(alive=alive)
+    if k == "aberrated_lens":  # components.py:193-215
+        f = c["focal_length"]
+        x, y, dx, dy = r.x, r.y, r.dx, r.dy
+        ideal_dx = -x / f + dx
+        ideal_dy = -y / f + dy
+        alpha = np.hypot(ideal_dx, ideal_dy)
+        phi = np.arctan2(ideal_dy, ideal_dx)
+        dwx, dwy = grad_w_krivanek(ideal_dx, ideal_dy, c.get("coeffs", {}))
+        return r.copy(dx=ideal_dx + (-dwx / f), dy=ideal_dy + (-dwy / f),
+                      pathlength=r.pathlength - (x ** 2 + y ** 2) / (2 * f)
+                      + w_krivanek(alpha, phi, c.get("coeffs", {})) / f,
+                      one=r.one * 1.0)
     raise NotImplementedError(k)
+
+
+# ---------------------------------------------------------------- aberrations
+_KRIV = ("C10", "C12", "phi12", "C21", "phi21", "C23", "phi23", "C30", "C32", "phi32", "C34",
+         "phi34", "C41", "phi41", "C43", "phi43", "C45", "phi45", "C50", "C52", "phi52", "C54",
+         "phi54", "C56", "phi56")
+
+
+def _kc(p: dict):
+    return {n: float(p.get(n, 0.0)) for n in _KRIV}
+
+
+def _brackets(phi, p):
+    """aberrations.py:42-48."""
+    c = lambda m, ph0: np.cos(m * (phi - ph0))  # noqa: E731
+    B2 = p["C10"] + p["C12"] * c(2, p["phi12"])
+    B3 = p["C21"] * c(1, p["phi21"]) + p["C23"] * c(3, p["phi23"])
+    B4 = p["C30"] + p["C32"] * c(2, p["phi32"]) + p["C34"] * c(4, p["phi34"])
+    B5 = p["C41"] * c(1, p["phi41"]) + p["C43"] * c(3, p["phi43"]) + p["C45"] * c(5, p["phi45"])
+    B6 = p["C50"] + p["C52"] * c(2, p["phi52"]) + p["C54"] * c(4, p["phi54"]) + p["C56"] * c(6, p["phi56"])
+    return B2, B3, B4, B5, B6
+
+
+def w_krivanek(alpha, phi, coeffs):
+    """aberrations.py:51-61."""
+    p = _kc(coeffs)
+    B2, B3, B4, B5, B6 = _brackets(phi, p)
+    a = alpha
+    a2 = a * a
+    a3 = a2 * a
+    a4 = a2 * a2
+    a6 = a3 * a3
+    return 0.5 * a2 * B2 + (a3 / 3.0) * B3 + 0.25 * a4 * B4 + 0.2 * a4 * a * B5 + (a6 / 6.0) * B6
+
+
+def grad_w_krivanek(ax, ay, coeffs):
+    """aberrations.py:64-108 (polar chain rule, alpha = 0 guarded)."""
+    p = _kc(coeffs)
+    a = np.hypot(ax, ay)
+    phi = np.arctan2(ay, ax)
+    B2, B3, B4, B5, B6 = _brackets(phi, p)
+    s = lambda m, ph0: np.sin(m * (phi - ph0))  # noqa: E731
+    a2 = a * a
+    a3 = a2 * a
+    a4 = a2 * a2
+    a5 = a4 * a
+    a6 = a3 * a3
+    dwda = a * B2 + a2 * B3 + a3 * B4 + a4 * B5 + a5 * B6
+    dwdphi = (0.5 * a2) * (-2.0 * p["C12"] * s(2, p["phi12"]))
+    dwdphi += (a3 / 3.0) * (-1.0 * p["C21"] * s(1, p["phi21"]) - 3.0 * p["C23"] * s(3, p["phi23"]))
+    dwdphi += (0.25 * a4) * (-2.0 * p["C32"] * s(2, p["phi32"]) - 4.0 * p["C34"] * s(4, p["phi34"]))
+    dwdphi += (0.2 * a4 * a) * (-1.0 * p["C41"] * s(1, p["phi41"]) - 3.0 * p["C43"] * s(3, p["phi43"])
+                                - 5.0 * p["C45"] * s(5, p["phi45"]))
+    dwdphi += (a6 / 6.0) * (-2.0 * p["C52"] * s(2, p["phi52"]) - 4.0 * p["C54"] * s(4, p["phi54"])
+                            - 6.0 * p["C56"] * s(6, p["phi56"]))
+    a_safe = np.where(a == 0, 1e-30, a)
+    inv_a = 1.0 / a_safe
+    inv_a2 = inv_a * inv_a
+    return (dwda * (ax * inv_a) + dwdphi * (-ay * inv_a2),
+            dwda * (ay * inv_a) + dwdphi * (ax * inv_a2))
+
+
+def aberrated_lens_matrix(c: dict, x, y, dx, dy):
+    """5x5 Jacobian of the aberrated lens at one ray state: the Hessian of W
+    at the ideal slopes by central differences of grad_w_krivanek (step 1e-6
+    of the slope scale); no _one column (the aberration does not scale with
+    _one)."""
+    f = c["focal_length"]
+    ux, uy = -x / f + dx, -y / f + dy
+    h = 1e-6 * max(abs(ux), abs(uy), 1e-3)
+    gxp, gyp = grad_w_krivanek(ux + h, uy, c.get("coeffs", {}))
+    gxm, gym = grad_w_krivanek(ux - h, uy, c.get("coeffs", {}))
+    hxx, hyx = (gxp - gxm) / (2 * h), (gyp - gym) / (2 * h)
+    gxp, gyp = grad_w_krivanek(ux, uy + h, c.get("coeffs", {}))
+    gxm, gym = grad_w_krivanek(ux, uy - h, c.get("coeffs", {}))
+    hxy, hyy = (gxp - gxm) / (2 * h), (gyp - gym) / (2 * h)
+    hs = 0.5 * (hxy + hyx)
+    k = 1.0 / f
+    m = np.eye(5)
+    m[2, 0], m[2, 1], m[2, 2], m[2, 3] = -k + hxx * k * k, hs * k * k, 1 - hxx * k, -hs * k
+    m[3, 0], m[3, 1], m[3, 2], m[3, 3] = hs * k * k, -k + hyy * k * k, -hs * k, 1 - hyy * k
+    return m
 
 
 def run_iter(r: ORay, model):
@@ -214,7 +312,11 @@ def solve_model(r: ORay, model):
         d = comp_z(c) - r.z
         mats.append(free_matrix(float(np.asarray(d).ravel()[0])))
         r = propagate(r, d)
-        mats.append(component_matrix(c, float(np.asarray(r.x).ravel()[0])))
+        if c["kind"] == "aberrated_lens":
+            v = [float(np.asarray(t).ravel()[0]) for t in (r.x, r.y, r.dx, r.dy)]
+            mats.append(aberrated_lens_matrix(c, *v))
+        else:
+            mats.append(component_matrix(c, float(np.asarray(r.x).ravel()[0])))
         r = apply_component(c, r)
     return np.array(mats)
 

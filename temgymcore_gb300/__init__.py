@@ -61,7 +61,9 @@ from .ray import Ray, GaussianRay  # noqa: E402,F401
 from .components import (  # noqa: E402,F401
     Component, Plane, Lens, ScanGrid, Scanner, Descanner, DescanError, Detector, ThickLens,
     Deflector, Rotator, Biprism, Aperture, Source, PointSource, ParallelBeam, Grid,
+    AberratedLensKrivanek,
 )
+from .aberrations import KrivanekCoeffs, W_krivanek, grad_W_krivanek  # noqa: E402,F401
 from .propagator import FreeSpaceParaxial, FreeSpaceDirCosine, Propagator, BasePropagator  # noqa: E402,F401
 from .run import (  # noqa: E402,F401
     run_to_end, run_iter, solve_model, abcd_matrix, trace_to_image, pack_model, TracePlan,

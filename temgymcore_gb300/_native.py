@@ -22,7 +22,7 @@ STATUS = {
 }
 
 # enum tg_kind
-PLANE, LENS, SCANNER, DESCANNER, DEFLECTOR, BIPRISM, ROTATOR, THICKLENS, APERTURE = range(9)
+PLANE, LENS, SCANNER, DESCANNER, DEFLECTOR, BIPRISM, ROTATOR, THICKLENS, APERTURE, ABERLENS = range(10)
 FLAG_PER_PROBE = 0x1
 MAX_COMPONENTS = 60
 
@@ -31,7 +31,7 @@ EW_NONFINITE, EW_TABLE, EW_TIMEOUT, EW_MMA = 0x1, 0x2, 0x4, 0x8
 
 class TgComponent(C.Structure):
     _fields_ = [("kind", C.c_int32), ("flags", C.c_int32), ("z", C.c_double),
-                ("p", C.c_double * 24)]
+                ("p", C.c_double * 32)]
 
 
 class TgModel(C.Structure):

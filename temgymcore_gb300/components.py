@@ -226,6 +226,24 @@ class Lens(Component):
 
 
 @dataclass(frozen=True)
+class AberratedLensKrivanek(Lens):
+    """Thin lens with Krivanek aberrations (components.py:177-215): ideal
+    thin-lens slopes u, then slopes u - grad W(u)/f and pathlength
+    - (x^2 + y^2)/(2f) + W(u)/f.  ``coeffs``: KrivanekCoeffs (or a dict of
+    its fields).  Runs in the forward chain kernels (run_to_end, 4D-STEM
+    scans) and the beamlet-field preparation; the adjoint and batched paths
+    reject it."""
+    coeffs: Any = None
+    _kind = N.ABERLENS
+    _pfields = ("focal_length",)
+
+    def _params(self) -> list:
+        from .aberrations import KrivanekCoeffs, as_coeffs
+        c = KrivanekCoeffs() if self.coeffs is None else as_coeffs(self.coeffs)
+        return [_f(self.focal_length)] + c.as_list()
+
+
+@dataclass(frozen=True)
 class ScanGrid(Component, Grid):
     """Scan grid geometry at z (components.py:218-249); a no-op on rays."""
     z: Any

@@ -30,7 +30,8 @@ TG_DEFINE_ERROR_WORD(field)
 
 namespace tg {
 
-enum DKind : int32_t { D_NOP = 0, D_FREE = 1, D_LENS = 2, D_SHIFT = 3, D_BIPRISM = 4, D_ROTATE = 5 };
+enum DKind : int32_t { D_NOP = 0, D_FREE = 1, D_LENS = 2, D_SHIFT = 3, D_BIPRISM = 4, D_ROTATE = 5,
+                       D_ABER = 6 };
 
 struct DStep {
   int32_t kind;
@@ -40,8 +41,9 @@ struct DStep {
 
 struct DModel {
   int32_t n;
-  int32_t pad;
+  int32_t n_aber;
   DStep s[kMaxSteps];
+  double aber[kMaxAber][kAberW];  // D_ABER (pad = slot): W monomials, float64
 };
 
 struct cd {
@@ -173,6 +175,22 @@ k_field_prep(const __grid_constant__ DModel M, const __grid_constant__ PrepArgs 
         double sg = x > 0.0 ? 1.0 : (x < 0.0 ? -1.0 : 0.0);
         m[2][4] += st.a[0] * sg;
         dx += st.a[0] * sg;
+      } break;
+      case D_ABER: {  // Jacobian (I - H/f) [-I/f, I] at the ideal slopes; no offset column
+        const double k1 = 1.0 / st.a[0];
+        const double ux = dx - x * k1, uy = dy - y * k1;
+        double W, Wx, Wy, Hxx, Hxy, Hyy;
+        aber_eval_f64(M.aber[st.pad], ux, uy, &W, &Wx, &Wy, &Hxx, &Hxy, &Hyy);
+        const double a20 = -k1 + Hxx * k1 * k1, a21 = Hxy * k1 * k1, a22 = 1.0 - Hxx * k1, a23 = -Hxy * k1;
+        const double a30 = Hxy * k1 * k1, a31 = -k1 + Hyy * k1 * k1, a32 = -Hxy * k1, a33 = 1.0 - Hyy * k1;
+#pragma unroll
+        for (int j = 0; j < 5; ++j) {
+          const double r0 = m[0][j], r1 = m[1][j], r2 = m[2][j], r3 = m[3][j];
+          m[2][j] = a20 * r0 + a21 * r1 + a22 * r2 + a23 * r3;
+          m[3][j] = a30 * r0 + a31 * r1 + a32 * r2 + a33 * r3;
+        }
+        dx = ux - Wx * k1;
+        dy = uy - Wy * k1;
       } break;
       case D_ROTATE: {
         double c = st.a[0], sn = st.a[1];
@@ -639,6 +657,14 @@ static int build_dmodel(const tg_model* model, double z_in, DModel* dm) {
         s.a[0] = std::cos(a);
         s.a[1] = std::sin(a);
       } break;
+      case TG_ABERLENS:
+        if (!(p[0] != 0.0)) return TG_ERR_INVALID;
+        if (dm->n_aber >= kMaxAber) return TG_ERR_TOO_LARGE;
+        s.kind = D_ABER;
+        s.pad = dm->n_aber;
+        s.a[0] = p[0];
+        aber_monomials(p + 1, dm->aber[dm->n_aber++]);
+        break;
       default:
         return TG_ERR_UNSUPPORTED;
     }

@@ -143,6 +143,22 @@ int compile_program(const tg_model* model, bool per_ray_z, double z_scalar,
         co.c[2] = (float)p[2];
         prog->has_aperture = 1;
         break;
+      case TG_ABERLENS: {
+        double f = p[0];
+        if (!(f != 0.0)) return TG_ERR_INVALID;
+        if (prog->n_aber >= kMaxAber) return TG_ERR_TOO_LARGE;
+        co.kind = OP_ABER;
+        co.aux = prog->n_aber;
+        co.c[0] = (float)(1.0 / f);
+        co.c[1] = (float)(1.0 / (2.0 * f));
+        double w[kAberW], gx[kAberG], gy[kAberG];
+        aber_monomials(p + 1, w);
+        aber_gradient(w, gx, gy);
+        float* a = prog->aber[prog->n_aber++];
+        for (int k = 0; k < kAberW; ++k) a[k] = (float)w[k];
+        for (int k = 0; k < kAberG; ++k) a[kAberW + k] = (float)gx[k];
+        for (int k = 0; k < kAberG; ++k) a[kAberW + kAberG + k] = (float)gy[k];
+      } break;
       default:
         return TG_ERR_UNSUPPORTED;
     }
@@ -233,6 +249,30 @@ extern "C" int tg_abcd_compose(const tg_model* model, const double central[5],
         double s = x > 0 ? 1.0 : (x < 0 ? -1.0 : 0.0);
         cm[14] = p[0] * s;
         dx += p[0] * s;
+      } break;
+      case TG_ABERLENS: {
+        // Jacobian of the aberrated lens at the ray: ideal slopes u = d - r/f,
+        // d' = u - grad W(u)/f, so d(d')/d(r, d) = (I - H/f) [-I/f, I]
+        // with H the Hessian of W at u; no offset column (the aberration
+        // does not scale with the ray's _one).
+        const double f = p[0];
+        if (!(f != 0.0)) return TG_ERR_INVALID;
+        const double k1 = 1.0 / f;
+        double w[kAberW];
+        aber_monomials(p + 1, w);
+        const double ux = dx - x * k1, uy = dy - y * k1;
+        double W, Wx, Wy, Hxx, Hxy, Hyy;
+        aber_eval_f64(w, ux, uy, &W, &Wx, &Wy, &Hxx, &Hxy, &Hyy);
+        cm[10] = -k1 + Hxx * k1 * k1;  // [2,0]
+        cm[11] = Hxy * k1 * k1;        // [2,1]
+        cm[12] = 1.0 - Hxx * k1;       // [2,2]
+        cm[13] = -Hxy * k1;            // [2,3]
+        cm[15] = Hxy * k1 * k1;        // [3,0]
+        cm[16] = -k1 + Hyy * k1 * k1;  // [3,1]
+        cm[17] = -Hxy * k1;            // [3,2]
+        cm[18] = 1.0 - Hyy * k1;       // [3,3]
+        dx = ux - Wx * k1;
+        dy = uy - Wy * k1;
       } break;
       case TG_ROTATOR: {
         double a = p[0] * (M_PI / 180.0);

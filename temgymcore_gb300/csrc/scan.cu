@@ -71,7 +71,7 @@ __device__ __forceinline__ void trace_one(const Program& P, const float4* pshift
   uint64_t sb = 0;
   alive = true;
   for (int s = 0; s < P.n_steps; ++s)
-    op_forward(P.op[s], pshift, r, P.zc_first, z, dvar, sb, alive);
+    op_forward(P.op[s], pshift, r, P.zc_first, z, dvar, sb, alive, &P.aber[0][0]);
 }
 
 __device__ __forceinline__ int block_min(int v, int* red) {

@@ -19,6 +19,7 @@
 #include <stdint.h>
 
 #include "../../include/temgym_gb300.h"
+#include "aberration.cuh"
 
 namespace tg {
 
@@ -32,7 +33,8 @@ enum OpKind : int32_t {
   OP_BIPRISM = 6,    // c0 = def_x;   dx += def_x*sign(x); pl += dx*x + dy*y
   OP_ROTATE = 7,     // c0 = cos, c1 = sin
   OP_APERTURE = 8,   // c0 = r^2, c1 = cx, c2 = cy
-  OP_PROBE_SHIFT = 9 // per-probe shift: Delta = K (4x2) sp + k0 (float64 in pcoef)
+  OP_PROBE_SHIFT = 9, // per-probe shift: Delta = K (4x2) sp + k0 (float64 in pcoef)
+  OP_ABER = 10       // aberrated lens: c0 = 1/f, c1 = 1/(2f); aux = Program::aber slot
 };
 
 struct Op {
@@ -49,6 +51,8 @@ struct Program {
   int32_t n_biprism;
   int32_t has_aperture;
   int32_t n_probe_ops;
+  int32_t n_aber;     // aberrated lenses (OP_ABER); not supported by the adjoint paths
+  int32_t pad_;
   double zc_first;    // z of the first component (OP_FREE_VARZ)
   double pl_const;    // float64 sum of the uniform distances
   double z_out;       // uniform output z
@@ -56,6 +60,7 @@ struct Program {
   Op op[kMaxSteps];
   double dstep[kMaxSteps];  // float64 distance of each propagator step (0 elsewhere)
   int32_t comp_kind[kMaxSteps];  // tg_kind of the component behind each step (-1 = propagator)
+  float aber[kMaxAber][kAberFloats];  // per aberrated lens: W, dW/dx, dW/dy monomials
 };
 
 // Host-side compilation (model.cpp).  per_ray_z: input z is a per-ray array.
@@ -153,14 +158,29 @@ struct RayS {
   float x, y, dx, dy, plv;  // plv: per-ray (varying) pathlength part
 };
 
+// Aberrated lens (components.py:193-215): thin lens to the ideal slopes u,
+// then the slope kick -grad W(u) / f and the pathlength + W(u) / f, with W the
+// Krivanek polynomial of one Program::aber slot.
+__device__ __forceinline__ void aber_forward(const float* a, float k1, float h, RayS& r) {
+  const float x = r.x, y = r.y;
+  const float ux = fmaf(-x, k1, r.dx), uy = fmaf(-y, k1, r.dy);
+  const float W = tri_eval<6>(a, ux, uy);
+  const float Wx = tri_eval<5>(a + kAberW, ux, uy);
+  const float Wy = tri_eval<5>(a + kAberW + kAberG, ux, uy);
+  r.plv = fmaf(W, k1, r.plv - (x * x + y * y) * h);
+  r.dx = fmaf(-Wx, k1, ux);
+  r.dy = fmaf(-Wy, k1, uy);
+}
+
 // Apply one forward step.  zi is the ray's input z (OP_FREE_VARZ only);
-// pshift holds the current probe's shifts (OP_PROBE_SHIFT only);
+// pshift holds the current probe's shifts (OP_PROBE_SHIFT only); aber the
+// Program's aberration polynomials (OP_ABER only, may be NULL otherwise);
 // dvar receives that per-ray float64 distance.  sbits records biprism signs
 // (2 bits per biprism: 1 = +, 2 = -) and alive is cleared by apertures.
 __device__ __forceinline__ void op_forward(const Op& op, const float4* pshift,
                                            RayS& r, double zc, double zi,
                                            double& dvar, uint64_t& sbits,
-                                           bool& alive) {
+                                           bool& alive, const float* aber = nullptr) {
   switch (op.kind) {
     case OP_FREE: {
       float d = op.c[0];
@@ -216,6 +236,9 @@ __device__ __forceinline__ void op_forward(const Op& op, const float4* pshift,
       float ex = r.x - op.c[1], ey = r.y - op.c[2];
       if (!(ex * ex + ey * ey < op.c[0])) alive = false;
     } break;
+    case OP_ABER:
+      if (aber) aber_forward(aber + op.aux * kAberFloats, op.c[0], op.c[1], r);
+      break;
     default:
       break;
   }

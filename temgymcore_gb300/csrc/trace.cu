@@ -89,7 +89,7 @@ k_trace_fwd(const __grid_constant__ Program P, const __grid_constant__ FwdArgs A
       const Op op = P.op[s];
 #pragma unroll
       for (int k = 0; k < R; ++k)
-        op_forward(op, nullptr, r[k], P.zc_first, zi[k], dvar[k], sb[k], alive[k]);
+        op_forward(op, nullptr, r[k], P.zc_first, zi[k], dvar[k], sb[k], alive[k], &P.aber[0][0]);
     }
 #pragma unroll
     for (int k = 0; k < R; ++k) {
@@ -444,6 +444,7 @@ extern "C" int tg_trace_vjp(const tg_model* model, const tg_rays* in, const tg_r
   Program P;
   int st = compile_program(model, in->z != nullptr, in->z_scalar, &P);
   if (st != TG_OK) return st;
+  if (P.n_aber > 0) return TG_ERR_UNSUPPORTED;  // nonlinear lens: forward paths only
   if (P.n_probe_ops) return TG_ERR_UNSUPPORTED;
   if (in->n == 0) return TG_OK;
   const int grid = vjp_grid(in->n);

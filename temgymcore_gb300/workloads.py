@@ -15,7 +15,7 @@ from . import components as K
 _KIND = {"lens": K.Lens, "plane": K.Plane, "detector": K.Detector, "scangrid": K.ScanGrid,
          "scanner": K.Scanner, "descanner": K.Descanner, "deflector": K.Deflector,
          "biprism": K.Biprism, "rotator": K.Rotator, "thicklens": K.ThickLens,
-         "aperture": K.Aperture, "source": K.PointSource}
+         "aperture": K.Aperture, "source": K.PointSource, "aberrated_lens": K.AberratedLensKrivanek}
 
 
 def build_model(spec):
