@@ -535,6 +535,31 @@ def secondary_batched(torch, dev, hbm):
             "plain_per_model_ms": ms_plain, "speedup_vs_plain_per_model": ms_plain / ms}
 
 
+def secondary_aberrated_scan(torch, dev, hbm):
+    """The headline 4D-STEM scan with an AberratedLensKrivanek (f = 0.05 m at
+    z = 0.03 m; C10 = 0.02, C12 = 0.05 at 30 deg, C23 = 5 at 10 deg,
+    C30 = 300 m) between the sample and the detector: the nonlinear lens
+    runs inside the same fused scan kernel."""
+    import temgymcore_gb300 as t
+    from temgymcore_gb300.workloads import stem_model
+    w = _workload()
+    model = stem_model(w)
+    kc = t.KrivanekCoeffs(C10=0.02, C12=0.05, phi12=np.deg2rad(30.0), C23=5.0, phi23=np.deg2rad(10.0),
+                          C30=300.0)
+    model.insert(4, t.AberratedLensKrivanek(z=0.03, focal_length=0.05, coeffs=kc))
+    ray = t.Ray(x=torch.tensor(w["x"], device=dev), y=torch.tensor(w["y"], device=dev),
+                dx=torch.tensor(w["dx"], device=dev), dy=torch.tensor(w["dy"], device=dev),
+                z=0.0, pathlength=0.0)
+    n_probes = SCAN[0] * SCAN[1]
+    out = torch.empty((n_probes, 256, 256), dtype=torch.int32, device=dev)
+    ms = _time(torch, lambda: t.scan_images(ray, model, out=out), 200)
+    alg = n_probes * 256 * 256 * 4
+    return {"workload": "4D-STEM 64x64 x 1024 rays with an aberrated lens (6 components)",
+            "ms": ms, "ray_component_steps_per_s": n_probes * RAYS * (N_COMPONENTS + 1) / (ms * 1e-3),
+            "achieved_gbs": alg / (ms * 1e-3) / 1e9, "frac_of_hbm": alg / (ms * 1e-3) / 1e9 / hbm,
+            "hits": int(out.sum().item())}
+
+
 def run_gpu(args, world, rank, local):
     import torch
 
@@ -624,6 +649,10 @@ def run_gpu(args, world, rank, local):
             secondary["input_field"] = secondary_input_field(torch, dev, bf16)
         except Exception as e:
             secondary["input_field"] = {"error": repr(e)}
+        try:
+            secondary["aberrated_scan"] = secondary_aberrated_scan(torch, dev, hbm)
+        except Exception as e:
+            secondary["aberrated_scan"] = {"error": repr(e)}
         try:
             secondary["adjoint_fit"] = secondary_fit(torch, dev)
         except Exception as e:

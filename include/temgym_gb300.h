@@ -79,8 +79,15 @@ typedef struct tg_component {
   double p[32];  /* kind-specific parameters, see enum tg_kind */
 } tg_component;
 
+/* free-space propagator between components (propagator.py:43-116) */
+#define TG_PROP_PARAXIAL 0 /* FreeSpaceParaxial: x += dx d, pathlength += d          */
+#define TG_PROP_DIRCOS 1   /* FreeSpaceDirCosine: N = sqrt(1 + dx^2 + dy^2),         */
+                           /* x += dx d / N^2, pathlength += d N.  Forward trace,    */
+                           /* adjoint, scan and ABCD; batched / field: unsupported   */
+
 typedef struct tg_model {
   int32_t n_components;            /* <= TG_MAX_COMPONENTS */
+  int32_t propagator;              /* TG_PROP_* (0 = paraxial) */
   const tg_component *components;  /* host pointer */
 } tg_model;
 
@@ -198,6 +205,33 @@ typedef struct tg_scan {
  */
 int tg_scan_hist(const tg_model *model, const tg_rays *bundle, const tg_scan *scan,
                  const tg_grid *grid, int32_t *hist, float *probe_xy, void *stream);
+
+/* ---- transfer-matrix stacks (transfer.py:6-183) ----------------------- */
+/*
+ * tg_transfer_cumulative - host: the cumulative products of m row-major 5x5
+ * matrices exactly as transfer.py:150-183 accumulate_matrices_cumulative
+ * builds them: cumulative[0] = M[m-1], cumulative[k] = M[m-1-k] @
+ * cumulative[k-1] (so cumulative[k] = M[m-1-k] @ ... @ M[m-1]).
+ */
+int tg_transfer_cumulative(int32_t m, const double *matrices, double *cumulative);
+
+/*
+ * tg_transfer_rays - transfer.py:6-53: every ray (device float64 [n][5],
+ * rows x, y, dx, dy, 1) through each cumulative product of the m host
+ * matrices (m <= 120): out (device float64 [n][m][5]).  m == 0 is invalid
+ * (the reference raises IndexError).
+ */
+int tg_transfer_rays(int64_t n, const double *rays, int32_t m, const double *matrices,
+                     double *out, void *stream);
+
+/*
+ * tg_transfer_rays_pt_src - transfer.py:56-112: rays from the point (x0, y0)
+ * with slopes (slopes_x[k], slopes_y[k]) (device float64) through one host
+ * 5x5 matrix: out (device float64 [4][n], rows x, y, dx, dy).
+ */
+int tg_transfer_rays_pt_src(double x0, double y0, int64_t n, const double *slopes_x,
+                            const double *slopes_y, const double *matrix, double *out,
+                            void *stream);
 
 /* ---- many models in one persistent launch ------------------------------ */
 typedef struct tg_batch_info {

@@ -3,6 +3,7 @@
 Follows, operation by operation:
   - ``Ray``                          ray.py:8-166
   - ``FreeSpaceParaxial.propagate``  propagator.py:51-72
+  - ``FreeSpaceDirCosine.propagate`` propagator.py:79-116
   - ``run_iter`` / ``run_to_end``    run.py:47-116 (a propagator is inserted
     before EVERY component, with per-ray distance ``component.z - ray.z``)
   - components                       components.py:137-559
@@ -57,6 +58,25 @@ def propagate(r: ORay, d) -> ORay:
     """propagator.py:64-72: x += dx*d, y += dy*d, z += d, pathlength += d."""
     return r.copy(x=r.x + r.dx * d, y=r.y + r.dy * d, z=r.z + d,
                   pathlength=r.pathlength + d)
+
+
+def propagate_dircos(r: ORay, d) -> ORay:
+    """propagator.py:100-110 (FreeSpaceDirCosine): N = sqrt(1 + dx^2 + dy^2),
+    L = dx/N, M = dy/N; x += L/N*d, y += M/N*d, z = z*_one + d,
+    pathlength += d*N."""
+    n = np.sqrt(1 + r.dx ** 2 + r.dy ** 2)
+    L = r.dx / n
+    M = r.dy / n
+    return r.copy(x=r.x + L / n * d, y=r.y + M / n * d, z=r.z * r.one + d,
+                  pathlength=r.pathlength + d * n)
+
+
+def _prop(propagator):
+    if propagator in (None, "paraxial"):
+        return propagate
+    if propagator == "dircos":
+        return propagate_dircos
+    raise ValueError(propagator)
 
 
 def comp_z(c: dict):
@@ -234,19 +254,20 @@ def aberrated_lens_matrix(c: dict, x, y, dx, dy):
     return m
 
 
-def run_iter(r: ORay, model):
+def run_iter(r: ORay, model, propagator="paraxial"):
     """run.py:75-82: yields (step, ray) for the propagator then the component."""
+    prop = _prop(propagator)
     for c in model:
         d = comp_z(c) - r.z
-        r = propagate(r, d)
+        r = prop(r, d)
         yield ("propagator", d), r
         r = apply_component(c, r)
         yield c, r
 
 
-def run_to_end(r: ORay, model) -> ORay:
+def run_to_end(r: ORay, model, propagator="paraxial") -> ORay:
     """run.py:85-116."""
-    for _, r in run_iter(r, model):
+    for _, r in run_iter(r, model, propagator):
         pass
     return r
 
@@ -305,13 +326,30 @@ def component_matrix(c: dict, x_at_component=0.0):
     raise NotImplementedError(k)
 
 
-def solve_model(r: ORay, model):
+def dircos_matrix(r: ORay, d):
+    """5x5 Jacobian of propagate_dircos at a scalar ray, by complex step
+    (exact to rounding) on x, y, dx, dy."""
+    m = _eye5()
+    h = 1e-30
+    base = [complex(float(np.asarray(v).ravel()[0])) for v in (r.x, r.y, r.dx, r.dy)]
+    for j in range(4):
+        v = list(base)
+        v[j] += 1j * h
+        o = propagate_dircos(ORay(*[np.array([a]) for a in v], z=0.0, pathlength=0.0), d)
+        for i, f in enumerate((o.x, o.y, o.dx, o.dy)):
+            m[i, j] = np.imag(f[0]) / h
+    return m
+
+
+def solve_model(r: ORay, model, propagator="paraxial"):
     """run.py:150-179: per-step 5x5 matrices (propagator, component, ...)."""
+    prop = _prop(propagator)
     mats = []
     for c in model:
         d = comp_z(c) - r.z
-        mats.append(free_matrix(float(np.asarray(d).ravel()[0])))
-        r = propagate(r, d)
+        dd = float(np.asarray(d).ravel()[0])
+        mats.append(free_matrix(dd) if prop is propagate else dircos_matrix(r, dd))
+        r = prop(r, d)
         if c["kind"] == "aberrated_lens":
             v = [float(np.asarray(t).ravel()[0]) for t in (r.x, r.y, r.dx, r.dy)]
             mats.append(aberrated_lens_matrix(c, *v))
@@ -329,6 +367,6 @@ def accumulate_matrices(mats):
     return total
 
 
-def model_abcd(r: ORay, model):
+def model_abcd(r: ORay, model, propagator="paraxial"):
     """Whole-model ABCD about a scalar central ray (jacobian of run_to_end)."""
-    return accumulate_matrices(list(solve_model(r, model)))
+    return accumulate_matrices(list(solve_model(r, model, propagator)))

@@ -64,6 +64,8 @@ from .components import (  # noqa: E402,F401
     AberratedLensKrivanek,
 )
 from .aberrations import KrivanekCoeffs, W_krivanek, grad_W_krivanek  # noqa: E402,F401
+from .transfer import (  # noqa: E402,F401
+    transfer_rays, transfer_rays_pt_src, accumulate_matrices, accumulate_matrices_cumulative)
 from .propagator import FreeSpaceParaxial, FreeSpaceDirCosine, Propagator, BasePropagator  # noqa: E402,F401
 from .run import (  # noqa: E402,F401
     run_to_end, run_iter, solve_model, abcd_matrix, trace_to_image, pack_model, TracePlan,

@@ -24,6 +24,7 @@ STATUS = {
 # enum tg_kind
 PLANE, LENS, SCANNER, DESCANNER, DEFLECTOR, BIPRISM, ROTATOR, THICKLENS, APERTURE, ABERLENS = range(10)
 FLAG_PER_PROBE = 0x1
+PROP_PARAXIAL, PROP_DIRCOS = 0, 1
 MAX_COMPONENTS = 60
 
 EW_NONFINITE, EW_TABLE, EW_TIMEOUT, EW_MMA = 0x1, 0x2, 0x4, 0x8
@@ -35,7 +36,8 @@ class TgComponent(C.Structure):
 
 
 class TgModel(C.Structure):
-    _fields_ = [("n_components", C.c_int32), ("components", C.POINTER(TgComponent))]
+    _fields_ = [("n_components", C.c_int32), ("propagator", C.c_int32),
+                ("components", C.POINTER(TgComponent))]
 
 
 class TgRays(C.Structure):

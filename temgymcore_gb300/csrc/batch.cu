@@ -512,7 +512,7 @@ extern "C" int tg_batch_plan(int32_t n_models, const tg_model* models, const int
     Program P;
     int st = compile_program(&models[m], false, z_in ? z_in[m] : 0.0, &P);
     if (st != TG_OK) return st;
-    if (P.n_probe_ops || P.n_aber) return TG_ERR_UNSUPPORTED;
+    if (P.n_probe_ops || P.n_aber || P.dircos) return TG_ERR_UNSUPPORTED;
     BModel& M = bm[m];
     std::memset(&M, 0, sizeof(M));
     M.op_off = (int32_t)ops.size();

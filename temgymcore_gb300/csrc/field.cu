@@ -601,6 +601,7 @@ static int build_dmodel(const tg_model* model, double z_in, DModel* dm) {
   if (!model || model->n_components < 0 || model->n_components > TG_MAX_COMPONENTS)
     return TG_ERR_INVALID;
   if (model->n_components > 0 && !model->components) return TG_ERR_INVALID;
+  if (model->propagator != TG_PROP_PARAXIAL) return TG_ERR_UNSUPPORTED;  // make_gaussian_image is paraxial
   std::memset(dm, 0, sizeof(DModel));
   // reuse the float32 program compiler for distances/z bookkeeping, but keep
   // every coefficient in float64 here.

@@ -61,7 +61,10 @@ int compile_program(const tg_model* model, bool per_ray_z, double z_scalar,
       (model->n_components > 0 && !model->components))
     return TG_ERR_INVALID;
   if (model->n_components > TG_MAX_COMPONENTS) return TG_ERR_TOO_LARGE;
+  if (model->propagator != TG_PROP_PARAXIAL && model->propagator != TG_PROP_DIRCOS)
+    return TG_ERR_INVALID;
   std::memset(prog, 0, sizeof(Program));
+  prog->dircos = model->propagator == TG_PROP_DIRCOS;
   const int nc = model->n_components;
   prog->n_steps = 2 * nc;
   double z = z_scalar;
@@ -72,6 +75,7 @@ int compile_program(const tg_model* model, bool per_ray_z, double z_scalar,
     Op& co = prog->op[2 * i + 1];
     prog->comp_kind[2 * i] = -1;
     prog->comp_kind[2 * i + 1] = c.kind;
+    fo.aux = prog->dircos;  // 1: direction-cosine propagation
     if (i == 0 && per_ray_z) {
       fo.kind = OP_FREE_VARZ;
       prog->zc_first = c.z;
@@ -192,6 +196,8 @@ static void eye5(double m[25]) {
 extern "C" int tg_abcd_compose(const tg_model* model, const double central[5],
                                double out[25], double* steps) {
   if (!model || !central || !out) return TG_ERR_INVALID;
+  if (model->propagator != TG_PROP_PARAXIAL && model->propagator != TG_PROP_DIRCOS)
+    return TG_ERR_INVALID;
   if (model->n_components < 0 || model->n_components > TG_MAX_COMPONENTS)
     return TG_ERR_INVALID;
   if (model->n_components > 0 && !model->components) return TG_ERR_INVALID;
@@ -205,12 +211,25 @@ extern "C" int tg_abcd_compose(const tg_model* model, const double central[5],
     double d = c.z - z;
     double fm[25];
     eye5(fm);
-    fm[2] = d;       // [0,2]
-    fm[5 + 3] = d;   // [1,3]
-    mat5_mul(fm, total, total);
-    if (steps) std::memcpy(steps + 50 * i, fm, sizeof(fm));
-    x += dx * d;
-    y += dy * d;
+    if (model->propagator == TG_PROP_DIRCOS) {
+      // x' = x + d dx / n2, n2 = 1 + dx^2 + dy^2 (propagator.py:100-110)
+      const double n2 = 1.0 + dx * dx + dy * dy, inv = 1.0 / n2, inv2 = inv * inv;
+      fm[2] = d * (inv - 2.0 * dx * dx * inv2);  // [0,2]
+      fm[3] = -2.0 * d * dx * dy * inv2;         // [0,3]
+      fm[5 + 2] = -2.0 * d * dx * dy * inv2;     // [1,2]
+      fm[5 + 3] = d * (inv - 2.0 * dy * dy * inv2);  // [1,3]
+      mat5_mul(fm, total, total);
+      if (steps) std::memcpy(steps + 50 * i, fm, sizeof(fm));
+      x += dx * inv * d;
+      y += dy * inv * d;
+    } else {
+      fm[2] = d;       // [0,2]
+      fm[5 + 3] = d;   // [1,3]
+      mat5_mul(fm, total, total);
+      if (steps) std::memcpy(steps + 50 * i, fm, sizeof(fm));
+      x += dx * d;
+      y += dy * d;
+    }
     z += d;
     double cm[25];
     eye5(cm);

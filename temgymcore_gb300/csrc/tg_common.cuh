@@ -52,7 +52,7 @@ struct Program {
   int32_t has_aperture;
   int32_t n_probe_ops;
   int32_t n_aber;     // aberrated lenses (OP_ABER); not supported by the adjoint paths
-  int32_t pad_;
+  int32_t dircos;     // free-space steps use direction cosines (Op::aux = 1 on them)
   double zc_first;    // z of the first component (OP_FREE_VARZ)
   double pl_const;    // float64 sum of the uniform distances
   double z_out;       // uniform output z
@@ -182,17 +182,27 @@ __device__ __forceinline__ void op_forward(const Op& op, const float4* pshift,
                                            double& dvar, uint64_t& sbits,
                                            bool& alive, const float* aber = nullptr) {
   switch (op.kind) {
-    case OP_FREE: {
-      float d = op.c[0];
-      r.x = fmaf(r.dx, d, r.x);
-      r.y = fmaf(r.dy, d, r.y);
-    } break;
+    case OP_FREE:
     case OP_FREE_VARZ: {
-      double dd = zc - zi;
-      dvar = dd;
-      float d = (float)dd;
-      r.x = fmaf(r.dx, d, r.x);
-      r.y = fmaf(r.dy, d, r.y);
+      float d;
+      if (op.kind == OP_FREE) {
+        d = op.c[0];
+      } else {
+        const double dd = zc - zi;
+        dvar = dd;
+        d = (float)dd;
+      }
+      if (op.aux) {  // direction cosines (propagator.py:100-110): x += d dx / N^2, pl += d N
+        const float s2 = fmaf(r.dx, r.dx, r.dy * r.dy);
+        const float n2 = 1.f + s2;
+        const float t = d / n2;
+        r.x = fmaf(r.dx, t, r.x);
+        r.y = fmaf(r.dy, t, r.y);
+        r.plv = fmaf(d, s2 / (sqrtf(n2) + 1.f), r.plv);  // d (N - 1); the uniform d is float64
+      } else {
+        r.x = fmaf(r.dx, d, r.x);
+        r.y = fmaf(r.dy, d, r.y);
+      }
     } break;
     case OP_LENS: {
       float x = r.x, y = r.y;
@@ -259,13 +269,31 @@ __device__ __forceinline__ void op_reverse(const Op& op, const float4* pshift, R
     case OP_FREE:
     case OP_FREE_VARZ: {
       float d = (op.kind == OP_FREE) ? op.c[0] : (float)dvar;
-      float g = a.lx * r.dx + a.ly * r.dy + a.lpl;
-      c[0] = g;
-      if (op.kind == OP_FREE_VARZ) gz = -g;
-      r.x = fmaf(-r.dx, d, r.x);
-      r.y = fmaf(-r.dy, d, r.y);
-      a.ldx = fmaf(a.lx, d, a.ldx);
-      a.ldy = fmaf(a.ly, d, a.ldy);
+      if (op.aux) {  // direction cosines: slopes unchanged, so the step inverts exactly
+        const float dx = r.dx, dy = r.dy;
+        const float n2 = 1.f + fmaf(dx, dx, dy * dy);  // as in the forward step
+        const float inv = 1.f / n2, nn = sqrtf(n2);
+        const float g = (a.lx * dx + a.ly * dy) * inv + a.lpl * nn;
+        c[0] = g;
+        if (op.kind == OP_FREE_VARZ) gz = -g;
+        const float t = d / n2;
+        r.x = fmaf(-dx, t, r.x);
+        r.y = fmaf(-dy, t, r.y);
+        // d x'/d dx = d (1/n2 - 2 dx^2/n2^2), d x'/d dy = -2 d dx dy / n2^2, d pl'/d dx = d dx / N
+        const float di = d * inv, di2 = 2.f * di * inv;
+        const float jxx = di - di2 * dx * dx, jyy = di - di2 * dy * dy, jxy = -di2 * dx * dy;
+        const float pn = d / nn;
+        a.ldx += a.lx * jxx + a.ly * jxy + a.lpl * pn * dx;
+        a.ldy += a.lx * jxy + a.ly * jyy + a.lpl * pn * dy;
+      } else {
+        float g = a.lx * r.dx + a.ly * r.dy + a.lpl;
+        c[0] = g;
+        if (op.kind == OP_FREE_VARZ) gz = -g;
+        r.x = fmaf(-r.dx, d, r.x);
+        r.y = fmaf(-r.dy, d, r.y);
+        a.ldx = fmaf(a.lx, d, a.ldx);
+        a.ldy = fmaf(a.ly, d, a.ldy);
+      }
     } break;
     case OP_LENS: {
       float k = op.c[0], h = op.c[1];

@@ -1,7 +1,8 @@
 """Propagators (propagator.py:8-116).
 
-Only paraxial free space (propagator.py:43-76) is on the GPU path; it is
-fused into the chain kernel rather than applied as a separate pass.
+Paraxial free space (propagator.py:43-76, the default) and direction-cosine
+free space (propagator.py:79-116) are fused into the chain kernel rather than
+applied as a separate pass.
 """
 from __future__ import annotations
 
@@ -42,8 +43,17 @@ class FreeSpaceParaxial(BasePropagator):
 
 
 class FreeSpaceDirCosine(BasePropagator):
-    """Direction-cosine propagation (propagator.py:79-116) is outside the
-    accelerated paraxial path."""
+    """Direction-cosine propagation (propagator.py:79-116): with
+    N = sqrt(1 + dx^2 + dy^2), x += (dx/N)/N * d, y += (dy/N)/N * d,
+    z += d, pathlength += d * N; slopes unchanged.  On the GPU it replaces
+    the paraxial step inside the fused chain (``run_to_end(...,
+    propagator=FreeSpaceDirCosine())``), forward and adjoint."""
 
     def __call__(self, ray, distance):
-        raise NotImplementedError("FreeSpaceDirCosine is not part of the GPU paraxial path")
+        from .components import Plane
+        from .run import run_to_end
+        return run_to_end(ray, [Plane(z=ray.z + distance)], propagator=self)
+
+    @staticmethod
+    def propagate(ray, distance):
+        return FreeSpaceDirCosine()(ray, distance)

@@ -33,14 +33,26 @@ def _check_model(model) -> list:
     return comps
 
 
-def pack_model(model):
-    """(TgModel, keep-alive array) for a sequence of components."""
+def _prop_code(propagator) -> int:
+    """C-ABI propagator selector (TG_PROP_*) of a propagator object."""
+    from .propagator import FreeSpaceDirCosine
+    if propagator is None or isinstance(propagator, FreeSpaceParaxial):
+        return N.PROP_PARAXIAL
+    if isinstance(propagator, FreeSpaceDirCosine):
+        return N.PROP_DIRCOS
+    raise NotImplementedError(f"{type(propagator).__name__} is not a GPU propagator")
+
+
+def pack_model(model, propagator=None):
+    """(TgModel, keep-alive array) for a sequence of components; ``propagator``
+    selects the free-space model between them (default paraxial)."""
     comps = _check_model(model)
     arr = (N.TgComponent * max(1, len(comps)))()
     for i, c in enumerate(comps):
         c._pack(arr[i])
     m = N.TgModel()
     m.n_components = len(comps)
+    m.propagator = _prop_code(propagator)
     m.components = C.cast(arr, C.POINTER(N.TgComponent))
     return m, arr
 
@@ -85,7 +97,7 @@ def _ray_scalar_input(ray: Ray) -> bool:
                getattr(ray, f).ndim == 0 for f in ("x", "y", "dx", "dy"))
 
 
-def _fwd_launch(model, soa: _Soa, grid=None, want_pix=False, hist=None, want_amp=False):
+def _fwd_launch(model, soa: _Soa, grid=None, want_pix=False, hist=None, want_amp=False, propagator=None):
     dev = soa.x.device
     n = soa.n
     ox = torch.empty(n, dtype=torch.float32, device=dev)
@@ -94,7 +106,7 @@ def _fwd_launch(model, soa: _Soa, grid=None, want_pix=False, hist=None, want_amp
     ody = torch.empty_like(ox)
     opl = torch.empty(n, dtype=torch.float64, device=dev)
     oamp = torch.empty(n, dtype=torch.float32, device=dev) if (want_amp or soa.amp is not None) else None
-    m, keep = pack_model(model)
+    m, keep = pack_model(model, propagator)
     out = _rays_struct(n, ox, oy, odx, ody, None, 0.0, opl, 0.0, oamp)
     zout = C.c_double(0.0)
     py = px = None
@@ -187,7 +199,7 @@ class _TraceFn(torch.autograd.Function):
     @staticmethod
     def forward(ctx, spec, x, y, dx, dy, pl, zin, *params):
         comps, soa = spec["comps"], spec["soa"]
-        ox, oy, odx, ody, opl, zout, _, _, _ = _fwd_launch(comps, soa)
+        ox, oy, odx, ody, opl, zout, _, _, _ = _fwd_launch(comps, soa, propagator=spec["propagator"])
         spec["zout"] = zout
         ctx.spec = spec
         return ox, oy, odx, ody, opl
@@ -207,7 +219,7 @@ class _TraceFn(torch.autograd.Function):
         ix, iy, idx, idy = z32(), z32(), z32(), z32()
         ipl = torch.empty(n, dtype=torch.float64, device=dev)
         need_raw = bool(plist) or spec["z_grad"]
-        m, keep = pack_model(comps)
+        m, keep = pack_model(comps, spec["propagator"])
         raw = torch.zeros((2 * len(comps), 4), dtype=torch.float64, device=dev) if need_raw else None
         ws = None
         if need_raw:
@@ -255,9 +267,9 @@ def run_to_end(ray: Ray, components: Sequence[Component],
                propagator=FreeSpaceParaxial()) -> Ray:
     """Propagate rays through every component (run.py:85-116), one fused
     GPU launch.  Returns a Ray with float32 x, y, dx, dy, float64 pathlength
-    and uniform z."""
-    if not isinstance(propagator, FreeSpaceParaxial):
-        raise NotImplementedError("only FreeSpaceParaxial is on the GPU path")
+    and uniform z.  ``propagator``: FreeSpaceParaxial (default) or
+    FreeSpaceDirCosine (propagator.py:79-116)."""
+    _prop_code(propagator)
     comps = _check_model(components)
     dev = _device()
     soa = _Soa(ray, dev)
@@ -266,7 +278,7 @@ def run_to_end(ray: Ray, components: Sequence[Component],
         plist = _grad_params(comps)
         zt = ray.z if isinstance(ray.z, torch.Tensor) and ray.z.requires_grad and ray.z.dim() == 0 else None
         spec = {"comps": comps, "soa": soa, "params": plist, "shape": shape,
-                "z_grad": zt is not None}
+                "z_grad": zt is not None, "propagator": propagator}
         xs = [ray.x, ray.y, ray.dx, ray.dy]
         xs = [v if isinstance(v, torch.Tensor) and v.requires_grad else
               torch.zeros((), device=dev) for v in xs]
@@ -276,7 +288,7 @@ def run_to_end(ray: Ray, components: Sequence[Component],
         ox, oy, odx, ody, opl = _TraceFn.apply(spec, *xs, pl, zin, *[p[2] for p in plist])
         zout = spec["zout"]
     else:
-        ox, oy, odx, ody, opl, zout, _, _, _ = _fwd_launch(comps, soa)
+        ox, oy, odx, ody, opl, zout, _, _, _ = _fwd_launch(comps, soa, propagator=propagator)
     out = Ray(x=ox.reshape(shape), y=oy.reshape(shape), dx=odx.reshape(shape),
               dy=ody.reshape(shape), z=zout, pathlength=opl.reshape(shape),
               _one=ray._one)
@@ -312,7 +324,7 @@ def run_iter(ray: Ray, components: Sequence[Component], propagator=FreeSpacePara
     from .components import Plane
     for c in _check_model(components):
         d = _f(c.z) - _f(ray.z)
-        ray = run_to_end(ray, [Plane(z=_f(c.z))])
+        ray = run_to_end(ray, [Plane(z=_f(c.z))], propagator=propagator)
         yield Propagator(d, propagator), ray
         ray = run_component(c, ray)
         yield c, ray
@@ -325,11 +337,11 @@ def _central(ray: Ray):
             for a in v]
 
 
-def abcd_matrix(ray: Ray, components: Sequence[Component]) -> np.ndarray:
+def abcd_matrix(ray: Ray, components: Sequence[Component], propagator=None) -> np.ndarray:
     """float64 5x5 ABCD of the model about a central ray: the reference's
     custom_jacobian_matrix(jax.jacobian(run_to_end)(ray, model))
     (README.md:224-234, utils.py:7-43), composed from component matrices."""
-    m, keep = pack_model(components)
+    m, keep = pack_model(components, propagator)
     cen = (C.c_double * 5)(*_central(ray))
     out = (C.c_double * 25)()
     N.check(N.lib().tg_abcd_compose(C.byref(m), cen, out, None), "tg_abcd_compose")
@@ -340,7 +352,7 @@ def abcd_matrix(ray: Ray, components: Sequence[Component]) -> np.ndarray:
 def solve_model(ray: Ray, model: Sequence[Component], propagator=FreeSpaceParaxial()) -> np.ndarray:
     """run.py:150-179: per-step 5x5 matrices, shape (2*n_components, 5, 5)."""
     comps = _check_model(model)
-    m, keep = pack_model(comps)
+    m, keep = pack_model(comps, propagator)
     cen = (C.c_double * 5)(*_central(ray))
     out = (C.c_double * 25)()
     steps = (C.c_double * (50 * max(1, len(comps))))()
@@ -433,7 +445,7 @@ class TracePlan:
     """
 
     def __init__(self, components, x, y, dx, dy, z=0.0, pathlength=0.0, detector: Grid | None = None,
-                 pixels: bool = False, hist_dtype=torch.int64):
+                 pixels: bool = False, hist_dtype=torch.int64, propagator=None):
         N.require_cuda(x)
         self.comps = _check_model(components)
         for t in (x, y, dx, dy):
@@ -444,7 +456,7 @@ class TracePlan:
         dev = x.device
         self.out = tuple(torch.empty(self.n, dtype=torch.float32, device=dev) for _ in range(4))
         self.pathlength = torch.empty(self.n, dtype=torch.float64, device=dev)
-        self._m, self._keep = pack_model(self.comps)
+        self._m, self._keep = pack_model(self.comps, propagator)
         self._in = _rays_struct(self.n, x, y, dx, dy, None, float(z), None, float(pathlength))
         self._o = _rays_struct(self.n, *self.out, None, 0.0, self.pathlength, 0.0)
         self._zout = C.c_double(0.0)
