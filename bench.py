@@ -535,6 +535,24 @@ def secondary_batched(torch, dev, hbm):
             "plain_per_model_ms": ms_plain, "speedup_vs_plain_per_model": ms_plain / ms}
 
 
+def secondary_transfer(torch, dev, hbm):
+    """transfer_rays: 1,048,576 rays through the cumulative products of 16
+    transfer matrices -> (N, 16, 5) float64 (671 MB written)."""
+    import temgymcore_gb300 as t
+    rng = np.random.default_rng(0)
+    n, m = 1 << 20, 16
+    rays = torch.tensor(np.hstack([rng.normal(0, 1e-3, (n, 4)), np.ones((n, 1))]), device=dev)
+    mats = rng.normal(0, 1, (m, 5, 5))
+    ms = _time(torch, lambda: t.transfer_rays(rays, mats), 20)
+    out_bytes = n * m * 5 * 8
+    return {"workload": "transfer_rays: 1,048,576 rays x 16 cumulative 5x5 matrices, float64",
+            "ms": ms, "ray_planes_per_s": n * m / (ms * 1e-3),
+            "achieved_gbs": (out_bytes + n * 40) / (ms * 1e-3) / 1e9,
+            "frac_of_hbm": (out_bytes + n * 40) / (ms * 1e-3) / 1e9 / hbm,
+            "fp64_tflops": n * m * 50 / (ms * 1e-3) / 1e12,
+            "note": "25 float64 FMAs per (ray, plane): float64-pipe bound on GB300"}
+
+
 def secondary_aberrated_scan(torch, dev, hbm):
     """The headline 4D-STEM scan with an AberratedLensKrivanek (f = 0.05 m at
     z = 0.03 m; C10 = 0.02, C12 = 0.05 at 30 deg, C23 = 5 at 10 deg,
@@ -649,6 +667,10 @@ def run_gpu(args, world, rank, local):
             secondary["input_field"] = secondary_input_field(torch, dev, bf16)
         except Exception as e:
             secondary["input_field"] = {"error": repr(e)}
+        try:
+            secondary["transfer_rays"] = secondary_transfer(torch, dev, hbm)
+        except Exception as e:
+            secondary["transfer_rays"] = {"error": repr(e)}
         try:
             secondary["aberrated_scan"] = secondary_aberrated_scan(torch, dev, hbm)
         except Exception as e:

@@ -233,6 +233,39 @@ int tg_transfer_rays_pt_src(double x0, double y0, int64_t n, const double *slope
                             const double *slopes_y, const double *matrix, double *out,
                             void *stream);
 
+/* ---- ray sources and beam decomposition ------------------------------- */
+/*
+ * tg_source_count - host: number of rays tg_source_generate writes for
+ * num_approx: the concentric-ring total of utils.py:117-175 (random = 0) or
+ * exactly num_approx (random = 1).
+ */
+int tg_source_count(int64_t num_approx, int32_t random, int64_t *n_rays);
+
+/*
+ * tg_source_generate - Source.generate_array (source.py:36-188) on the GPU:
+ * out (device float64 [n][5], rows x, y, dx, dy, 1; capacity >= the count
+ * above).  kind 0 = PointSource (extent = semi_conv: slopes on the disc,
+ * positions at the offset), 1 = ParallelBeam (extent = radius: positions on
+ * the disc plus the offset, zero slopes).  random = 0: the reference's
+ * concentric rings, ray for ray (its running-angle recurrence included);
+ * random = 1: uniform in the disc from a hash of (seed, index) - the
+ * reference's distribution, not its NumPy draws.
+ */
+int tg_source_generate(int32_t kind, int32_t random, int64_t num_approx, uint64_t seed,
+                       double extent, double off_x, double off_y, double *out, int64_t capacity,
+                       void *stream);
+
+/*
+ * tg_decompose_q_inv - gaussian.py:35-89 for n beams: q_inv (device complex128
+ * [n][2][2], re/im interleaved), wavelength (device float64 [n] or NULL =
+ * wavelength_scalar) -> waist, radii (device float64 [n][2]: major axis first)
+ * and theta (device float64 [n]).  theta is the reference's up to a multiple
+ * of pi (an eigenvector's sign is a solver convention; Q^-1 is unchanged).
+ */
+int tg_decompose_q_inv(int64_t n, const double *q_inv, const double *wavelength,
+                       double wavelength_scalar, double eps, double *waist, double *radii,
+                       double *theta, void *stream);
+
 /* ---- many models in one persistent launch ------------------------------ */
 typedef struct tg_batch_info {
   size_t plan_bytes;       /* bytes of the packed plan (copy it to the device) */

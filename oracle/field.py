@@ -8,6 +8,7 @@ Follows:
   - ``_beam_field``                              gaussian.py:276-316
   - ``propagate_misaligned_gaussian_jax_scan``   gaussian.py:319-337
   - ``map_reduce`` (a plain sum over beams)      gaussian.py:340-369
+  - ``decompose_Q_inv``                          gaussian.py:35-89
   - ``evaluate_gaussian_input_image``            gaussian.py:372-400
   - ``_input_beam_field``                        gaussian.py:403-409
   - ``fibonacci_spiral``                         utils.py:297-325
@@ -218,6 +219,38 @@ def evaluate_gaussian_input_image(rays: dict, grid: dict, pixel_index=None, chun
     if pixel_index is not None:
         return acc
     return acc.reshape(grid["shape"])
+
+
+def decompose_Q_inv(Q_inv, wavelength, eps=1e-12):
+    """gaussian.py:35-89 with NumPy's eigh (LAPACK's eigenvector signs)."""
+    Q = np.asarray(Q_inv)
+    S = np.imag(Q)
+    S = 0.5 * (S + np.swapaxes(S, -1, -2))
+    _, evecs = np.linalg.eigh(S)
+    det = np.linalg.det(evecs)
+    sign = np.where(det < 0, -1.0, 1.0)
+    evecs = evecs.copy()
+    evecs[..., :, 1] *= sign[..., None]
+    Vt = np.swapaxes(evecs, -1, -2)
+    Qd = Vt @ Q @ evecs
+    qdiag = np.stack([Qd[..., 0, 0], Qd[..., 1, 1]], axis=-1)
+    imd_pre = np.imag(qdiag)
+    with np.errstate(divide="ignore"):
+        waists_pre = np.sqrt(np.where(np.abs(imd_pre) > eps, np.abs(wavelength / (np.pi * imd_pre)), np.inf))
+    swap = waists_pre[..., 0] < waists_pre[..., 1]
+    qdiag = np.where(swap[..., None], qdiag[..., ::-1], qdiag)
+    evecs = np.where(swap[..., None, None], evecs[..., :, ::-1], evecs)
+    det = np.linalg.det(evecs)
+    sign = np.where(det < 0, -1.0, 1.0)
+    evecs = evecs.copy()
+    evecs[..., :, 1] *= sign[..., None]
+    imd, red = np.imag(qdiag), np.real(qdiag)
+    with np.errstate(divide="ignore"):
+        waists = np.sqrt(np.where(np.abs(imd) > eps, np.abs(wavelength / (np.pi * imd)), np.inf))
+        radii = np.where(np.abs(red) > eps, 1.0 / red, np.inf)
+    e1 = evecs[..., :, 0]
+    theta = np.arctan2(e1[..., 1], e1[..., 0])
+    return waists[..., 0], waists[..., 1], radii[..., 0], radii[..., 1], theta
 
 
 def fibonacci_spiral(nb_samples: int, radius: float, alpha=2):

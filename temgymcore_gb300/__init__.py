@@ -72,6 +72,7 @@ from .run import (  # noqa: E402,F401
 )
 from .scan import scan_images, scan_positions, probe_model  # noqa: E402,F401
 from .gaussian import (  # noqa: E402,F401
-    make_gaussian_image, evaluate_gaussian_input_image, FieldPlan, fibonacci_spiral)
+    make_gaussian_image, evaluate_gaussian_input_image, FieldPlan, fibonacci_spiral, decompose_Q_inv)
+from .sources import concentric_rings, random_coords  # noqa: E402,F401
 
 __version__ = "0.1.0"

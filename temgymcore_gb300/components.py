@@ -55,25 +55,46 @@ class Component:
 
 
 class Source(Component):
-    """Pass-through source marker (source.py:11-34): run_iter inserts free
-    space before it like any component.  Ray generation is host-side set-up
-    and out of this package's scope."""
+    """Source (source.py:11-79): a no-op as a model element (run_iter inserts
+    free space before it like any component) that also generates its initial
+    rays on the GPU."""
+
+    def generate_array(self, num: int, random: bool = False, seed: int = 0) -> torch.Tensor:
+        """(N, 5) float64 device rays [x, y, dx, dy, 1] (source.py:36-57)."""
+        raise NotImplementedError
+
+    def make_rays(self, num: int, random: bool = False, seed: int = 0) -> Ray:
+        """Ray of the generated array at the source's z (source.py:59-79);
+        scalar fields when only one ray is generated."""
+        r = self.generate_array(num, random=random, seed=seed)
+        sl = 0 if r.shape[0] == 1 else slice(None)
+        return Ray(x=r[sl, 0], y=r[sl, 1], dx=r[sl, 2], dy=r[sl, 3], z=self.z, pathlength=0.0)
 
 
 @dataclass(frozen=True)
 class PointSource(Source):
-    """source.py:82-135 (as a model element: a no-op at z)."""
+    """source.py:82-135: rays from a point at ``offset_xy`` with slopes filling
+    a cone of ``semi_conv`` (concentric rings, or uniform random)."""
     z: Any
     semi_conv: Any = 0.0
     offset_xy: Any = (0.0, 0.0)
 
+    def generate_array(self, num: int, random: bool = False, seed: int = 0) -> torch.Tensor:
+        from .sources import POINT, generate
+        return generate(POINT, num, _f(self.semi_conv), self.offset_xy, random, seed)
+
 
 @dataclass(frozen=True)
 class ParallelBeam(Source):
-    """source.py:138-188 (as a model element: a no-op at z)."""
+    """source.py:138-188: parallel rays filling a disc of ``radius`` around
+    ``offset_xy``."""
     z: Any
     radius: Any = 0.0
     offset_xy: Any = (0.0, 0.0)
+
+    def generate_array(self, num: int, random: bool = False, seed: int = 0) -> torch.Tensor:
+        from .sources import PARALLEL, generate
+        return generate(PARALLEL, num, _f(self.radius), self.offset_xy, random, seed)
 
 
 class DescanError(NamedTuple):

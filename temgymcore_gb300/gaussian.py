@@ -54,6 +54,8 @@ N.register("tg_field_prep", C.c_int, [C.POINTER(N.TgModel), C.POINTER(TgBeams), 
                                       C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p])
 N.register("tg_field_prep_input", C.c_int, [C.POINTER(TgBeams), C.POINTER(TgPixelMap), C.c_void_p,
                                             C.c_size_t, C.c_void_p, C.c_void_p])
+N.register("tg_decompose_q_inv", C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_double, C.c_double,
+                                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p])
 N.register("tg_field_eval", C.c_int, [C.c_int32, C.c_int64, C.POINTER(TgPixelMap), C.c_void_p,
                                       C.c_void_p, C.c_size_t, C.c_void_p])
 
@@ -203,6 +205,33 @@ def evaluate_gaussian_input_image(gaussian_rays: GaussianRay, grid, batch_size: 
     sampled at the pixel centres of ``grid`` (gaussian.py:372-400)."""
     plan = FieldPlan(gaussian_rays, None, method, grid=grid)
     return plan.evaluate().clone()
+
+
+def decompose_Q_inv(Q_inv, wavelength, eps: float = 1e-12):
+    """gaussian.py:35-89: (waist_x, waist_y, r_x, r_y, theta) of 2x2 complex
+    Q^-1 matrices (leading batch axes allowed), the major axis first.  theta
+    equals the reference's up to a multiple of pi."""
+    dev = _device()
+    q = Q_inv if isinstance(Q_inv, torch.Tensor) else torch.as_tensor(np.asarray(Q_inv, np.complex128))
+    q = q.to(device=dev, dtype=torch.complex128)
+    batch = tuple(q.shape[:-2])
+    q = q.reshape(-1, 2, 2).contiguous()
+    n = q.shape[0]
+    wl = torch.as_tensor(wavelength, dtype=torch.float64)
+    wl_t = None
+    if wl.numel() > 1:
+        if wl.numel() != n:
+            raise ValueError("wavelength must be a scalar or one value per matrix")
+        wl_t = wl.to(dev).reshape(-1).contiguous()
+    waist = torch.empty((n, 2), dtype=torch.float64, device=dev)
+    radii = torch.empty((n, 2), dtype=torch.float64, device=dev)
+    theta = torch.empty(n, dtype=torch.float64, device=dev)
+    N.check(N.lib().tg_decompose_q_inv(n, torch.view_as_real(q).data_ptr(), N.ptr(wl_t),
+                                       float(wl.reshape(-1)[0]) if wl_t is None else 0.0, float(eps),
+                                       waist.data_ptr(), radii.data_ptr(), theta.data_ptr(),
+                                       N.stream_ptr()), "tg_decompose_q_inv")
+    rs = lambda t: t.reshape(batch) if batch else t.reshape(())  # noqa: E731
+    return rs(waist[:, 0]), rs(waist[:, 1]), rs(radii[:, 0]), rs(radii[:, 1]), rs(theta)
 
 
 def fibonacci_spiral(nb_samples: int, radius: float, alpha=2):
