@@ -43,8 +43,8 @@ N.register("tg_batch_run", C.c_int, [C.c_void_p, C.POINTER(TgBatchInfo), C.POINT
                                      C.c_int32, C.c_void_p, C.c_size_t, C.c_void_p])
 
 # (tile rays, block, rays per thread) candidates
-CANDIDATES = [(1024, 256, 1), (2048, 256, 2), (4096, 256, 4), (2048, 512, 1), (4096, 512, 2),
-              (8192, 256, 4), (8192, 512, 4)]
+CANDIDATES = [(2048, 256, 2), (4096, 256, 2), (4096, 128, 4), (8192, 256, 2), (4096, 256, 4),
+              (4096, 512, 2), (8192, 256, 4), (2048, 256, 1)]
 
 
 class _TuneCache:
@@ -140,7 +140,7 @@ class BatchedTrace:
     def signature(self) -> str:
         return f"m{len(self.models)}-r{self.total}-s{int(self.info.total_steps)}"
 
-    def autotune(self, x, y, dx, dy, out, targets=None, raw=None, reps=3):
+    def autotune(self, x, y, dx, dy, out, targets=None, raw=None, reps=5):
         """Time each candidate launch shape on this workload; keep the fastest."""
         key = self.signature() + ("-adj" if targets is not None else "-fwd")
         hit = TUNE_CACHE.get(key)

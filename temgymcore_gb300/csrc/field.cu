@@ -532,57 +532,57 @@ __device__ __forceinline__ void split_bf16(float v, __nv_bfloat16_raw& hi, __nv_
 
 // One thread per (beam, block of kOpLines lines): the beam's coefficients are
 // loaded once and the phase advances by exact 64-bit increments from line to
-// line.  Consecutive threads take consecutive beams, so each plane write of
-// a warp is one contiguous 64-byte run.  Line blocks [0, lines_v) are V
-// rows, the rest U columns.
+// line.  blockIdx.y is the line block ([0, lines_v / kOpLines) V rows, then U
+// columns; both paddings are multiples of kOpLines), blockIdx.x * blockDim.x
+// + threadIdx.x the beam, so there is no index division and the line loop
+// needs no bound.  Consecutive threads take consecutive beams: each plane
+// store of a warp is one contiguous 64-byte run.
 constexpr int kOpLines = 16;
 
 __global__ void __launch_bounds__(256) k_field_operands(const __grid_constant__ OperandArgs A) {
-  const int64_t vblocks = (A.lines_v + kOpLines - 1) / kOpLines;
-  const int64_t ublocks = (A.lines_u + kOpLines - 1) / kOpLines;
-  const int64_t total = (vblocks + ublocks) * A.kpad;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t lb = i / A.kpad, b = i - lb * A.kpad;
-    const bool isv = lb < vblocks;
-    const int64_t line0 = (isv ? lb : lb - vblocks) * kOpLines;
-    const int64_t nlines = isv ? A.lines_v : A.lines_u;
-    const int64_t live_lines = isv ? A.h : A.w;
-    const int64_t plane = nlines * A.kpad;
-    __nv_bfloat16_raw* base = (isv ? A.v_planes : A.u_planes) + line0 * A.kpad + b;
-    const bool live_b = b < A.n;
-    uint64_t p2 = 0, p1 = 0, p0 = 0;
-    float cen = 0.f, e0 = 0.f, bq = 0.f, bl = 0.f;
-    if (live_b) {
-      const BeamFast& B = A.beams[b];
-      if (B.p_rc != 0 || B.b_rc != 0.f) atomicOr(&g_tg_err, 0x10u);
-      if (isv) { p2 = B.p_rr; p1 = B.p_r; p0 = B.p_0; cen = B.r0; e0 = B.e0; bq = B.b_rr; bl = B.l_r; }
-      else { p2 = B.p_cc; p1 = B.p_c; p0 = 0; cen = B.c0; e0 = 0.f; bq = B.b_cc; bl = B.l_c; }
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= A.kpad) return;
+  const int vblocks = A.lines_v / kOpLines;
+  const bool isv = (int)blockIdx.y < vblocks;
+  const int line0 = ((int)blockIdx.y - (isv ? 0 : vblocks)) * kOpLines;
+  const int live_lines = isv ? A.h : A.w;
+  const int64_t kpad = A.kpad;
+  const int64_t plane = (isv ? A.lines_v : A.lines_u) * kpad;
+  __nv_bfloat16_raw* dst = (isv ? A.v_planes : A.u_planes) + line0 * kpad + b;
+  const bool live_b = b < A.n;
+  uint64_t p2 = 0, p1 = 0, p0 = 0;
+  float cen = 0.f, e0 = 0.f, bq = 0.f, bl = 0.f;
+  if (live_b) {
+    const BeamFast& B = A.beams[b];
+    if (B.p_rc != 0 || B.b_rc != 0.f) atomicOr(&g_tg_err, 0x10u);
+    if (isv) { p2 = B.p_rr; p1 = B.p_r; p0 = B.p_0; cen = B.r0; e0 = B.e0; bq = B.b_rr; bl = B.l_r; }
+    else { p2 = B.p_cc; p1 = B.p_c; p0 = 0; cen = B.c0; e0 = 0.f; bq = B.b_cc; bl = B.l_c; }
+  }
+  // exact phase at line0 and its first difference; second difference 2*p2
+  const uint64_t u0 = (uint64_t)line0;
+  uint64_t th = p2 * (u0 * u0) + p1 * u0 + p0;
+  uint64_t dth = p2 * (2 * u0 + 1) + p1;
+  const uint64_t ddth = 2 * p2;
+  float d = (float)line0 - cen;
+#pragma unroll 4
+  for (int j = 0; j < kOpLines; ++j) {
+    float re = 0.f, im = 0.f;
+    if (live_b && line0 + j < live_lines) {
+      const float2 z = cexpf_turn(e0 - (bq * d * d + bl * d), th);
+      re = z.x;
+      im = z.y;
     }
-    // exact phase at line0 and its first difference; second difference 2*p2
-    const uint64_t u0 = (uint64_t)line0;
-    uint64_t th = p2 * (u0 * u0) + p1 * u0 + p0;
-    uint64_t dth = p2 * (2 * u0 + 1) + p1;
-    const uint64_t ddth = 2 * p2;
-    for (int j = 0; j < kOpLines && line0 + j < nlines; ++j) {
-      float re = 0.f, im = 0.f;
-      if (live_b && line0 + j < live_lines) {
-        const float d = (float)(line0 + j) - cen;
-        const float2 z = cexpf_turn(e0 - (bq * d * d + bl * d), th);
-        re = z.x;
-        im = z.y;
-      }
-      __nv_bfloat16_raw* dst = base + (int64_t)j * A.kpad;
-      __nv_bfloat16_raw h, l;
-      split_bf16(re, h, l);
-      dst[0] = h;
-      dst[plane] = l;
-      split_bf16(im, h, l);
-      dst[2 * plane] = h;
-      dst[3 * plane] = l;
-      th += dth;
-      dth += ddth;
-    }
+    __nv_bfloat16_raw h, l;
+    split_bf16(re, h, l);
+    dst[0] = h;
+    dst[plane] = l;
+    split_bf16(im, h, l);
+    dst[2 * plane] = h;
+    dst[3 * plane] = l;
+    dst += kpad;
+    d += 1.f;
+    th += dth;
+    dth += ddth;
   }
 }
 
@@ -848,7 +848,9 @@ extern "C" int tg_field_eval(int32_t method, int64_t n_beams, const tg_pixel_map
     A.w = pm->w;
     A.v_planes = reinterpret_cast<__nv_bfloat16_raw*>(ws + L.vplanes);
     A.u_planes = reinterpret_cast<__nv_bfloat16_raw*>(ws + L.uplanes);
-    k_field_operands<<<sm_count_field() * 8, 256, 0, s>>>(A);
+    if (L.lines_v % kOpLines || L.lines_u % kOpLines || L.kpad > INT32_MAX) return TG_ERR_TOO_LARGE;
+    k_field_operands<<<dim3((unsigned)((L.kpad + 255) / 256), (unsigned)((L.lines_v + L.lines_u) / kOpLines)), 256,
+                       0, s>>>(A);
     int st = launch_field_gemm(A.v_planes, A.u_planes, L.lines_v, L.lines_u, L.kpad, L.chunks,
                                pm->h, pm->w, part, s);
     if (st != TG_OK) return st;
