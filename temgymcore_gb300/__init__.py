@@ -74,5 +74,7 @@ from .scan import scan_images, scan_positions, probe_model  # noqa: E402,F401
 from .gaussian import (  # noqa: E402,F401
     make_gaussian_image, evaluate_gaussian_input_image, FieldPlan, fibonacci_spiral, decompose_Q_inv)
 from .sources import concentric_rings, random_coords  # noqa: E402,F401
+from .batched import BatchedTrace  # noqa: E402,F401
+from .fit import StemFit  # noqa: E402,F401
 
 __version__ = "0.1.0"
