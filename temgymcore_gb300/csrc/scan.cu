@@ -12,8 +12,11 @@
 //      keeps each ray's packed pixel in shared memory,
 //   3. reduces the hits' bounding box; when it fits the shared-memory window
 //      (the normal case: a probe lights a small disc) it histograms there,
-//   4. streams the whole dense image to HBM once with 16-byte stores
-//      (window counts inside, zeros elsewhere).
+//   4. writes the dense image once: the image rows outside the window's row
+//      span are all zeros and leave as TMA bulk copies from a zero buffer
+//      in shared memory (asynchronous: the CTA goes on to the next probe
+//      while the copy engine streams them), the window rows as 16-byte
+//      stores of counts and zeros.
 // A probe whose hits do not fit the window, or a bundle larger than the
 // shared ray buffer, takes the slow path: zero-fill, barrier, global atomics.
 // The HBM traffic is therefore the dense histogram write, ~h*w*4 bytes/probe.
@@ -27,7 +30,9 @@ namespace tg {
 
 constexpr int kScanThreads = 256;
 constexpr int kMaxSmemRays = 4096;  // packed pixels kept in shared memory
-constexpr int kWinBins = 7680;      // shared histogram window (u32 counters);
+constexpr int kWinBins = 5632;      // shared histogram window (u32 counters)
+constexpr int kScanBands = 1;       // row bands per probe image (work items per probe)
+constexpr int kZeroBytes = 8192;    // zero source of the bulk row copies;
                                     // static shared memory stays under 48 KB
 
 struct ScanArgs {
@@ -96,11 +101,23 @@ k_scan_hist(const __grid_constant__ Program P, const __grid_constant__ ScanArgs 
   __shared__ float4 pshift[kMaxProbeOps];
   __shared__ uint32_t pix[kMaxSmemRays];  // (py << 16) | px, or 0xffffffff = no hit
   __shared__ uint32_t win[kWinBins];
+  __shared__ __align__(128) int4 zbuf[kZeroBytes / 16];
   __shared__ int red[kScanThreads / 32];
   const int64_t n = A.n;
   const bool fits = n <= kMaxSmemRays;
   const int H = A.h, W = A.w;
-  for (int p = blockIdx.x; p < A.n_probes; p += gridDim.x) {
+  for (int i = threadIdx.x; i < kZeroBytes / 16; i += blockDim.x) zbuf[i] = make_int4(0, 0, 0, 0);
+  // the bulk copies read zbuf through the async proxy
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  __syncthreads();
+  const uint32_t zsrc = (uint32_t)__cvta_generic_to_shared(zbuf);
+  // work item = (probe, band of kScanBands row bands); each band re-traces
+  // the (L2-resident) bundle and keeps only its rows' hits.  Measured on the
+  // 64x64-probe workload: one band 0.179 ms, two bands 0.186 ms (the doubled
+  // per-item trace and barriers cost more than the finer balance gains)
+  for (int it = blockIdx.x; it < kScanBands * A.n_probes; it += gridDim.x) {
+    const int p = it / kScanBands, band = it - p * kScanBands;
+    const int ra = (int)((int64_t)band * H / kScanBands), rb = (int)((int64_t)(band + 1) * H / kScanBands);
     if (threadIdx.x == 0) probe_shifts(P, A, p, pshift);
     __syncthreads();
     int rmin = 0x7fffffff, rmax = -1, cmin = 0x7fffffff, cmax = -1;
@@ -108,13 +125,13 @@ k_scan_hist(const __grid_constant__ Program P, const __grid_constant__ ScanArgs 
       RayS r;
       bool alive;
       trace_one(P, pshift, A.x[i], A.y[i], A.dx[i], A.dy[i], A.z_scalar, r, alive);
-      if (A.probe_xy) {
+      if (A.probe_xy && band == 0) {  // written once per probe
         A.probe_xy[(size_t)p * 2 * n + i] = r.x;
         A.probe_xy[(size_t)p * 2 * n + n + i] = r.y;
       }
       int py, px;
       bin_yx(r.x, r.y, B, py, px);
-      bool ok = alive && py >= 0 && py < H && px >= 0 && px < W;
+      bool ok = alive && py >= ra && py < rb && px >= 0 && px < W;
       if (!(isfinite(r.x) && isfinite(r.y))) atomicOr(&g_tg_err, TG_EW_NONFINITE);
       if (fits) pix[i] = ok ? ((uint32_t)py << 16) | (uint32_t)px : 0xffffffffu;
       if (ok) {
@@ -143,14 +160,36 @@ k_scan_hist(const __grid_constant__ Program P, const __grid_constant__ ScanArgs 
         }
         __syncthreads();
       }
-      // dense write of the whole image: window counts inside, zeros outside
       if (A.vec4) {
+        // band rows outside [r0, r1) are zeros: bulk copies of the zero
+        // buffer (row starts are 16-byte aligned: W is a multiple of 4 and
+        // the images 16-byte aligned); one thread issues them, the group is
+        // committed and left in flight
+        const int r0 = any ? rmin : ra, r1 = any ? rmax + 1 : ra;
+        if (threadIdx.x == 0) {
+          char* base = reinterpret_cast<char*>(img);
+          const int64_t row_bytes = (int64_t)W * 4;
+          const int64_t spans[2][2] = {{ra * row_bytes, r0 * row_bytes}, {r1 * row_bytes, rb * row_bytes}};
+          for (int sp = 0; sp < 2; ++sp)
+            for (int64_t off = spans[sp][0]; off < spans[sp][1]; off += kZeroBytes) {
+              const int64_t left = spans[sp][1] - off;
+              const uint32_t bytes = (uint32_t)(left < kZeroBytes ? left : kZeroBytes);
+              asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
+                           :: "l"(base + off), "r"(zsrc), "r"(bytes) : "memory");
+            }
+          asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+          // keep at most four items' copies in flight (a hardware wait on
+          // the copy engine, no polling)
+          asm volatile("cp.async.bulk.wait_group.read 4;" ::: "memory");
+        }
+        // window rows: counts inside [cmin, cmax], zeros elsewhere
         const int w4 = W >> 2;
-        const int total = H * w4;
+        const int total = (r1 - r0) * w4;
+        int4* rows = reinterpret_cast<int4*>(img) + (int64_t)r0 * w4;
         for (int i = threadIdx.x; i < total; i += blockDim.x) {
-          const int row = i / w4, c0 = (i - row * w4) << 2;
+          const int row = r0 + i / w4, c0 = (i % w4) << 2;
           int4 v = make_int4(0, 0, 0, 0);
-          if (any && row >= rmin && row <= rmax && c0 + 3 >= cmin && c0 <= cmax) {
+          if (c0 + 3 >= cmin && c0 <= cmax) {
             const uint32_t* wrow = win + (row - rmin) * wc;
             int c = c0;
             v.x = (c >= cmin && c <= cmax) ? (int)wrow[c - cmin] : 0; ++c;
@@ -158,10 +197,10 @@ k_scan_hist(const __grid_constant__ Program P, const __grid_constant__ ScanArgs 
             v.z = (c >= cmin && c <= cmax) ? (int)wrow[c - cmin] : 0; ++c;
             v.w = (c >= cmin && c <= cmax) ? (int)wrow[c - cmin] : 0;
           }
-          __stcs(reinterpret_cast<int4*>(img) + i, v);
+          __stcs(rows + i, v);
         }
       } else {
-        for (int i = threadIdx.x; i < H * W; i += blockDim.x) {
+        for (int i = ra * W + threadIdx.x; i < rb * W; i += blockDim.x) {
           const int row = i / W, c = i - row * W;
           int v = 0;
           if (any && row >= rmin && row <= rmax && c >= cmin && c <= cmax)
@@ -170,8 +209,8 @@ k_scan_hist(const __grid_constant__ Program P, const __grid_constant__ ScanArgs 
         }
       }
     } else {
-      // slow path: zero the image, then global atomics (re-trace if needed)
-      for (int i = threadIdx.x; i < H * W; i += blockDim.x) img[i] = 0;
+      // slow path: zero the band's rows, then global atomics (re-trace if needed)
+      for (int i = ra * W + threadIdx.x; i < rb * W; i += blockDim.x) img[i] = 0;
       __syncthreads();
       for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
         int py, px;
@@ -186,13 +225,15 @@ k_scan_hist(const __grid_constant__ Program P, const __grid_constant__ ScanArgs 
           bool alive;
           trace_one(P, pshift, A.x[i], A.y[i], A.dx[i], A.dy[i], A.z_scalar, r, alive);
           bin_yx(r.x, r.y, B, py, px);
-          ok = alive && py >= 0 && py < H && px >= 0 && px < W;
+          ok = alive && py >= ra && py < rb && px >= 0 && px < W;
         }
         if (ok) atomicAdd(img + py * W + px, 1);
       }
     }
-    __syncthreads();  // shared buffers are reused by the next probe
+    __syncthreads();  // shared buffers are reused by the next item
   }
+  // every bulk copy has read zbuf and written its rows before the CTA exits
+  if (threadIdx.x == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
 }
 
 static int sm_count_scan() {
@@ -243,7 +284,7 @@ extern "C" int tg_scan_hist(const tg_model* model, const tg_rays* bundle, const 
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scan_hist, kScanThreads, 0);
   if (per_sm < 1) per_sm = 1;
   int blocks = sm_count_scan() * per_sm;
-  if (blocks > scan->n_probes) blocks = scan->n_probes;
+  if (blocks > kScanBands * scan->n_probes) blocks = kScanBands * scan->n_probes;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   k_scan_hist<<<blocks, kScanThreads, 0, s>>>(P, A, B);
   return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;

@@ -81,3 +81,23 @@ def test_stem_empty_cases(cuda):
     imgs = t.scan_images(t.Ray(x=e, y=e, dx=e, dy=e, z=0.0, pathlength=0.0), model,
                          positions=np.zeros((0, 2)))
     assert imgs.shape == (0, 256, 256)
+
+
+def test_stem_probes_that_miss_and_garbage_output(cuda):
+    """Probes whose whole bundle misses the detector (images written only by
+    the zero-row copies), probes near the edge (window rows at the image
+    border), over an output buffer pre-filled with garbage."""
+    import temgymcore_gb300 as t
+    from temgymcore_gb300.workloads import stem_4d, stem_model
+    w = stem_4d(seed=5, scan=(2, 2), rays_per_probe=1024)
+    model = stem_model(w)
+    ray = t.Ray(x=torch.tensor(w["x"], device=cuda), y=torch.tensor(w["y"], device=cuda),
+                dx=torch.tensor(w["dx"], device=cuda), dy=torch.tensor(w["dy"], device=cuda),
+                z=0.0, pathlength=0.0)
+    half = 0.5 * 256 * w["detector"]["pixel_size"][0]
+    pos = np.array([[0.0, 0.0], [1.0, 1.0], [half * 0.98, 0.0], [0.0, -half * 0.98], [-half * 0.97, half * 0.97]])
+    out = torch.full((len(pos), 256, 256), 12345, dtype=torch.int32, device=cuda)
+    imgs, xy = t.scan_images(ray, model, positions=pos, out=out, return_xy=True)
+    _check(w, imgs, xy, pos)
+    assert int(imgs[1].abs().sum()) == 0
+    assert t._native.error_word() == 0
