@@ -46,6 +46,7 @@ struct ScanArgs {
   float* probe_xy;  // optional [n_probes][2][n]
   int32_t h, w;
   int32_t vec4;  // rows are 16-byte aligned: dense write with int4 stores
+  int32_t bulk;  // images in device memory: zero rows as TMA bulk copies
 };
 
 __device__ __forceinline__ void probe_shifts(const Program& P, const ScanArgs& A, int p,
@@ -164,9 +165,10 @@ k_scan_hist(const __grid_constant__ Program P, const __grid_constant__ ScanArgs 
         // band rows outside [r0, r1) are zeros: bulk copies of the zero
         // buffer (row starts are 16-byte aligned: W is a multiple of 4 and
         // the images 16-byte aligned); one thread issues them, the group is
-        // committed and left in flight
-        const int r0 = any ? rmin : ra, r1 = any ? rmax + 1 : ra;
-        if (threadIdx.x == 0) {
+        // committed and left in flight.  Images in host memory (written
+        // across the host link) take 16-byte stores for every row instead.
+        const int r0 = A.bulk ? (any ? rmin : ra) : ra, r1 = A.bulk ? (any ? rmax + 1 : ra) : rb;
+        if (A.bulk && threadIdx.x == 0) {
           char* base = reinterpret_cast<char*>(img);
           const int64_t row_bytes = (int64_t)W * 4;
           const int64_t spans[2][2] = {{ra * row_bytes, r0 * row_bytes}, {r1 * row_bytes, rb * row_bytes}};
@@ -189,7 +191,7 @@ k_scan_hist(const __grid_constant__ Program P, const __grid_constant__ ScanArgs 
         for (int i = threadIdx.x; i < total; i += blockDim.x) {
           const int row = r0 + i / w4, c0 = (i % w4) << 2;
           int4 v = make_int4(0, 0, 0, 0);
-          if (c0 + 3 >= cmin && c0 <= cmax) {
+          if (any && row >= rmin && row <= rmax && c0 + 3 >= cmin && c0 <= cmax) {
             const uint32_t* wrow = win + (row - rmin) * wc;
             int c = c0;
             v.x = (c >= cmin && c <= cmax) ? (int)wrow[c - cmin] : 0; ++c;
@@ -233,7 +235,7 @@ k_scan_hist(const __grid_constant__ Program P, const __grid_constant__ ScanArgs 
     __syncthreads();  // shared buffers are reused by the next item
   }
   // every bulk copy has read zbuf and written its rows before the CTA exits
-  if (threadIdx.x == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+  if (A.bulk && threadIdx.x == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
 }
 
 static int sm_count_scan() {
@@ -279,6 +281,13 @@ extern "C" int tg_scan_hist(const tg_model* model, const tg_rays* bundle, const 
   A.h = grid->h;
   A.w = grid->w;
   A.vec4 = ((grid->w & 3) == 0) && ((reinterpret_cast<uintptr_t>(hist) & 15) == 0);
+  {  // images may live in pinned host memory (written by the kernel across the host link)
+    cudaPointerAttributes pa;
+    if (cudaPointerGetAttributes(&pa, hist) != cudaSuccess) return TG_ERR_CUDA;
+    A.bulk = A.vec4 && pa.type == cudaMemoryTypeDevice;
+    if (pa.type != cudaMemoryTypeDevice && pa.type != cudaMemoryTypeHost && pa.type != cudaMemoryTypeManaged)
+      return TG_ERR_INVALID;  // unregistered host memory
+  }
   BinCoef B = make_bincoef(grid);
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scan_hist, kScanThreads, 0);

@@ -75,7 +75,9 @@ def scan_images(ray: Ray, model, scan_grid: ScanGrid | None = None, detector: Gr
     ``model`` at every scan position of ``scan_grid`` (row-major probe order)
     or of ``positions`` ((n, 2) x, y metres), binned on ``detector``
     (default: the model's last component).  With ``return_xy`` also returns
-    the per-probe detector coordinates (n_probes, 2, n_rays) float32."""
+    the per-probe detector coordinates (n_probes, 2, n_rays) float32.
+    ``out`` may be a pinned host tensor: the kernel then writes the images
+    straight across the host link (no separate copy)."""
     comps = _check_model(model)
     if scan_grid is None and positions is None:
         found = [c for c in comps if isinstance(c, ScanGrid)]
@@ -101,6 +103,8 @@ def scan_images(ray: Ray, model, scan_grid: ScanGrid | None = None, detector: Gr
         out = torch.empty((s.n_probes, h, w), dtype=torch.int32, device=dev)
     if tuple(out.shape) != (s.n_probes, h, w) or out.dtype != torch.int32 or not out.is_contiguous():
         raise ValueError("out must be a contiguous int32 tensor (n_probes, H, W)")
+    if not out.is_cuda and not out.is_pinned():
+        raise ValueError("out must be a CUDA tensor or a pinned host tensor")
     xy = torch.empty((s.n_probes, 2, n), dtype=torch.float32, device=dev) if return_xy else None
     m, keep = pack_scan_model(comps)
     g = detector._tg_grid()

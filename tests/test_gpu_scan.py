@@ -101,3 +101,24 @@ def test_stem_probes_that_miss_and_garbage_output(cuda):
     _check(w, imgs, xy, pos)
     assert int(imgs[1].abs().sum()) == 0
     assert t._native.error_word() == 0
+
+
+def test_stem_images_into_pinned_host_memory(cuda):
+    """scan_images with a pinned host output (the kernel writes across the
+    host link, plain stores instead of the bulk zero rows) equals the device
+    result."""
+    import temgymcore_gb300 as t
+    from temgymcore_gb300.workloads import stem_4d, stem_model
+    w = stem_4d(seed=6, scan=(3, 4), rays_per_probe=1024)
+    model = stem_model(w)
+    ray = t.Ray(x=torch.tensor(w["x"], device=cuda), y=torch.tensor(w["y"], device=cuda),
+                dx=torch.tensor(w["dx"], device=cuda), dy=torch.tensor(w["dy"], device=cuda),
+                z=0.0, pathlength=0.0)
+    dev_imgs = t.scan_images(ray, model)
+    host = torch.full((12, 256, 256), -7, dtype=torch.int32).pin_memory()
+    t.scan_images(ray, model, out=host)
+    torch.cuda.synchronize()
+    assert torch.equal(host, dev_imgs.cpu())
+    with pytest.raises(ValueError):
+        t.scan_images(ray, model, out=torch.zeros((12, 256, 256), dtype=torch.int32))
+    assert t._native.error_word() == 0
