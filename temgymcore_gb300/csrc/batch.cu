@@ -302,6 +302,13 @@ k_batch(const uint8_t* __restrict__ plan, const __grid_constant__ BatchIO io,
     const float* __restrict__ gy = io.y + T.start;
     const float* __restrict__ gdx = io.dx + T.start;
     const float* __restrict__ gdy = io.dy + T.start;
+    float* __restrict__ ox = io.ox + T.start;
+    float* __restrict__ oy = io.oy + T.start;
+    float* __restrict__ odx = io.odx + T.start;
+    float* __restrict__ ody = io.ody + T.start;
+    double* __restrict__ opl = io.opl ? io.opl + T.start : nullptr;
+    const float* __restrict__ gtx = adj ? io.tx + T.start : nullptr;
+    const float* __restrict__ gty = adj ? io.ty + T.start : nullptr;
     float mw[10];
 #pragma unroll
     for (int j = 0; j < 10; ++j) mw[j] = 0.f;
@@ -321,8 +328,8 @@ k_batch(const uint8_t* __restrict__ plan, const __grid_constant__ BatchIO io,
         const int i = inr[k] ? idx[k] : 0;
         v0[k][0] = gx[i]; v0[k][1] = gy[i]; v0[k][2] = gdx[i]; v0[k][3] = gdy[i];
         if (adj) {
-          tx[k] = io.tx[T.start + i];
-          ty[k] = io.ty[T.start + i];
+          tx[k] = gtx[i];
+          ty[k] = gty[i];
         }
         x[k] = v0[k][0]; y[k] = v0[k][1]; dx[k] = v0[k][2]; dy[k] = v0[k][3];
         pl[k] = 0.f;
@@ -385,12 +392,12 @@ k_batch(const uint8_t* __restrict__ plan, const __grid_constant__ BatchIO io,
 #pragma unroll
       for (int k = 0; k < R; ++k) {
         if (inr[k]) {
-          const int64_t i = T.start + idx[k];
-          io.ox[i] = x[k];
-          io.oy[i] = y[k];
-          io.odx[i] = dx[k];
-          io.ody[i] = dy[k];
-          if (io.opl) io.opl[i] = M.pl_const + (double)pl[k];
+          const int i = idx[k];
+          ox[i] = x[k];
+          oy[i] = y[k];
+          odx[i] = dx[k];
+          ody[i] = dy[k];
+          if (opl) opl[i] = M.pl_const + (double)pl[k];
         }
       }
       if (!adj) continue;
