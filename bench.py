@@ -185,6 +185,16 @@ def cpu_baseline(sample_probes=SCAN[0] * SCAN[1]):
                       "restatement of run_to_end + metres_to_pixels + into_image per probe, 1 thread"}
 
 
+def headline_config(world: int) -> dict:
+    """The headline workload (both arms print this config)."""
+    return {"workload": "4D-STEM shadow images: 64x64 scan (step 1e-9 m, rotation "
+                        "U(0,2pi)), 1024-ray point-source bundle per probe, descan I+N(0,1e-3), "
+                        "camera length 0.1 m, 256x256 int32 images at 5.5e-5 m",
+            "rays_per_step": SCAN[0] * SCAN[1] * RAYS, "components": N_COMPONENTS,
+            "l2": "no flush: 1.07 GB of images written per step > 129 MB L2",
+            "parallelism": f"dp{world} (independent scans per rank)"}
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return
@@ -211,8 +221,7 @@ def run_reference(args, world, rank):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded), no dataset",
-            "config": {"workload": "4D-STEM shadow images, 64x64 scan x 1024 rays, 256x256 detector",
-                       "sample_per_step": f"{per_step} probes"},
+            "config": headline_config(1),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": f"{per_step} of 4096 probes per step, {cores} spawn workers"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -689,12 +698,7 @@ def run_gpu(args, world, rank, local):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 rays / f64 binning ties", "data": "synthetic (seeded)",
-            "config": {"workload": "4D-STEM shadow images: 64x64 scan (step 1e-9 m, rotation "
-                                   "U(0,2pi)), 1024-ray point-source bundle per probe, descan I+N(0,1e-3), "
-                                   "camera length 0.1 m, 256x256 int32 images at 5.5e-5 m",
-                       "rays_per_step": n_probes * RAYS, "components": N_COMPONENTS,
-                       "l2": "no flush: 1.07 GB of images written per step > 129 MB L2",
-                       "parallelism": f"dp{world} (independent scans per rank)"},
+            "config": headline_config(world),
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps,
             "clocks": clk.summary(), "error_word": err, "secondary": secondary}
     if rank == 0:
