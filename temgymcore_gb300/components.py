@@ -163,11 +163,19 @@ class Grid:
                                           self.flip_y, _f(self.rotation))
 
     def _tg_grid(self) -> N.TgGrid:
+        # grids are frozen dataclasses: the C struct is built once per instance
+        # (tensor-valued fields are read each time: they may change in place)
+        cached = self.__dict__.get("_tg_grid_cache")
+        if cached is not None:
+            return cached
         m = self.metres_to_pixels_mat
         g = N.TgGrid()
         g.h, g.w = int(self.shape[0]), int(self.shape[1])
         for i, v in enumerate((m[0, 0], m[0, 1], m[0, 2], m[1, 0], m[1, 1], m[1, 2])):
             g.m[i] = float(v)
+        fields = (self.pixel_size, self.shape, self.rotation, self.centre)
+        if not any(isinstance(f, torch.Tensor) for f in fields):
+            object.__setattr__(self, "_tg_grid_cache", g)
         return g
 
     @property

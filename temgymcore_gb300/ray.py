@@ -50,10 +50,15 @@ class Ray:
     @property
     def size(self) -> int:
         """ray.py:59-77 (asserts equal field sizes)."""
+        cached = self.__dict__.get("_size_cache")  # fields are frozen: computed once
+        if cached is not None:
+            return cached
         sizes = {_size(getattr(self, f.name)) for f in dataclasses.fields(self)
                  if _is_vec(getattr(self, f.name))}
         assert len(sizes) <= 1, "ray fields have mismatched sizes"
-        return sizes.pop() if sizes else 1
+        n = sizes.pop() if sizes else 1
+        object.__setattr__(self, "_size_cache", n)
+        return n
 
     def __getitem__(self, arg):
         """ray.py:79-96."""
@@ -139,6 +144,9 @@ def _dev():
 
 def as_f32(v, n: int, device) -> torch.Tensor:
     """Contiguous float32 device vector of length n (broadcasting scalars)."""
+    if (isinstance(v, torch.Tensor) and v.dtype == torch.float32 and v.dim() == 1 and v.is_cuda
+            and v.numel() == n and v.is_contiguous() and v.device == device):
+        return v  # already in the kernel layout (only its address is used)
     if isinstance(v, torch.Tensor):
         t = v.detach().to(device=device, dtype=torch.float32).reshape(-1)
     else:

@@ -100,10 +100,8 @@ def _ray_scalar_input(ray: Ray) -> bool:
 def _fwd_launch(model, soa: _Soa, grid=None, want_pix=False, hist=None, want_amp=False, propagator=None):
     dev = soa.x.device
     n = soa.n
-    ox = torch.empty(n, dtype=torch.float32, device=dev)
-    oy = torch.empty_like(ox)
-    odx = torch.empty_like(ox)
-    ody = torch.empty_like(ox)
+    o4 = torch.empty((4, n), dtype=torch.float32, device=dev)  # one allocation, four views
+    ox, oy, odx, ody = o4[0], o4[1], o4[2], o4[3]
     opl = torch.empty(n, dtype=torch.float64, device=dev)
     oamp = torch.empty(n, dtype=torch.float32, device=dev) if (want_amp or soa.amp is not None) else None
     m, keep = pack_model(model, propagator)
@@ -289,9 +287,8 @@ def run_to_end(ray: Ray, components: Sequence[Component],
         zout = spec["zout"]
     else:
         ox, oy, odx, ody, opl, zout, _, _, _ = _fwd_launch(comps, soa, propagator=propagator)
-    out = Ray(x=ox.reshape(shape), y=oy.reshape(shape), dx=odx.reshape(shape),
-              dy=ody.reshape(shape), z=zout, pathlength=opl.reshape(shape),
-              _one=ray._one)
+    rs = _reshaper(shape, soa.n)
+    out = Ray(x=rs(ox), y=rs(oy), dx=rs(odx), dy=rs(ody), z=zout, pathlength=rs(opl), _one=ray._one)
     return out
 
 
@@ -426,11 +423,18 @@ def trace_to_image(ray: Ray, components: Sequence[Component], detector: Grid | N
         acc = torch.zeros((h, w), dtype=torch.int64, device=dev)
     ox, oy, odx, ody, opl, zout, oamp, py, px = _fwd_launch(comps, soa, detector, want_pixels, acc)
     shape = _in_shape(ray)
-    out = Ray(x=ox.reshape(shape), y=oy.reshape(shape), dx=odx.reshape(shape),
-              dy=ody.reshape(shape), z=zout, pathlength=opl.reshape(shape), _one=ray._one)
+    rs = _reshaper(shape, soa.n)
+    out = Ray(x=rs(ox), y=rs(oy), dx=rs(odx), dy=rs(ody), z=zout, pathlength=rs(opl), _one=ray._one)
     from . import PixelsYX
-    pix = PixelsYX(y=py.reshape(shape), x=px.reshape(shape)) if want_pixels else None
+    pix = PixelsYX(y=rs(py), x=rs(px)) if want_pixels else None
     return out, pix, acc
+
+
+def _reshaper(shape, n):
+    """Reshape to the input's shape, skipping the no-op case (vector input)."""
+    if shape == (n,):
+        return lambda t: t
+    return lambda t: t.reshape(shape)
 
 
 class TracePlan:
