@@ -124,6 +124,9 @@ const char *tg_status_string(int status);
  * synchronises the device. */
 int tg_get_error_word(uint32_t *out, int clear);
 
+/* Read and clear the device error word (0xffffffff if it could not be read). */
+uint32_t tg_get_last_error_word(void);
+
 /* ---- ray chain -------------------------------------------------------- */
 /*
  * tg_trace_fwd - fused forward trace (+ optional pixel binning + histogram).
@@ -177,6 +180,20 @@ int tg_abcd_compose(const tg_model *model, const double central[5],
  *   workspace: device scratch of tg_trace_vjp_workspace(n) bytes.
  */
 size_t tg_trace_vjp_workspace(int64_t n, const tg_model *model);
+
+/*
+ * tg_trace_adj - gradient of loss = sum_i |(x, y)_out,i - target_i|^2 for
+ * one model in one call (forward, residual, adjoint): the reference's
+ * jax.grad of a squared detector-position loss over run_to_end
+ * (README.md:113-160).  target_x/y: device float32 [n].  dparams: device
+ * float64 [2*n_components][4], OVERWRITTEN with the per-step sums of
+ * tg_trace_vjp.  dray (may be NULL): gradients w.r.t. the input rays.
+ * workspace: device, tg_trace_adj_workspace(n, model) bytes, 256-byte aligned.
+ */
+size_t tg_trace_adj_workspace(int64_t n, const tg_model *model);
+int tg_trace_adj(const tg_model *model, const tg_rays *in, const float *target_x,
+                 const float *target_y, double *dparams, tg_rays *dray, void *workspace,
+                 size_t ws_bytes, void *stream);
 int tg_trace_vjp(const tg_model *model, const tg_rays *in, const tg_rays *gout,
                  tg_rays *gin, double *raw, void *workspace, size_t ws_bytes,
                  void *stream);
@@ -426,6 +443,13 @@ int tg_field_prep_input(const tg_beams *beams, const tg_pixel_map *pm, void *wor
  */
 int tg_field_eval(int32_t method, int64_t n_beams, const tg_pixel_map *pm, float *out,
                   void *workspace, size_t ws_bytes, void *stream);
+
+/* tg_field_prep + tg_field_eval(TG_FIELD_DIRECT / TG_FIELD_SEPARABLE) in one
+ * call; workspace as for tg_field_eval with that method. */
+int tg_field_direct(const tg_model *model, const tg_beams *beams, const tg_pixel_map *pm,
+                    float *out, void *workspace, size_t ws_bytes, void *stream);
+int tg_field_separable(const tg_model *model, const tg_beams *beams, const tg_pixel_map *pm,
+                       float *out, void *workspace, size_t ws_bytes, void *stream);
 
 /*
  * tg_field_direct_noalloc - tg_field_prep + tg_field_eval(TG_FIELD_DIRECT)

@@ -932,3 +932,21 @@ extern "C" int tg_field_direct_noalloc(const tg_model* model, const tg_beams* be
   k_field_reduce<<<(int)((npx + 255) / 256), 256, 0, s>>>(A.out, used, npx, o);
   return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
 }
+
+// ------------------------------------------- one-call field entry points
+// tg_field_prep followed by tg_field_eval with a fixed method, for callers
+// that want the detector field in one call (the caller's workspace holds
+// the records and partials: tg_field_workspace(n, h, w, method) bytes).
+extern "C" int tg_field_direct(const tg_model* model, const tg_beams* beams, const tg_pixel_map* pm,
+                               float* out, void* workspace, size_t ws_bytes, void* stream) {
+  int st = tg_field_prep(model, beams, pm, workspace, ws_bytes, nullptr, stream);
+  if (st != TG_OK) return st;
+  return tg_field_eval(TG_FIELD_DIRECT, beams->n, pm, out, workspace, ws_bytes, stream);
+}
+
+extern "C" int tg_field_separable(const tg_model* model, const tg_beams* beams, const tg_pixel_map* pm,
+                                  float* out, void* workspace, size_t ws_bytes, void* stream) {
+  int st = tg_field_prep(model, beams, pm, workspace, ws_bytes, nullptr, stream);
+  if (st != TG_OK) return st;
+  return tg_field_eval(TG_FIELD_SEPARABLE, beams->n, pm, out, workspace, ws_bytes, stream);
+}

@@ -335,6 +335,13 @@ extern "C" int tg_internal_err_gemm(uint32_t*, int);
 extern "C" int tg_internal_err_fit(uint32_t*, int);
 extern "C" int tg_internal_err_batch(uint32_t*, int);
 
+extern "C" int tg_get_error_word(uint32_t* out, int clear);
+
+extern "C" uint32_t tg_get_last_error_word(void) {
+  uint32_t v = 0;
+  return tg_get_error_word(&v, 1) == TG_OK ? v : 0xffffffffu;
+}
+
 extern "C" int tg_get_error_word(uint32_t* out, int clear) {
   if (!out) return TG_ERR_INVALID;
   if (cudaDeviceSynchronize() != cudaSuccess) return TG_ERR_CUDA;

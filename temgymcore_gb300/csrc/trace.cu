@@ -475,3 +475,66 @@ extern "C" int tg_trace_vjp(const tg_model* model, const tg_rays* in, const tg_r
   }
   return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
 }
+
+// ------------------------------------------------------- tg_trace_adj
+// Gradient of loss = sum_i |(x, y)_out,i - target_i|^2 for one model in one
+// call: forward trace into the workspace, upstream gradient 2 (out - target),
+// then the adjoint.  Workspace layout (256-byte aligned pieces): x, y, dx, dy
+// outputs (float32 [4][n]), upstream x, y, zero dx, dy (float32 [4][n]), the
+// adjoint's partial sums.
+namespace tg {
+
+__global__ void k_residual_grad(int64_t n, const float* __restrict__ ox, const float* __restrict__ oy,
+                                const float* __restrict__ tx, const float* __restrict__ ty,
+                                float* __restrict__ gx, float* __restrict__ gy, float* __restrict__ gdx,
+                                float* __restrict__ gdy) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    gx[i] = 2.f * (ox[i] - tx[i]);
+    gy[i] = 2.f * (oy[i] - ty[i]);
+    gdx[i] = 0.f;
+    gdy[i] = 0.f;
+  }
+}
+
+static inline size_t al256t(size_t v) { return (v + 255) & ~(size_t)255; }
+
+}  // namespace tg
+
+extern "C" size_t tg_trace_adj_workspace(int64_t n, const tg_model* model) {
+  if (!model || n < 0) return 0;
+  const size_t vec = al256t((size_t)n * sizeof(float));
+  return 8 * vec + al256t(tg_trace_vjp_workspace(n, model));
+}
+
+extern "C" int tg_trace_adj(const tg_model* model, const tg_rays* in, const float* target_x,
+                            const float* target_y, double* dparams, tg_rays* dray, void* workspace,
+                            size_t ws_bytes, void* stream) {
+  if (!model || !in || !dparams) return TG_ERR_INVALID;
+  if (in->n < 0 || (in->n > 0 && (!target_x || !target_y))) return TG_ERR_INVALID;
+  const int64_t n = in->n;
+  const size_t need = tg_trace_adj_workspace(n, model);
+  if (!workspace || ws_bytes < need) return TG_ERR_WORKSPACE;
+  if (((uintptr_t)workspace & 255) != 0) return TG_ERR_ALIGN;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  const size_t steps = (size_t)(2 * model->n_components);
+  if (cudaMemsetAsync(dparams, 0, steps * 4 * sizeof(double), s) != cudaSuccess) return TG_ERR_CUDA;
+  if (n == 0) return TG_OK;
+  char* ws = reinterpret_cast<char*>(workspace);
+  const size_t vec = al256t((size_t)n * sizeof(float));
+  float* v[8];
+  for (int i = 0; i < 8; ++i) v[i] = reinterpret_cast<float*>(ws + i * vec);
+  tg_rays out;
+  std::memset(&out, 0, sizeof(out));
+  out.n = n;
+  out.x = v[0]; out.y = v[1]; out.dx = v[2]; out.dy = v[3];
+  int st = tg_trace_fwd(model, in, &out, nullptr, nullptr, nullptr, nullptr, nullptr, 0, stream);
+  if (st != TG_OK) return st;
+  int blocks = (int)((n + 255) / 256);
+  if (blocks > 4096) blocks = 4096;
+  k_residual_grad<<<blocks, 256, 0, s>>>(n, v[0], v[1], target_x, target_y, v[4], v[5], v[6], v[7]);
+  tg_rays gout;
+  std::memset(&gout, 0, sizeof(gout));
+  gout.n = n;
+  gout.x = v[4]; gout.y = v[5]; gout.dx = v[6]; gout.dy = v[7];
+  return tg_trace_vjp(model, in, &gout, dray, dparams, ws + 8 * vec, ws_bytes - 8 * vec, stream);
+}

@@ -145,3 +145,31 @@ def test_full_config_properties(cuda):
     assert e2 < 1e-7, e2
     dire = _np(plan.evaluate("direct").clone()).reshape(-1)[idx]
     assert np.max(np.abs(dire - ref)) / np.max(np.abs(ref)) < 1e-4
+
+
+def test_one_call_field_entry_points(cuda):
+    """tg_field_direct / tg_field_separable (prep + eval in one call) equal the
+    two-call FieldPlan results."""
+    import ctypes as C
+    import temgymcore_gb300 as t
+    from temgymcore_gb300 import _native as N
+    from temgymcore_gb300.gaussian import BeamSet, TgBeams, TgPixelMap, pixel_map
+    from temgymcore_gb300.run import pack_model
+    from temgymcore_gb300.workloads import build_model, gaussian_rays
+    for name in ("tg_field_direct", "tg_field_separable"):
+        N.register(name, C.c_int, [C.POINTER(N.TgModel), C.POINTER(TgBeams), C.POINTER(TgPixelMap), C.c_void_p,
+                                   C.c_void_p, C.c_size_t, C.c_void_p])
+    w = _small(False)
+    model = build_model(w["model"])
+    plan = t.FieldPlan(gaussian_rays(w["rays"]), model)
+    beams = BeamSet(gaussian_rays(w["rays"]), cuda)
+    pm = pixel_map(model[-1])
+    m, keep = pack_model(model)
+    for name, meth in (("tg_field_direct", "direct"), ("tg_field_separable", "separable")):
+        out = torch.empty(plan.shape, dtype=torch.complex64, device=cuda)
+        N.check(getattr(N.lib(), name)(C.byref(m), C.byref(beams.struct()), C.byref(pm),
+                                       torch.view_as_real(out).data_ptr(), plan.ws_ptr, plan.ws_bytes,
+                                       N.stream_ptr()))
+        ref = plan.evaluate(meth).clone()
+        torch.cuda.synchronize()
+        assert torch.equal(out, ref), name

@@ -316,3 +316,51 @@ def test_trace_plan_and_graph_match_api(cuda):
     g.replay()
     torch.cuda.synchronize()
     assert torch.equal(plan.image, 2 * img)
+
+
+def test_trace_adj_one_call_matches_composition(cuda):
+    """tg_trace_adj (forward + residual + adjoint in one call) equals
+    tg_trace_fwd, 2 (out - target) and tg_trace_vjp done separately."""
+    import ctypes as C
+    from temgymcore_gb300 import _native as N
+    from temgymcore_gb300.run import _rays_struct, pack_model
+    from temgymcore_gb300.workloads import build_model
+    N.register("tg_trace_adj_workspace", C.c_size_t, [C.c_int64, C.POINTER(N.TgModel)])
+    N.register("tg_trace_adj", C.c_int, [C.POINTER(N.TgModel), C.POINTER(N.TgRays), C.c_void_p, C.c_void_p,
+                                         C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p])
+    N.register("tg_get_last_error_word", C.c_uint32, [])
+    t = T()
+    rng = np.random.default_rng(4)
+    n = 5003
+    w = {k: torch.tensor(rng.normal(0, s, n).astype(np.float32), device=cuda)
+         for k, s in (("x", 1e-4), ("y", 1e-4), ("dx", 1e-3), ("dy", 1e-3))}
+    tx, ty = (torch.tensor(rng.normal(0, 1e-4, n).astype(np.float32), device=cuda) for _ in range(2))
+    m, keep = pack_model(build_model(_full_chain_spec()))
+    ns = 2 * m.n_components
+    rin = _rays_struct(n, w["x"], w["y"], w["dx"], w["dy"], None, 0.0, None, 0.0)
+    ws = torch.empty(N.lib().tg_trace_adj_workspace(n, C.byref(m)) + 256, dtype=torch.uint8, device=cuda)
+    wp = ws.data_ptr() + (-ws.data_ptr()) % 256
+    dpar = torch.full((ns, 4), 7.0, dtype=torch.float64, device=cuda)
+    g = [torch.empty(n, device=cuda) for _ in range(4)]
+    gin = _rays_struct(n, *g, None, 0.0, None, 0.0)
+    N.check(N.lib().tg_trace_adj(C.byref(m), C.byref(rin), tx.data_ptr(), ty.data_ptr(), dpar.data_ptr(),
+                                 C.byref(gin), wp, ws.numel() - 256, N.stream_ptr()))
+    # composition
+    o = [torch.empty(n, device=cuda) for _ in range(4)]
+    rout = _rays_struct(n, *o, None, 0.0, None, 0.0)
+    N.check(N.lib().tg_trace_fwd(C.byref(m), C.byref(rin), C.byref(rout), None, None, None, None, None, 0,
+                                 N.stream_ptr()))
+    gx, gy = 2 * (o[0] - tx), 2 * (o[1] - ty)
+    z = torch.zeros(n, device=cuda)
+    gout = _rays_struct(n, gx.contiguous(), gy.contiguous(), z, z, None, 0.0, None, 0.0)
+    raw = torch.zeros((ns, 4), dtype=torch.float64, device=cuda)
+    g2 = [torch.empty(n, device=cuda) for _ in range(4)]
+    gin2 = _rays_struct(n, *g2, None, 0.0, None, 0.0)
+    ws2 = torch.empty(max(8, N.lib().tg_trace_vjp_workspace(n, C.byref(m))), dtype=torch.uint8, device=cuda)
+    N.check(N.lib().tg_trace_vjp(C.byref(m), C.byref(rin), C.byref(gout), C.byref(gin2), raw.data_ptr(),
+                                 ws2.data_ptr(), ws2.numel(), N.stream_ptr()))
+    torch.cuda.synchronize()
+    assert normwise_err(np_(dpar), np_(raw)) < 1e-6
+    for a, b in zip(g, g2):
+        assert normwise_err(np_(a), np_(b)) < 1e-6
+    assert N.lib().tg_get_last_error_word() == 0
