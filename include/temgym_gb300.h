@@ -338,6 +338,19 @@ int tg_batch_run(const void *plan_dev, const tg_batch_info *info, const tg_batch
                  int32_t block, int32_t rays_per_thread, void *workspace, size_t ws_bytes,
                  void *stream);
 
+/*
+ * tg_batched_trace - tg_batch_plan + tg_batch_run in one call: the plan is
+ * built on the host, copied into the front of the caller's device workspace
+ * (tg_batched_trace_workspace bytes, 256-byte aligned; the call synchronises
+ * the stream after that copy, so it is not for graph capture) and run with
+ * tiles of 4,096 rays, 256 threads x 2 rays.
+ */
+size_t tg_batched_trace_workspace(int32_t n_models, const tg_model *models, const int64_t *n_rays,
+                                  const double *z_in);
+int tg_batched_trace(int32_t n_models, const tg_model *models, const int64_t *n_rays,
+                     const double *z_in, const tg_batch_io *io, void *workspace, size_t ws_bytes,
+                     void *stream);
+
 /* ---- 4D-STEM calibration fit (device-resident parameters) -------------- */
 /* Model: bundle at z = 0 -> Scanner + Descanner at z = defocus with the
  * probe's scan position (ScanGrid of rows x cols, centre 0) -> Lens(f) at

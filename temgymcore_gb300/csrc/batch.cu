@@ -639,3 +639,39 @@ extern "C" int tg_batch_run(const void* plan_dev, const tg_batch_info* info, con
   else k_batch<4><<<grid, block, dyn, s>>>(plan, A, counter, done, partial, moments);
   return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
 }
+
+// One call for callers that do not keep a plan: pack the models on the host,
+// copy the plan into the front of the caller's workspace (a synchronous
+// staging copy from pageable memory, so this entry point is not for graph
+// capture: tg_batch_plan + tg_batch_run are) and run with the launch shape
+// measured best on GB300 (tiles of 4,096 rays, 256 threads x 2 rays).
+namespace tg {
+constexpr int32_t kDefTile = 4096, kDefBlock = 256, kDefRpt = 2;
+}
+
+extern "C" size_t tg_batched_trace_workspace(int32_t n_models, const tg_model* models,
+                                             const int64_t* n_rays, const double* z_in) {
+  tg_batch_info info;
+  if (tg_batch_plan(n_models, models, n_rays, z_in, kDefTile, nullptr, 0, &info) != TG_OK) return 0;
+  return (size_t)al256((int64_t)info.plan_bytes) + info.workspace_bytes;
+}
+
+extern "C" int tg_batched_trace(int32_t n_models, const tg_model* models, const int64_t* n_rays,
+                                const double* z_in, const tg_batch_io* io, void* workspace,
+                                size_t ws_bytes, void* stream) {
+  tg_batch_info info;
+  int st = tg_batch_plan(n_models, models, n_rays, z_in, kDefTile, nullptr, 0, &info);
+  if (st != TG_OK) return st;
+  const size_t head = (size_t)al256((int64_t)info.plan_bytes);
+  if (!workspace || ws_bytes < head + info.workspace_bytes) return TG_ERR_WORKSPACE;
+  if (((uintptr_t)workspace & 255) != 0) return TG_ERR_ALIGN;
+  std::vector<uint8_t> host(info.plan_bytes);
+  st = tg_batch_plan(n_models, models, n_rays, z_in, kDefTile, host.data(), host.size(), &info);
+  if (st != TG_OK) return st;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (cudaMemcpyAsync(workspace, host.data(), host.size(), cudaMemcpyHostToDevice, s) != cudaSuccess)
+    return TG_ERR_CUDA;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return TG_ERR_CUDA;  // the host plan goes out of scope
+  return tg_batch_run(workspace, &info, io, kDefBlock, kDefRpt, reinterpret_cast<uint8_t*>(workspace) + head,
+                      ws_bytes - head, stream);
+}

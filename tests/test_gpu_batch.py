@@ -95,3 +95,34 @@ def test_batched_graph_and_autotune(cuda):
     torch.cuda.synchronize()
     assert torch.equal(out[0], ref_x)
     assert torch.equal(raw, ref_raw)  # per-tile partials reduced in fixed order
+
+
+def test_one_call_batched_trace(cuda):
+    """tg_batched_trace (plan + run in one call) equals BatchedTrace.run."""
+    import ctypes as C
+    from temgymcore_gb300 import _native as N
+    from temgymcore_gb300.batched import BatchedTrace, TgBatchIO
+    from temgymcore_gb300.workloads import build_model
+    N.register("tg_batched_trace_workspace", C.c_size_t, [C.c_int32, C.POINTER(N.TgModel), C.POINTER(C.c_int64),
+                                                          C.POINTER(C.c_double)])
+    N.register("tg_batched_trace", C.c_int, [C.c_int32, C.POINTER(N.TgModel), C.POINTER(C.c_int64),
+                                             C.POINTER(C.c_double), C.POINTER(TgBatchIO), C.c_void_p, C.c_size_t,
+                                             C.c_void_p])
+    w = _small(cuda, seed=3)
+    models = [build_model(s) for s in w["specs"]]
+    bt = BatchedTrace(models, w["counts"], tile_rays=4096)
+    x, y, dx, dy, tx, ty = (torch.tensor(w[k], device=cuda) for k in ("x", "y", "dx", "dy", "tx", "ty"))
+    out, raw = bt.alloc_outputs(), bt.alloc_raw()
+    bt.run(x, y, dx, dy, out, (tx, ty), raw, 256, 2)
+    out2, raw2 = bt.alloc_outputs(), bt.alloc_raw()
+    io = bt.io(x, y, dx, dy, out2, (tx, ty), raw2)
+    cnt = (C.c_int64 * len(models))(*[int(v) for v in w["counts"]])
+    nb = N.lib().tg_batched_trace_workspace(len(models), bt._arr, cnt, None)
+    assert nb > 0
+    ws = torch.empty(nb + 256, dtype=torch.uint8, device=cuda)
+    wp = ws.data_ptr() + (-ws.data_ptr()) % 256
+    N.check(N.lib().tg_batched_trace(len(models), bt._arr, cnt, None, C.byref(io), wp, nb, N.stream_ptr()))
+    torch.cuda.synchronize()
+    for a, b in zip(out, out2):
+        assert torch.equal(a, b)
+    assert torch.equal(raw, raw2)
