@@ -27,6 +27,7 @@ namespace tg {
 
 constexpr int kFitThreads = 256;
 constexpr int kFitOut = 22;  // loss + 21 gradients
+constexpr int kRedChunks = 8;  // probe chunks per output in the reduction
 
 struct FitArgs {
   int32_t n, rows, cols, n_probes;
@@ -39,6 +40,9 @@ struct FitArgs {
   double2* sp;           // [n_probes] scan position (x, y)
   float* fpar;           // [4] D, Lp, 1/f, gap (float32 copies)
   double* psum;          // [n_probes][8] per-probe sums
+  double2* rot;          // [1] cos, sin of the scan rotation (written by k_fit_setup)
+  double* part;          // [kFitOut][kRedChunks] reduction partials
+  int32_t* cnt;          // [kFitOut] chunks counted per output (zeroed by k_fit_setup)
   int32_t forward_only;
 };
 
@@ -58,12 +62,14 @@ __global__ void __launch_bounds__(256) k_fit_setup(const __grid_constant__ FitAr
     cs[0] = cr;
     cs[1] = sr;
     if (blockIdx.x == 0) {
+      A.rot[0] = make_double2(cr, sr);
       A.fpar[0] = (float)A.theta[1];
       A.fpar[1] = (float)(A.theta[2] - A.gap);
       A.fpar[2] = (float)(1.0 / A.theta[0]);
       A.fpar[3] = (float)A.gap;
     }
   }
+  if (blockIdx.x == 0 && threadIdx.x < kFitOut) A.cnt[threadIdx.x] = 0;
   __syncthreads();
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= A.n_probes) return;
@@ -131,24 +137,23 @@ __global__ void __launch_bounds__(kFitThreads) k_stem_fit(const __grid_constant_
 }
 
 // out[j] for j = blockIdx.x: loss (j = 0) or dL/dtheta[j-1], from the
-// per-probe sums through the scan-geometry chain rule (float64), block tree
-// reduction in a fixed order.
-__global__ void __launch_bounds__(256) k_fit_reduce(const __grid_constant__ FitArgs A, double* __restrict__ out) {
-  __shared__ double red[256];
-  __shared__ double cs[2];
-  const int j = blockIdx.x;
-  if (threadIdx.x == 0) {
-    double sr, cr;
-    sincos(A.theta[3] * (3.141592653589793 / 180.0), &sr, &cr);
-    cs[0] = cr;
-    cs[1] = sr;
-  }
-  __syncthreads();
-  const double cr = cs[0], sr = cs[1], step = A.theta[4];
+// per-probe sums through the scan-geometry chain rule (float64).  Each of
+// the kRedChunks blocks of an output (blockIdx.y) reduces one chunk of probes
+// with a fixed-order tree; the block that counts an output's last chunk adds
+// the chunk partials in chunk order (deterministic).  Spreading the float64
+// work over kFitOut x kRedChunks blocks matters on GB300, whose float64 rate
+// is ~1/64 of float32.
+__global__ void __launch_bounds__(128) k_fit_reduce(const __grid_constant__ FitArgs A, double* __restrict__ out) {
+  __shared__ double red[128];
+  __shared__ int s_last;
+  const int j = blockIdx.x, chunk = blockIdx.y;
+  const double cr = A.rot[0].x, sr = A.rot[0].y, step = A.theta[4];
   const double* M = A.theta + 5;
   const double kdeg = 3.141592653589793 / 180.0;
+  const int per = (A.n_probes + kRedChunks - 1) / kRedChunks;
+  const int p0 = chunk * per, p1 = (p0 + per) < A.n_probes ? (p0 + per) : A.n_probes;
   double acc = 0.0;
-  for (int p = threadIdx.x; p < A.n_probes; p += blockDim.x) {
+  for (int p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
     const double* t = A.psum + (size_t)p * 8;
     double c = 0.0;
     if (j == 0) c = t[0];
@@ -176,7 +181,18 @@ __global__ void __launch_bounds__(256) k_fit_reduce(const __grid_constant__ FitA
     if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
     __syncthreads();
   }
-  if (threadIdx.x == 0) out[j] = red[0];
+  if (threadIdx.x == 0) {
+    A.part[j * kRedChunks + chunk] = red[0];
+    __threadfence();
+    s_last = atomicAdd(A.cnt + j, 1) == kRedChunks - 1;
+  }
+  __syncthreads();
+  if (s_last && threadIdx.x == 0) {
+    __threadfence();
+    double t = 0.0;
+    for (int c = 0; c < kRedChunks; ++c) t += __ldcg(A.part + j * kRedChunks + c);
+    out[j] = t;
+  }
 }
 
 // Adam on float64 parameters; the step counter lives on the device so the
@@ -216,9 +232,10 @@ static int fit_grid(int n_probes) {
   return g < n_probes ? g : (n_probes > 0 ? n_probes : 1);
 }
 
-// workspace: shift [n_probes] float4 | sp [n_probes] double2 | psum [n_probes][8] | fpar[4]
+// workspace: shift [n_probes] float4 | sp [n_probes] double2 | psum [n_probes][8] |
+// fpar[4] + rot (256 B) | part [kFitOut][kRedChunks] | cnt [kFitOut] (256 B)
 static size_t fit_ws(int32_t n_probes) {
-  return (size_t)n_probes * (16 + 16 + 64) + 256;
+  return (size_t)n_probes * (16 + 16 + 64) + 256 + kFitOut * kRedChunks * sizeof(double) + 256;
 }
 
 }  // namespace tg
@@ -251,6 +268,9 @@ static int fit_args(const tg_stem_fit* c, const double* theta, void* ws, size_t 
   A->sp = reinterpret_cast<double2*>(w + (size_t)A->n_probes * 16);
   A->psum = reinterpret_cast<double*>(w + (size_t)A->n_probes * 32);
   A->fpar = reinterpret_cast<float*>(w + (size_t)A->n_probes * 96);
+  A->rot = reinterpret_cast<double2*>(w + (size_t)A->n_probes * 96 + 16);
+  A->part = reinterpret_cast<double*>(w + (size_t)A->n_probes * 96 + 256);
+  A->cnt = reinterpret_cast<int32_t*>(w + (size_t)A->n_probes * 96 + 256 + kFitOut * kRedChunks * sizeof(double));
   return TG_OK;
 }
 
@@ -278,7 +298,7 @@ extern "C" int tg_stem_fit_loss_grad(const tg_stem_fit* cfg, const double* theta
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   k_fit_setup<<<(A.n_probes + 255) / 256, 256, 0, s>>>(A);
   k_stem_fit<<<fit_grid(A.n_probes), kFitThreads, 0, s>>>(A);
-  k_fit_reduce<<<kFitOut, 256, 0, s>>>(A, out);
+  k_fit_reduce<<<dim3(kFitOut, kRedChunks), 128, 0, s>>>(A, out);
   return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
 }
 
