@@ -70,7 +70,7 @@ from .propagator import FreeSpaceParaxial, FreeSpaceDirCosine, Propagator, BaseP
 from .run import (  # noqa: E402,F401
     run_to_end, run_iter, solve_model, abcd_matrix, trace_to_image, pack_model, TracePlan,
 )
-from .scan import scan_images, scan_positions, probe_model  # noqa: E402,F401
+from .scan import scan_images, scan_positions, scan_shard, probe_model  # noqa: E402,F401
 from .gaussian import (  # noqa: E402,F401
     make_gaussian_image, evaluate_gaussian_input_image, FieldPlan, fibonacci_spiral, decompose_Q_inv)
 from .sources import concentric_rings, random_coords  # noqa: E402,F401

@@ -69,6 +69,21 @@ def scan_positions(scan_grid: ScanGrid) -> np.ndarray:
     return np.stack([x, y], axis=-1)
 
 
+def scan_shard(scan_grid: ScanGrid, rank: int, world: int):
+    """Probe range and positions of one rank when a scan is split over
+    ``world`` GPUs: contiguous row-major probe ranges whose sizes differ by at
+    most one.  The probes are independent, so the ranks need no exchange; the
+    images of rank r are probes [start, stop) of the full scan.
+    Returns (start, stop, positions (stop - start, 2))."""
+    if world < 1 or not 0 <= rank < world:
+        raise ValueError("rank must satisfy 0 <= rank < world")
+    n = int(scan_grid.shape[0]) * int(scan_grid.shape[1])
+    base, extra = divmod(n, world)
+    start = rank * base + min(rank, extra)
+    stop = start + base + (1 if rank < extra else 0)
+    return start, stop, scan_positions(scan_grid)[start:stop]
+
+
 def scan_images(ray: Ray, model, scan_grid: ScanGrid | None = None, detector: Grid | None = None,
                 positions=None, out: torch.Tensor | None = None, return_xy: bool = False):
     """Dense int32 images (n_probes, H, W): the bundle ``ray`` traced through
