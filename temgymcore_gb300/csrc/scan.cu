@@ -73,11 +73,11 @@ __device__ __forceinline__ void trace_one(const Program& P, const float4* pshift
                                           float y, float dx, float dy, double z, RayS& r,
                                           bool& alive) {
   r = RayS{x, y, dx, dy, 0.f};
-  double dvar = 0.0;
   uint64_t sb = 0;
   alive = true;
+  (void)z;  // the bundle starts from one plane: no per-ray first distance
   for (int s = 0; s < P.n_steps; ++s)
-    op_forward(P.op[s], pshift, r, P.zc_first, z, dvar, sb, alive, &P.aber[0][0]);
+    op_forward(P.op[s], pshift, r, 0.f, sb, alive, &P.aber[0][0]);
 }
 
 __device__ __forceinline__ int block_min(int v, int* red) {

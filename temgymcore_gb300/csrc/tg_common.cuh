@@ -153,6 +153,19 @@ __device__ __forceinline__ void hist_add_warp(CountT* hist, int bin, bool valid)
   }
 }
 
+// Exact float -> double conversion with integer operations (the hardware
+// conversion issues on the float64 pipe, ~1/64 of the float32 rate on GB300):
+// normal numbers rebias the exponent and widen the mantissa; zeros, denormals,
+// infinities and NaNs take the hardware conversion.
+__device__ __forceinline__ double f32_to_f64(float v) {
+  const uint32_t b = __float_as_uint(v);
+  const uint32_t e = (b >> 23) & 0xffu;
+  if (e == 0u || e == 0xffu) return (double)v;
+  const uint64_t d = ((uint64_t)(b >> 31) << 63) | ((uint64_t)(e + (1023u - 127u)) << 52) |
+                     ((uint64_t)(b & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)d);
+}
+
 // ---------------------------------------------------------------- ray ops
 struct RayS {
   float x, y, dx, dy, plv;  // plv: per-ray (varying) pathlength part
@@ -172,26 +185,20 @@ __device__ __forceinline__ void aber_forward(const float* a, float k1, float h, 
   r.dy = fmaf(-Wy, k1, uy);
 }
 
-// Apply one forward step.  zi is the ray's input z (OP_FREE_VARZ only);
-// pshift holds the current probe's shifts (OP_PROBE_SHIFT only); aber the
-// Program's aberration polynomials (OP_ABER only, may be NULL otherwise);
-// dvar receives that per-ray float64 distance.  sbits records biprism signs
-// (2 bits per biprism: 1 = +, 2 = -) and alive is cleared by apertures.
+// Apply one forward step.  dvar is the ray's own first distance (OP_FREE_VARZ
+// only: component z minus the ray's z, formed in float64 by the caller once
+// per ray, outside the step loop); pshift holds the current probe's shifts
+// (OP_PROBE_SHIFT only); aber the Program's aberration polynomials (OP_ABER
+// only, may be NULL otherwise).  sbits records biprism signs (2 bits per
+// biprism: 1 = +, 2 = -) and alive is cleared by apertures.  No float64
+// arithmetic runs per step.
 __device__ __forceinline__ void op_forward(const Op& op, const float4* pshift,
-                                           RayS& r, double zc, double zi,
-                                           double& dvar, uint64_t& sbits,
+                                           RayS& r, float dvar, uint64_t& sbits,
                                            bool& alive, const float* aber = nullptr) {
   switch (op.kind) {
     case OP_FREE:
     case OP_FREE_VARZ: {
-      float d;
-      if (op.kind == OP_FREE) {
-        d = op.c[0];
-      } else {
-        const double dd = zc - zi;
-        dvar = dd;
-        d = (float)dd;
-      }
+      const float d = op.kind == OP_FREE ? op.c[0] : dvar;
       if (op.aux) {  // direction cosines (propagator.py:100-110): x += d dx / N^2, pl += d N
         const float s2 = fmaf(r.dx, r.dx, r.dy * r.dy);
         const float n2 = 1.f + s2;
@@ -263,12 +270,12 @@ struct Adj {
 // after it; on exit both describe the state before it.  c receives the step's
 // parameter sensitivities for this ray.  gz receives dL/dz_in (OP_FREE_VARZ).
 __device__ __forceinline__ void op_reverse(const Op& op, const float4* pshift, RayS& r,
-                                           Adj& a, uint64_t sbits, double dvar,
+                                           Adj& a, uint64_t sbits, float dvar,
                                            float c[4], float& gz) {
   switch (op.kind) {
     case OP_FREE:
     case OP_FREE_VARZ: {
-      float d = (op.kind == OP_FREE) ? op.c[0] : (float)dvar;
+      float d = (op.kind == OP_FREE) ? op.c[0] : dvar;
       if (op.aux) {  // direction cosines: slopes unchanged, so the step inverts exactly
         const float dx = r.dx, dy = r.dy;
         const float n2 = 1.f + fmaf(dx, dx, dy * dy);  // as in the forward step

@@ -30,6 +30,7 @@ struct FwdArgs {
   void* hist;
   int32_t h, w;
   int32_t do_bin;
+  int32_t opl_vec;  // opl is 16-byte aligned: paired double stores
 };
 
 template <int R>
@@ -74,22 +75,30 @@ k_trace_fwd(const __grid_constant__ Program P, const __grid_constant__ FwdArgs A
     load4<R>(A.dx, i0, n, dx, vec);
     load4<R>(A.dy, i0, n, dy, vec);
     RayS r[R];
-    double zi[R], dvar[R];
+    double dvar[R];  // per-ray first distance (per-ray input z only), float64 once per ray
+    float dvf[R];
     uint64_t sb[R];
     bool alive[R];
 #pragma unroll
     for (int k = 0; k < R; ++k) {
       r[k] = RayS{x[k], y[k], dx[k], dy[k], 0.f};
-      zi[k] = (A.z && i0 + k < n) ? A.z[i0 + k] : A.z_scalar;
       dvar[k] = 0.0;
+      dvf[k] = 0.f;
       sb[k] = 0;
       alive[k] = true;
+    }
+    if (A.z) {
+#pragma unroll
+      for (int k = 0; k < R; ++k) {
+        dvar[k] = P.zc_first - (i0 + k < n ? A.z[i0 + k] : A.z_scalar);
+        dvf[k] = (float)dvar[k];
+      }
     }
     for (int s = 0; s < P.n_steps; ++s) {
       const Op op = P.op[s];
 #pragma unroll
       for (int k = 0; k < R; ++k)
-        op_forward(op, nullptr, r[k], P.zc_first, zi[k], dvar[k], sb[k], alive[k], &P.aber[0][0]);
+        op_forward(op, nullptr, r[k], dvf[k], sb[k], alive[k], &P.aber[0][0]);
     }
 #pragma unroll
     for (int k = 0; k < R; ++k) {
@@ -100,15 +109,24 @@ k_trace_fwd(const __grid_constant__ Program P, const __grid_constant__ FwdArgs A
     store4<R>(A.odx, i0, n, dx, vec);
     store4<R>(A.ody, i0, n, dy, vec);
     if (A.opl) {
-      // float64 adds per ray kept to the minimum (one, plus one per per-ray
-      // input): GB300 issues float64 at ~1/60 of the float32 rate
+      // float64 work per ray kept to one add (plus one per per-ray input):
+      // GB300 issues float64 at ~1/64 of the float32 rate, so the float ->
+      // double conversion is done with integer operations
+      double o[R];
 #pragma unroll
       for (int k = 0; k < R; ++k) {
-        if (i0 + k < n) {
-          double base = A.pl ? (A.pl[i0 + k] + P.pl_const) : pl_uniform;
-          if (A.z) base += dvar[k];
-          A.opl[i0 + k] = base + (double)r[k].plv;
-        }
+        double base = pl_uniform;
+        if (A.pl && i0 + k < n) base = A.pl[i0 + k] + P.pl_const;
+        if (A.z) base += dvar[k];
+        o[k] = base + f32_to_f64(r[k].plv);
+      }
+      if (R == 4 && vec && A.opl_vec) {  // two 16-byte stores (i0 is a multiple of 4)
+        reinterpret_cast<double2*>(A.opl + i0)[0] = make_double2(o[0], o[1]);
+        reinterpret_cast<double2*>(A.opl + i0)[1] = make_double2(o[2 % R], o[3 % R]);
+      } else {
+#pragma unroll
+        for (int k = 0; k < R; ++k)
+          if (i0 + k < n) A.opl[i0 + k] = o[k];
       }
     }
     if (A.oz) {
@@ -229,11 +247,23 @@ extern "C" int tg_trace_fwd(const tg_model* model, const tg_rays* in, tg_rays* o
   }
   bool vec = al16(A.x) && al16(A.y) && al16(A.dx) && al16(A.dy) && al16(A.ox) &&
              al16(A.oy) && al16(A.odx) && al16(A.ody);
+  A.opl_vec = A.opl && al16(A.opl);
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   const int threads = 256;
   const int R = vec ? 4 : 1;
   int64_t blocks_needed = (A.n + (int64_t)threads * R - 1) / ((int64_t)threads * R);
-  int64_t cap = (int64_t)sm_count() * 8;
+  // every block resident at once: with the grid-stride loop each block has
+  // the same share, so blocks waiting for a slot would lengthen the tail
+  int per_sm = 1;
+  if (vec) {
+    if (hist_i64) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_fwd<4, long long>, threads, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_fwd<4, int>, threads, 0);
+  } else {
+    if (hist_i64) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_fwd<1, long long>, threads, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_fwd<1, int>, threads, 0);
+  }
+  if (per_sm < 1) per_sm = 1;
+  int64_t cap = (int64_t)sm_count() * per_sm;
   int blocks = (int)(blocks_needed < cap ? blocks_needed : cap);
   if (vec) {
     if (hist_i64) k_trace_fwd<4, long long><<<blocks, threads, 0, s>>>(P, A, B);
@@ -257,7 +287,11 @@ extern "C" int tg_bin(int64_t n, const float* x, const float* y, const uint8_t* 
   BinCoef B = make_bincoef(grid);
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   int64_t need = (n + 255) / 256;
-  int64_t cap = (int64_t)sm_count() * 8;
+  int per_sm = 1;
+  if (hist_i64) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bin<long long>, 256, 0);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bin<int>, 256, 0);
+  if (per_sm < 1) per_sm = 1;
+  int64_t cap = (int64_t)sm_count() * per_sm;
   int blocks = (int)(need < cap ? need : cap);
   if (hist_i64) k_bin<long long><<<blocks, 256, 0, s>>>(A, B);
   else k_bin<int><<<blocks, 256, 0, s>>>(A, B);
@@ -314,17 +348,21 @@ __device__ __forceinline__ int op_nsums(int kind) {
   }
 }
 
+constexpr int kVjpThreads = 256;
+
 template <int R>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(kVjpThreads)
 k_trace_vjp(const __grid_constant__ Program P, const __grid_constant__ VjpArgs A) {
-  __shared__ double acc[kMaxSteps * 4];
+  // per-warp float32 step sums (each warp owns a row: no atomics, no float64
+  // in the ray loop); combined in float64 in warp order at the end
+  __shared__ float wacc[kVjpThreads / 32][kMaxSteps * 4];
   const bool sums = A.partial != nullptr;
   if (sums)
-    for (int i = threadIdx.x; i < P.n_steps * 4; i += blockDim.x) acc[i] = 0.0;
+    for (int i = threadIdx.x; i < (kVjpThreads / 32) * kMaxSteps * 4; i += blockDim.x) (&wacc[0][0])[i] = 0.f;
   __syncthreads();
   const int64_t n = A.n;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x * R;
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int64_t blk = (int64_t)blockIdx.x * blockDim.x * R; blk < n; blk += stride) {
     const int64_t i0 = blk + (int64_t)threadIdx.x * R;
     const bool vec = (R == 4) && (i0 + 3 < n);
@@ -335,7 +373,7 @@ k_trace_vjp(const __grid_constant__ Program P, const __grid_constant__ VjpArgs A
     load4<R>(A.dy, i0, n, dy, vec);
     RayS r[R];
     Adj ad[R];
-    double zi[R], dvar[R];
+    float dvf[R];  // per-ray first distance (per-ray input z only)
     uint64_t sb[R];
     bool alive[R];
     float gz[R];
@@ -348,8 +386,7 @@ k_trace_vjp(const __grid_constant__ Program P, const __grid_constant__ VjpArgs A
     for (int k = 0; k < R; ++k) {
       const bool inr = i0 + k < n;
       r[k] = RayS{x[k], y[k], dx[k], dy[k], 0.f};
-      zi[k] = (A.z && inr) ? A.z[i0 + k] : A.z_scalar;
-      dvar[k] = 0.0;
+      dvf[k] = 0.f;
       sb[k] = 0;
       alive[k] = true;
       gz[k] = 0.f;
@@ -357,11 +394,15 @@ k_trace_vjp(const __grid_constant__ Program P, const __grid_constant__ VjpArgs A
       // rays beyond n carry zero adjoints so they add nothing to the sums
       ad[k] = inr ? Adj{gx[k], gy[k], gdx[k], gdy[k], gp} : Adj{0.f, 0.f, 0.f, 0.f, 0.f};
     }
+    if (A.z) {
+#pragma unroll
+      for (int k = 0; k < R; ++k) dvf[k] = (float)(P.zc_first - (i0 + k < n ? A.z[i0 + k] : A.z_scalar));
+    }
     for (int s = 0; s < P.n_steps; ++s) {
       const Op op = P.op[s];
 #pragma unroll
       for (int k = 0; k < R; ++k)
-        op_forward(op, nullptr, r[k], P.zc_first, zi[k], dvar[k], sb[k], alive[k]);
+        op_forward(op, nullptr, r[k], dvf[k], sb[k], alive[k]);
     }
     for (int s = P.n_steps - 1; s >= 0; --s) {
       const Op op = P.op[s];
@@ -369,14 +410,14 @@ k_trace_vjp(const __grid_constant__ Program P, const __grid_constant__ VjpArgs A
 #pragma unroll
       for (int k = 0; k < R; ++k) {
         float ck[4] = {0.f, 0.f, 0.f, 0.f};
-        op_reverse(op, nullptr, r[k], ad[k], sb[k], dvar[k], ck, gz[k]);
+        op_reverse(op, nullptr, r[k], ad[k], sb[k], dvf[k], ck, gz[k]);
         c[0] += ck[0]; c[1] += ck[1]; c[2] += ck[2]; c[3] += ck[3];
       }
       if (sums) {
         const int ns = op_nsums(op.kind);
         for (int j = 0; j < ns; ++j) {
           float v = warp_sum(c[j]);
-          if (lane == 0) atomicAdd(&acc[4 * s + j], (double)v);
+          if (lane == 0) wacc[warp][4 * s + j] += v;
         }
       }
     }
@@ -399,7 +440,11 @@ k_trace_vjp(const __grid_constant__ Program P, const __grid_constant__ VjpArgs A
   if (sums) {
     __syncthreads();
     double* dst = A.partial + (size_t)blockIdx.x * P.n_steps * 4;
-    for (int i = threadIdx.x; i < P.n_steps * 4; i += blockDim.x) dst[i] = acc[i];
+    for (int i = threadIdx.x; i < P.n_steps * 4; i += blockDim.x) {
+      double t = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += (double)wacc[w][i];
+      dst[i] = t;
+    }
   }
 }
 
@@ -419,9 +464,18 @@ __global__ void k_reduce_partials(const double* __restrict__ partial, int nblock
   raw[i] += ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
 }
 
+// Grid of the adjoint: every block resident at once (the grid-stride loop
+// gives each block the same share, so a block that waits for a free slot
+// would double the tail).  The residency of the wider variant bounds both.
 static int vjp_grid(int64_t n) {
+  static int per_sm = 0;
+  if (!per_sm) {
+    int v = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_trace_vjp<4>, kVjpThreads, 0);
+    per_sm = v > 0 ? v : 1;
+  }
   int64_t need = (n + 1023) / 1024;
-  int64_t cap = (int64_t)sm_count() * 4;
+  int64_t cap = (int64_t)sm_count() * per_sm;
   int64_t g = need < cap ? need : cap;
   return (int)(g < 1 ? 1 : g);
 }
@@ -467,8 +521,8 @@ extern "C" int tg_trace_vjp(const tg_model* model, const tg_rays* in, const tg_r
              al16(A.gy) && al16(A.gdx) && al16(A.gdy) && (!A.ix || al16(A.ix)) &&
              (!A.iy || al16(A.iy)) && (!A.idx || al16(A.idx)) && (!A.idy || al16(A.idy));
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-  if (vec) k_trace_vjp<4><<<grid, 256, 0, s>>>(P, A);
-  else k_trace_vjp<1><<<grid, 256, 0, s>>>(P, A);
+  if (vec) k_trace_vjp<4><<<grid, kVjpThreads, 0, s>>>(P, A);
+  else k_trace_vjp<1><<<grid, kVjpThreads, 0, s>>>(P, A);
   if (A.partial) {
     int width = P.n_steps * 4;
     k_reduce_partials<<<(width + 127) / 128, 128, 0, s>>>(A.partial, grid, width, raw);
