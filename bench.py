@@ -544,6 +544,52 @@ def secondary_batched(torch, dev, hbm):
             "plain_per_model_ms": ms_plain, "speedup_vs_plain_per_model": ms_plain / ms}
 
 
+def secondary_trace_large(torch, dev, hbm):
+    """The fused chain at 16,777,216 rays (Lens + Detector): forward with
+    pathlength (40 B/ray), forward + pixels + int64 histogram (48 B/ray), and
+    the adjoint with input gradients and per-step sums (48 B/ray), through
+    the C ABI on device buffers."""
+    import ctypes as C
+
+    from temgymcore_gb300 import _native as N
+    from temgymcore_gb300.run import _rays_struct, pack_model
+    from temgymcore_gb300.workloads import build_model
+    n = 1 << 24
+    rng = np.random.default_rng(0)
+    x, y = (torch.tensor(rng.uniform(-1e-3, 1e-3, n).astype(np.float32), device=dev) for _ in range(2))
+    dx, dy = (torch.tensor(rng.normal(0, 1e-3, n).astype(np.float32), device=dev) for _ in range(2))
+    model = build_model([{"kind": "lens", "z": 0.5, "focal_length": 0.2},
+                         {"kind": "detector", "z": 1.0, "pixel_size": (1e-5, 1e-5), "shape": (256, 256)}])
+    m, keep = pack_model(model)
+    o = [torch.empty(n, device=dev) for _ in range(4)]
+    opl = torch.empty(n, dtype=torch.float64, device=dev)
+    rin = _rays_struct(n, x, y, dx, dy, None, 0.0, None, 0.0)
+    rout = _rays_struct(n, *o, None, 0.0, opl, 0.0)
+    grid = model[-1]._tg_grid()
+    py, px = (torch.empty(n, dtype=torch.int32, device=dev) for _ in range(2))
+    hist = torch.zeros((256, 256), dtype=torch.int64, device=dev)
+    g = [torch.randn(n, device=dev) for _ in range(4)]
+    gi = [torch.empty(n, device=dev) for _ in range(4)]
+    gout = _rays_struct(n, *g, None, 0.0, None, 0.0)
+    gin = _rays_struct(n, *gi, None, 0.0, None, 0.0)
+    raw = torch.zeros((4, 4), dtype=torch.float64, device=dev)
+    lib = N.lib()
+    ws = torch.empty(lib.tg_trace_vjp_workspace(n, C.byref(m)) + 256, dtype=torch.uint8, device=dev)
+    sp = N.stream_ptr()
+    fwd = lambda: lib.tg_trace_fwd(C.byref(m), C.byref(rin), C.byref(rout), None, None, None, None, None, 0, sp)  # noqa: E731
+    fwd_bin = lambda: lib.tg_trace_fwd(C.byref(m), C.byref(rin), C.byref(rout), None, C.byref(grid),  # noqa: E731
+                                       py.data_ptr(), px.data_ptr(), hist.data_ptr(), 1, sp)
+    vjp = lambda: lib.tg_trace_vjp(C.byref(m), C.byref(rin), C.byref(gout), C.byref(gin), raw.data_ptr(),  # noqa: E731
+                                   ws.data_ptr(), ws.numel(), sp)
+    res = {"workload": "fused chain, 16,777,216 rays, Lens + Detector 256x256"}
+    for name, fn, bpr in (("forward", fwd, 40), ("forward_pixels_histogram", fwd_bin, 48), ("adjoint", vjp, 48)):
+        ms = _time(torch, fn, 20)
+        res[name] = {"ms": ms, "rays_per_s": n / (ms * 1e-3), "bytes_per_ray": bpr,
+                     "achieved_gbs": n * bpr / (ms * 1e-3) / 1e9, "frac_of_hbm": n * bpr / (ms * 1e-3) / 1e9 / hbm}
+    del keep
+    return res
+
+
 def secondary_transfer(torch, dev, hbm):
     """transfer_rays: 1,048,576 rays through the cumulative products of 16
     transfer matrices -> (N, 16, 5) float64 (671 MB written)."""
@@ -678,6 +724,10 @@ def run_gpu(args, world, rank, local):
             secondary["input_field"] = secondary_input_field(torch, dev, bf16)
         except Exception as e:
             secondary["input_field"] = {"error": repr(e)}
+        try:
+            secondary["trace_large"] = secondary_trace_large(torch, dev, hbm)
+        except Exception as e:
+            secondary["trace_large"] = {"error": repr(e)}
         try:
             secondary["transfer_rays"] = secondary_transfer(torch, dev, hbm)
         except Exception as e:
