@@ -12,11 +12,11 @@
 //      keeps each ray's packed pixel in shared memory,
 //   3. reduces the hits' bounding box; when it fits the shared-memory window
 //      (the normal case: a probe lights a small disc) it histograms there,
-//   4. writes the dense image once: the image rows outside the window's row
-//      span are all zeros and leave as TMA bulk copies from a zero buffer
-//      in shared memory (asynchronous: the CTA goes on to the next probe
-//      while the copy engine streams them), the window rows as 16-byte
-//      stores of counts and zeros.
+//   4. writes the dense image once: the window rows, and a quarter of the
+//      image's rows of zeros around them, as 16-byte stores; the other rows
+//      are all zeros and leave as TMA bulk copies from a zero buffer in
+//      shared memory (asynchronous: the CTA goes on to the next probe while
+//      the copy engine streams them).  Both write paths run at once.
 // A probe whose hits do not fit the window, or a bundle larger than the
 // shared ray buffer, takes the slow path: zero-fill, barrier, global atomics.
 // The HBM traffic is therefore the dense histogram write, ~h*w*4 bytes/probe.
@@ -47,6 +47,7 @@ struct ScanArgs {
   int32_t h, w;
   int32_t vec4;  // rows are 16-byte aligned: dense write with int4 stores
   int32_t bulk;  // images in device memory: zero rows as TMA bulk copies
+  int32_t store_rows;  // zero rows next to the window written by stores, not bulk copies
 };
 
 __device__ __forceinline__ void probe_shifts(const Program& P, const ScanArgs& A, int p,
@@ -162,12 +163,20 @@ k_scan_hist(const __grid_constant__ Program P, const __grid_constant__ ScanArgs 
         __syncthreads();
       }
       if (A.vec4) {
-        // band rows outside [r0, r1) are zeros: bulk copies of the zero
-        // buffer (row starts are 16-byte aligned: W is a multiple of 4 and
+        // the window rows and store_rows zero rows around them are written
+        // by 16-byte stores, [r0, r1); band rows outside are zeros: bulk
+        // copies of the zero buffer (row starts are 16-byte aligned: W is a multiple of 4 and
         // the images 16-byte aligned); one thread issues them, the group is
         // committed and left in flight.  Images in host memory (written
         // across the host link) take 16-byte stores for every row instead.
-        const int r0 = A.bulk ? (any ? rmin : ra) : ra, r1 = A.bulk ? (any ? rmax + 1 : ra) : rb;
+        int r0 = A.bulk ? (any ? rmin : ra) : ra, r1 = A.bulk ? (any ? rmax + 1 : ra) : rb;
+        if (A.bulk && A.store_rows > 0) {  // store_rows more zero rows by stores, around the window
+          int below = min(A.store_rows >> 1, r0 - ra);
+          const int above = min(A.store_rows - below, rb - r1);
+          below = min(A.store_rows - above, r0 - ra);
+          r0 -= below;
+          r1 += above;
+        }
         if (A.bulk && threadIdx.x == 0) {
           char* base = reinterpret_cast<char*>(img);
           const int64_t row_bytes = (int64_t)W * 4;
@@ -281,6 +290,10 @@ extern "C" int tg_scan_hist(const tg_model* model, const tg_rays* bundle, const 
   A.h = grid->h;
   A.w = grid->w;
   A.vec4 = ((grid->w & 3) == 0) && ((reinterpret_cast<uintptr_t>(hist) & 15) == 0);
+  // a quarter of the rows go out as stores beside the bulk copies: the two
+  // write paths run in parallel (256x256 images, 64x64 probes: 0.1815 ms with
+  // bulk copies alone, 0.1777 ms with 64 stored rows; 32 and 80 rows between)
+  A.store_rows = grid->h / 4;
   {  // images may live in pinned host memory (written by the kernel across the host link)
     cudaPointerAttributes pa;
     if (cudaPointerGetAttributes(&pa, hist) != cudaSuccess) return TG_ERR_CUDA;
