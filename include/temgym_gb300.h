@@ -127,6 +127,16 @@ int tg_get_error_word(uint32_t *out, int clear);
 /* Read and clear the device error word (0xffffffff if it could not be read). */
 uint32_t tg_get_last_error_word(void);
 
+/*
+ * tg_selftest_add_f64_f32 - diagnostics: the pathlength rounding the trace
+ * kernels use (base + float32 part, rounded to nearest even with float32 and
+ * integer operations) next to the float64 add, over n device pairs:
+ * fast[i] = emulated b[i] + p[i], ref[i] = float64 b[i] + (double)p[i].  The
+ * two must agree bit for bit.  No reference counterpart.
+ */
+int tg_selftest_add_f64_f32(const double *b, const float *p, double *fast, double *ref,
+                            int64_t n, void *stream);
+
 /* ---- ray chain -------------------------------------------------------- */
 /*
  * tg_trace_fwd - fused forward trace (+ optional pixel binning + histogram).

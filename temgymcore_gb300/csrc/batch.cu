@@ -397,7 +397,7 @@ k_batch(const uint8_t* __restrict__ plan, const __grid_constant__ BatchIO io,
           oy[i] = y[k];
           odx[i] = dx[k];
           ody[i] = dy[k];
-          if (opl) opl[i] = M.pl_const + (double)pl[k];
+          if (opl) opl[i] = add_f64_f32(M.pl_const, pl[k]);
         }
       }
       if (!adj) continue;

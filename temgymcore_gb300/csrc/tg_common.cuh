@@ -166,6 +166,41 @@ __device__ __forceinline__ double f32_to_f64(float v) {
   return __longlong_as_double((long long)d);
 }
 
+// b + p rounded to nearest even, bit-identical to __dadd_rn(b, (double)p),
+// with float32 and integer operations in the usual case: p small against b
+// (a per-ray pathlength part added to a metre-scale base), so that the sum
+// stays in b's binade.  With u = ulp(b) = 2^(e_b - 1075), b + p is
+// (-1)^sign(b) * (m_b + (-1)^sign(b) * p/u) * u for b's 53-bit integer
+// significand m_b; p/u is exact in float32 (a power-of-two scale), its
+// rounding to an integer n (ties to even, by the 1.5*2^23 magic constant)
+// is the rounding of the sum when the result keeps b's exponent, and adding
+// +-n to b's bit pattern adds it to the significand.  The float64 add is
+// taken when b is zero, denormal, non-finite or outside 2^-75..2^178, when
+// |p/u| >= 2^22 or is NaN, on an exact tie (|p/u - n| = 1/2: ties go to the
+// even significand, not the even n), when the sum leaves b's binade other
+// than onto its upper boundary, and when it lands on the lower boundary.
+__device__ __forceinline__ double add_f64_f32(double b, float p) {
+  const long long bb = __double_as_longlong(b);
+  const int eb = (int)((bb >> 52) & 0x7ff);
+  const int k = 1075 - eb;  // p / ulp(b) = p * 2^k
+  if (k >= -126 && k <= 127) {
+    const float s = __fmul_rn(p, __int_as_float((k + 127) << 23));
+    const float magic = 12582912.f;  // 1.5 * 2^23: float32 ulp 1 on (2^23, 2^24)
+    const float t = __fadd_rn(s, magic);
+    const int n = __float_as_int(t) - __float_as_int(magic);
+    const float r = __fsub_rn(s, __fsub_rn(t, magic));  // exact
+    if (fabsf(s) < 4194304.f && fabsf(r) != 0.5f) {
+      const long long nb = bb + (bb < 0 ? -(long long)n : (long long)n);
+      const int en = (int)((nb >> 52) & 0x7ff);
+      const bool mant0 = (nb & 0xfffffffffffffLL) == 0;
+      // a result on the binade's lower boundary (a power of two) may belong
+      // below it, where the grid is twice as fine: float64 add
+      if ((en == eb && !mant0) || (en == eb + 1 && mant0)) return __longlong_as_double(nb);
+    }
+  }
+  return __dadd_rn(b, (double)p);
+}
+
 // ---------------------------------------------------------------- ray ops
 struct RayS {
   float x, y, dx, dy, plv;  // plv: per-ray (varying) pathlength part

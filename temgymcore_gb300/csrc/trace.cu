@@ -3,9 +3,11 @@
 //
 // One kernel pass reads each ray once (x, y, dx, dy as float4 vectors of four
 // consecutive rays per thread), runs the whole component chain in registers,
-// and writes the outputs once.  The float64 work per ray is one add for the
-// pathlength and, for the rare coordinates near a pixel-rounding tie, one
-// exact float64 binning evaluation (see tg_common.cuh).
+// and writes the outputs once.  No float64 arithmetic runs per ray in the
+// usual case: the pathlength's float64 base + float32 part is rounded with
+// float32 / integer operations (add_f64_f32), and only the rare coordinates
+// near a pixel-rounding tie take an exact float64 binning evaluation (see
+// tg_common.cuh).
 #include <cstring>
 
 #include "tg_common.cuh"
@@ -109,16 +111,16 @@ k_trace_fwd(const __grid_constant__ Program P, const __grid_constant__ FwdArgs A
     store4<R>(A.odx, i0, n, dx, vec);
     store4<R>(A.ody, i0, n, dy, vec);
     if (A.opl) {
-      // float64 work per ray kept to one add (plus one per per-ray input):
-      // GB300 issues float64 at ~1/64 of the float32 rate, so the float ->
-      // double conversion is done with integer operations
+      // no float64 arithmetic per ray for a uniform base (one add per
+      // per-ray input): GB300 issues float64 at ~1/64 of the float32 rate,
+      // so base + plv is rounded with float32 / integer operations
       double o[R];
 #pragma unroll
       for (int k = 0; k < R; ++k) {
         double base = pl_uniform;
         if (A.pl && i0 + k < n) base = A.pl[i0 + k] + P.pl_const;
         if (A.z) base += dvar[k];
-        o[k] = base + f32_to_f64(r[k].plv);
+        o[k] = add_f64_f32(base, r[k].plv);
       }
       if (R == 4 && vec && A.opl_vec) {  // two 16-byte stores (i0 is a multiple of 4)
         reinterpret_cast<double2*>(A.opl + i0)[0] = make_double2(o[0], o[1]);
@@ -433,7 +435,7 @@ k_trace_vjp(const __grid_constant__ Program P, const __grid_constant__ VjpArgs A
     for (int k = 0; k < R; ++k) {
       if (i0 + k < n) {
         if (A.ipl) A.ipl[i0 + k] = A.gpl ? A.gpl[i0 + k] : 0.0;
-        if (A.iz) A.iz[i0 + k] = (double)gz[k];
+        if (A.iz) A.iz[i0 + k] = f32_to_f64(gz[k]);
       }
     }
   }
@@ -591,4 +593,25 @@ extern "C" int tg_trace_adj(const tg_model* model, const tg_rays* in, const floa
   gout.n = n;
   gout.x = v[4]; gout.y = v[5]; gout.dx = v[6]; gout.dy = v[7];
   return tg_trace_vjp(model, in, &gout, dray, dparams, ws + 8 * vec, ws_bytes - 8 * vec, stream);
+}
+
+namespace tg {
+__global__ void k_selftest_add(const double* __restrict__ b, const float* __restrict__ p,
+                               double* __restrict__ fast, double* __restrict__ ref, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    fast[i] = add_f64_f32(b[i], p[i]);
+    ref[i] = __dadd_rn(b[i], (double)p[i]);
+  }
+}
+}  // namespace tg
+
+extern "C" int tg_selftest_add_f64_f32(const double* b, const float* p, double* fast, double* ref,
+                                       int64_t n, void* stream) {
+  if (n < 0 || (n > 0 && (!b || !p || !fast || !ref))) return TG_ERR_INVALID;
+  if (n == 0) return TG_OK;
+  int blocks = (int)((n + 255) / 256);
+  if (blocks > 4096) blocks = 4096;
+  k_selftest_add<<<blocks, 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(b, p, fast, ref, n);
+  return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
 }
