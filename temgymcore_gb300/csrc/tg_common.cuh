@@ -99,8 +99,13 @@ struct BinCoef {
   double d[6];
 };
 
-__device__ __forceinline__ int bin_exact64(double a, double b, double m0,
+__device__ __forceinline__ int bin_exact64(float af, float bf, double m0,
                                            double m1, double m2) {
+  // the conversions sit in volatile blocks, so that the compiler keeps them
+  // behind the caller's branch instead of running them for every thread
+  double a, b;
+  asm volatile("cvt.f64.f32 %0, %1;" : "=d"(a) : "f"(af));
+  asm volatile("cvt.f64.f32 %0, %1;" : "=d"(b) : "f"(bf));
   double v = __dadd_rn(__dadd_rn(__dmul_rn(m0, a), __dmul_rn(m1, b)), m2);
   if (v != v) return 0;       // NaN -> 0 (the hardware conversion gives INT_MIN)
   return __double2int_rn(v);  // cvt.rni.s32.f64: saturating
@@ -114,11 +119,15 @@ __device__ __forceinline__ int bin_one(float a, float b, float m0, float m1,
   float s = fabsf(p0) + fabsf(p1) + fabsf(m2);
   // |v - exact| <= ~5 * 2^-24 * s; use 2^-19 * s (16x margin) + denormal guard
   float bound = s * 1.9073486e-06f + 1e-30f;
-  float fl = floorf(v);
-  float dist = fabsf((v - fl) - 0.5f);
-  bool ok = (fabsf(v) < 4194304.f) && (dist > bound);  // |v| < 2^22, finite
-  if (ok) return __float2int_rn(v);
-  return bin_exact64((double)a, (double)b, d0, d1, d2);
+  // nearest integer by the 1.5 * 2^23 constant (float32 ulp 1 there, exact
+  // for |v| < 2^22), so no conversion instruction runs; r = v - rint(v)
+  // exactly, and 1/2 - |r| is the distance to the nearest half-integer
+  const float magic = 12582912.f;
+  const float t = __fadd_rn(v, magic);
+  const float r = __fsub_rn(v, __fsub_rn(t, magic));
+  bool ok = (fabsf(v) < 4194304.f) && (0.5f - fabsf(r) > bound);  // |v| < 2^22, finite
+  if (ok) return __float_as_int(t) - __float_as_int(magic);
+  return bin_exact64(a, b, d0, d1, d2);
 }
 
 __device__ __forceinline__ void bin_yx(float x, float y, const BinCoef& bc,
@@ -166,39 +175,65 @@ __device__ __forceinline__ double f32_to_f64(float v) {
   return __longlong_as_double((long long)d);
 }
 
+// m / 2^a rounded half-even (m < 2^24, 1 <= a <= 26); tie: exactly halfway.
+__device__ __forceinline__ long long rne_shr(uint32_t m, int a, bool& tie) {
+  const uint32_t q = m >> a, rem = m & ((1u << a) - 1u), half = 1u << (a - 1);
+  tie = rem == half;
+  return (long long)(q + ((rem > half || (tie && (q & 1u))) ? 1u : 0u));
+}
+
 // b + p rounded to nearest even, bit-identical to __dadd_rn(b, (double)p),
-// with float32 and integer operations in the usual case: p small against b
-// (a per-ray pathlength part added to a metre-scale base), so that the sum
-// stays in b's binade.  With u = ulp(b) = 2^(e_b - 1075), b + p is
-// (-1)^sign(b) * (m_b + (-1)^sign(b) * p/u) * u for b's 53-bit integer
-// significand m_b; p/u is exact in float32 (a power-of-two scale), its
-// rounding to an integer n (ties to even, by the 1.5*2^23 magic constant)
-// is the rounding of the sum when the result keeps b's exponent, and adding
-// +-n to b's bit pattern adds it to the significand.  The float64 add is
-// taken when b is zero, denormal, non-finite or outside 2^-75..2^178, when
-// |p/u| >= 2^22 or is NaN, on an exact tie (|p/u - n| = 1/2: ties go to the
-// even significand, not the even n), when the sum leaves b's binade other
-// than onto its upper boundary, and when it lands on the lower boundary.
+// with integer operations in the usual case (a metre-scale float64 base plus
+// a float32 per-ray part): GB300 runs float64 at ~1/64 of the float32 rate.
+// With u = ulp(b) = 2^(e_b - 1075) and p = m 2^(e_p - 150) (m its 24-bit
+// significand), p / u = m 2^sh, sh = e_p - e_b + 925: a shift of m, exact
+// for sh >= 0 and rounded half-even for sh < 0.  Adding n = round(p / u) to
+// b's bit pattern adds it to b's 53-bit integer significand, which is the
+// correctly rounded sum while the result keeps b's exponent (or lands on the
+// next power of two).  When it would land on or below b's binade's lower
+// boundary the grid below is twice as fine: the sum is rounded at u / 2
+// instead (n2 = round(2 p / u)), and the bits follow from b's mantissa field
+// f as bits(b) + f + n2 (or the power of two itself when that rounding
+// stays on it).  The float64 add is kept for zero, denormal and non-finite
+// operands, b outside 2^-1021..2^1022, |p| beyond ~|b|, exact halfway
+// cases (ties go to the even significand of the sum, not of n) and sums
+// that leave the binade further.
 __device__ __forceinline__ double add_f64_f32(double b, float p) {
   const long long bb = __double_as_longlong(b);
-  const int eb = (int)((bb >> 52) & 0x7ff);
-  const int k = 1075 - eb;  // p / ulp(b) = p * 2^k
-  if (k >= -126 && k <= 127) {
-    const float s = __fmul_rn(p, __int_as_float((k + 127) << 23));
-    const float magic = 12582912.f;  // 1.5 * 2^23: float32 ulp 1 on (2^23, 2^24)
-    const float t = __fadd_rn(s, magic);
-    const int n = __float_as_int(t) - __float_as_int(magic);
-    const float r = __fsub_rn(s, __fsub_rn(t, magic));  // exact
-    if (fabsf(s) < 4194304.f && fabsf(r) != 0.5f) {
-      const long long nb = bb + (bb < 0 ? -(long long)n : (long long)n);
-      const int en = (int)((nb >> 52) & 0x7ff);
-      const bool mant0 = (nb & 0xfffffffffffffLL) == 0;
-      // a result on the binade's lower boundary (a power of two) may belong
-      // below it, where the grid is twice as fine: float64 add
-      if ((en == eb && !mant0) || (en == eb + 1 && mant0)) return __longlong_as_double(nb);
+  const uint32_t pb = __float_as_uint(p);
+  const int eb = (int)((bb >> 52) & 0x7ff), ep = (int)((pb >> 23) & 0xffu);
+  if (eb >= 2 && eb <= 2045) {
+    if ((pb & 0x7fffffffu) == 0u) return b;  // b + (+-0)
+    const int sh = ep - eb + 925;
+    if (ep >= 1 && ep <= 254 && sh <= 29) {
+      const uint32_t m = (pb & 0x7fffffu) | 0x800000u;
+      long long n = 0, n2 = 0;  // p / u and 2 p / u, rounded half-even
+      bool tie = false, tie2 = false;
+      if (sh >= 0) {
+        n = (long long)m << sh;
+        n2 = n << 1;
+      } else if (sh >= -26) {  // below: |p / u| < 1/8, both round to 0
+        n = rne_shr(m, -sh, tie);
+        n2 = sh == -1 ? (long long)m : rne_shr(m, -sh - 1, tie2);
+      }
+      const bool neg = ((pb >> 31) != 0u) != (bb < 0);  // the magnitude of b shrinks
+      const long long N = neg ? -n : n, N2 = neg ? -n2 : n2;
+      const long long f = bb & 0xfffffffffffffLL;
+      if (f + N >= 1) {  // inside the binade, or onto the next power of two
+        if (!tie && f + N <= (1LL << 52)) return __longlong_as_double(bb + N);
+      } else {  // at or below the binade's lower boundary: the finer grid
+        const long long low = 2 * f + N2;
+        if (!tie && !tie2 && low >= -(1LL << 52))
+          return __longlong_as_double(low >= 0 ? bb - f : bb + f + N2);
+      }
     }
   }
-  return __dadd_rn(b, (double)p);
+  // the float64 add in a volatile block, so that the compiler does not run
+  // it (conversion + add) ahead of the branch for every thread
+  double r;
+  asm volatile("{\n\t.reg .f64 pd;\n\tcvt.f64.f32 pd, %2;\n\tadd.rn.f64 %0, %1, pd;\n\t}"
+               : "=d"(r) : "d"(b), "f"(p));
+  return r;
 }
 
 // ---------------------------------------------------------------- ray ops
