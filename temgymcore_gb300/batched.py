@@ -43,8 +43,8 @@ N.register("tg_batch_run", C.c_int, [C.c_void_p, C.POINTER(TgBatchInfo), C.POINT
                                      C.c_int32, C.c_void_p, C.c_size_t, C.c_void_p])
 
 # (tile rays, block, rays per thread) candidates
-CANDIDATES = [(2048, 256, 2), (4096, 256, 2), (4096, 128, 4), (8192, 256, 2), (4096, 256, 4),
-              (4096, 512, 2), (8192, 256, 4), (2048, 256, 1)]
+CANDIDATES = [(2048, 256, 2), (4096, 256, 2), (4096, 128, 4), (8192, 256, 2), (16384, 256, 2),
+              (4096, 256, 4), (4096, 512, 2), (8192, 256, 4), (2048, 256, 1)]
 
 
 class _TuneCache:

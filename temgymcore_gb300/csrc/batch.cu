@@ -20,6 +20,7 @@
 // per ray); the CTA that finishes a model's last tile reduces its moments and
 // turns them into the per-step sums with 5x5 algebra (batch_model_tail), so
 // one launch does the whole forward + adjoint.
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -30,7 +31,7 @@ TG_DEFINE_ERROR_WORD(batch)
 namespace tg {
 
 struct BModel {
-  int32_t op_off, n_steps, tile_off, n_tiles;
+  int32_t op_off, n_steps, n_tiles, pad;
   int64_t ray_off, n_rays;
   double pl_const, z_out;
   int64_t part_off;  // doubles: this model's first tile partial
@@ -41,6 +42,8 @@ struct BModel {
 struct BTile {
   int32_t model, count;
   int64_t start;  // absolute ray index
+  int32_t slot;   // tile index within its model: the partial's row
+  int32_t pad;
 };
 
 struct BHeader {
@@ -280,6 +283,11 @@ k_batch(const uint8_t* __restrict__ plan, const __grid_constant__ BatchIO io,
       continue;
     }
     const BModel M = models[T.model];
+    if (T.slot < 0 || T.slot >= M.n_tiles) {  // corrupt plan: flag and skip
+      if (threadIdx.x == 0) atomicOr(&g_tg_err, TG_EW_TABLE);
+      __syncthreads();
+      continue;
+    }
     const int nc = M.n_steps >> 1, nm = M.n_mom, nb = M.n_bip;
     for (int i = threadIdx.x; i < nc; i += blockDim.x) {
       const Op fr = ops[M.op_off + 2 * i], co = ops[M.op_off + 2 * i + 1];
@@ -399,7 +407,7 @@ k_batch(const uint8_t* __restrict__ plan, const __grid_constant__ BatchIO io,
           ody[i] = dy[k];
           // the float64 add: add_f64_f32's integer rounding measured slower
           // in this register-bound kernel (0.318 vs 0.291 ms on the sweep)
-          if (opl) opl[i] = M.pl_const + f32_to_f64(pl[k]);
+          if (opl) opl[i] = M.pl_const + (double)pl[k];
         }
       }
       if (!adj) continue;
@@ -467,7 +475,7 @@ k_batch(const uint8_t* __restrict__ plan, const __grid_constant__ BatchIO io,
       // counts a model's last tile runs its adjoint tail (only warp 0 waits
       // for the fence, the other warps' ray stores are not ordered with it)
       if (warp == 0) {
-        double* dst = partial + M.part_off + (int64_t)(t - M.tile_off) * nm;
+        double* dst = partial + M.part_off + (int64_t)T.slot * nm;
         for (int i = lane; i < nm; i += 32) {
           double a = 0.0;
           for (int w = 0; w < nwarps; ++w) a += (double)wacc[w * nm + i];
@@ -514,6 +522,7 @@ extern "C" int tg_batch_plan(int32_t n_models, const tg_model* models, const int
   std::vector<BTile> bt;
   std::vector<Op> ops;
   std::vector<int32_t> mom_model;
+  std::vector<int64_t> work;  // per tile: rays x (components + adjoint overhead)
   int64_t ray_off = 0, part_off = 0, mom_off = 0;
   int32_t max_steps = 0, max_mom = 10;
   for (int m = 0; m < n_models; ++m) {
@@ -527,7 +536,6 @@ extern "C" int tg_batch_plan(int32_t n_models, const tg_model* models, const int
     M.op_off = (int32_t)ops.size();
     M.n_steps = P.n_steps;
     if (P.n_steps > max_steps) max_steps = P.n_steps;
-    M.tile_off = (int32_t)bt.size();
     M.ray_off = ray_off;
     M.n_rays = n_rays[m];
     M.pl_const = P.pl_const;
@@ -547,13 +555,25 @@ extern "C" int tg_batch_plan(int32_t n_models, const tg_model* models, const int
       T.model = m;
       T.start = ray_off + r;
       T.count = (int32_t)((n_rays[m] - r) < tile_rays ? (n_rays[m] - r) : tile_rays);
+      T.slot = nt;
+      T.pad = 0;
       bt.push_back(T);
+      work.push_back((int64_t)T.count * (P.n_steps / 2 + 2));
     }
     M.n_tiles = nt;
     part_off += (int64_t)nt * M.n_mom;
     mom_off += M.n_mom;
     ray_off += n_rays[m];
     if (bt.size() > 0x7fffffff || ops.size() > 0x7fffffff) return TG_ERR_TOO_LARGE;
+  }
+  {  // longest tiles first (the work counter hands them out in list order), so
+     // the launch ends on small tiles; ties keep model order
+    std::vector<int32_t> ord(bt.size());
+    for (size_t i = 0; i < ord.size(); ++i) ord[i] = (int32_t)i;
+    std::stable_sort(ord.begin(), ord.end(), [&](int32_t a, int32_t b) { return work[a] > work[b]; });
+    std::vector<BTile> sorted(bt.size());
+    for (size_t i = 0; i < ord.size(); ++i) sorted[i] = bt[ord[i]];
+    bt.swap(sorted);
   }
   BHeader H;
   std::memset(&H, 0, sizeof(H));
