@@ -35,45 +35,6 @@ constexpr int kGemmSmem = kGStages * kStageBytes + 1024 /*align*/ + 256 /*barrie
 // kind::f16 instruction descriptor: f32 accumulate, bf16 A and B, both
 // K-major, N = 256, M = 128.
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((256u >> 3) << 17) | ((128u >> 4) << 24);
-constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t a, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint32_t a, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes)
-               : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try(uint32_t a, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(a), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// Bounded wait; returns false (and flags the error word) on timeout.
-__device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity) {
-  long long t0 = clock64();
-  for (uint32_t it = 0;; ++it) {
-    if (mbar_try(a, parity)) return true;
-    if ((it & 255u) == 255u && clock64() - t0 > kWaitCycles) {
-      atomicOr(&g_tg_err, TG_EW_MMA);
-      return false;
-    }
-  }
-}
-
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int c0, int c1,
                                             uint32_t mbar) {
   asm volatile(
@@ -171,7 +132,7 @@ k_field_gemm(const __grid_constant__ GemmMaps maps, const __grid_constant__ Gemm
     for (int i = 0; i < A.nkb && ok; ++i) {
       const int s = i % kGStages;
       const uint32_t ph = (uint32_t)(i / kGStages) & 1u;
-      if (!mbar_wait(empty0 + 8 * s, ph ^ 1u)) { ok = false; break; }
+      if (!mbar_wait(empty0 + 8 * s, ph ^ 1u, &g_tg_err, TG_EW_MMA)) { ok = false; break; }
       const uint32_t base = smem_u32(smem + s * kStageBytes);
       mbar_expect_tx(full0 + 8 * s, kStageBytes);
       const int kc = (kb0 + i) * 32;
@@ -190,7 +151,7 @@ k_field_gemm(const __grid_constant__ GemmMaps maps, const __grid_constant__ Gemm
     for (int i = 0; i < A.nkb; ++i) {
       const int s = i % kGStages;
       const uint32_t ph = (uint32_t)(i / kGStages) & 1u;
-      if (!mbar_wait(full0 + 8 * s, ph)) { ok = false; break; }
+      if (!mbar_wait(full0 + 8 * s, ph, &g_tg_err, TG_EW_MMA)) { ok = false; break; }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint32_t base = smem_u32(smem + s * kStageBytes);
 #pragma unroll
@@ -211,7 +172,7 @@ k_field_gemm(const __grid_constant__ GemmMaps maps, const __grid_constant__ Gemm
   __syncwarp();
 
   // ---------------- epilogue: TMEM -> registers -> partial image
-  const bool got = mbar_wait(done, 0);
+  const bool got = mbar_wait(done, 0, &g_tg_err, TG_EW_MMA);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const int row = mt * 128 + warp * 32 + lane;
   float2* out = A.part + (size_t)sp * A.h * A.w + (size_t)row * A.w;
@@ -245,7 +206,7 @@ k_field_gemm(const __grid_constant__ GemmMaps maps, const __grid_constant__ Gemm
   // drain: a producer that issued loads must see them land before the CTA exits
   if (warp == 0 && lane == 0 && !got) {
     for (int i = (loads_issued > kGStages ? loads_issued - kGStages : 0); i < loads_issued; ++i)
-      mbar_wait(full0 + 8 * (i % kGStages), (uint32_t)(i / kGStages) & 1u);
+      mbar_wait(full0 + 8 * (i % kGStages), (uint32_t)(i / kGStages) & 1u, &g_tg_err, TG_EW_MMA);
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();

@@ -236,6 +236,49 @@ __device__ __forceinline__ double add_f64_f32(double b, float p) {
   return r;
 }
 
+// ---------------------------------------------------------------- mbarriers
+// Shared-memory mbarriers for TMA copies and tensor-core commits.  Every wait
+// is bounded: after kWaitCycles the caller gets false and the error word its
+// translation unit passes in receives the given bit.
+constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t a, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t a, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t a, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(a), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity, uint32_t* err,
+                                          uint32_t bit) {
+  const long long t0 = clock64();
+  for (uint32_t it = 0;; ++it) {
+    if (mbar_try(a, parity)) return true;
+    if ((it & 255u) == 255u && clock64() - t0 > kWaitCycles) {
+      atomicOr(err, bit);
+      return false;
+    }
+  }
+}
+
 // ---------------------------------------------------------------- ray ops
 struct RayS {
   float x, y, dx, dy, plv;  // plv: per-ray (varying) pathlength part
