@@ -60,6 +60,12 @@ struct BatchIO {
   double* raw;
 };
 
+// 4-byte asynchronous global -> shared copy (zero-filled when src_bytes = 0)
+__device__ __forceinline__ void cp_async4(uint32_t dst, const float* src, uint32_t src_bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src), "r"(src_bytes)
+               : "memory");
+}
+
 __device__ __forceinline__ float bt_warp_sum(float v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -255,10 +261,12 @@ template <int R>
 __global__ void __launch_bounds__(512, (R == 4 ? 1 : 2))  // R = 1, 2: <= 64 registers (32 warps per SM)
 k_batch(const uint8_t* __restrict__ plan, const __grid_constant__ BatchIO io,
         int32_t* __restrict__ counter, int32_t* __restrict__ done, double* __restrict__ partial,
-        double* __restrict__ moments) {
+        double* __restrict__ moments, int pf_off) {
   // dynamic shared memory: [warps][n_mom] per-warp float32 moments of the tile,
   // reused by the model's adjoint tail (moments + per-step products)
   extern __shared__ __align__(16) float wacc[];
+  float* pf = wacc + pf_off;  // input stages [2][4 fields][R][blockDim] float32
+  const uint32_t pf_base = (uint32_t)__cvta_generic_to_shared(pf);
   __shared__ int s_last;
   __shared__ __align__(16) FOp sops[TG_MAX_COMPONENTS];
   __shared__ int s_tile;
@@ -324,22 +332,49 @@ k_batch(const uint8_t* __restrict__ plan, const __grid_constant__ BatchIO io,
 #pragma unroll
     for (int j = 0; j < kRegBip; ++j) bsx[j] = bsy[j] = 0.f;
     const int cnt = T.count;
-    for (int it = 0; it < cnt; it += blockDim.x * R) {
+    const int per = blockDim.x * R;
+    // the next iteration's x, y, dx, dy arrive by cp.async (4-byte copies into
+    // this thread's own slots: no barrier) while this one computes; measured
+    // on the 512-model sweep: forward 0.217 -> 0.200 ms, forward + adjoint
+    // 0.250 -> 0.244 ms.  The targets, needed only after the chain, are plain
+    // loads whose latency the chain hides, and the inputs are re-read from
+    // the stage for the moments instead of being held in registers.
+    auto prefetch = [&](int it2, int st2) {
+#pragma unroll
+      for (int k = 0; k < R; ++k) {
+        const int id = it2 + (int)threadIdx.x + k * (int)blockDim.x;
+        const uint32_t sz = id < cnt ? 4u : 0u;
+        const int i = id < cnt ? id : 0;
+        const uint32_t b = pf_base + 4u * (uint32_t)((st2 * 4 * R + k) * (int)blockDim.x + (int)threadIdx.x);
+        const uint32_t fs = 4u * (uint32_t)(R * (int)blockDim.x);
+        cp_async4(b + 0 * fs, gx + i, sz);
+        cp_async4(b + 1 * fs, gy + i, sz);
+        cp_async4(b + 2 * fs, gdx + i, sz);
+        cp_async4(b + 3 * fs, gdy + i, sz);
+      }
+      asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    prefetch(0, 0);
+    for (int it = 0, st = 0; it < cnt; it += per, st ^= 1) {
       float x[R], y[R], dx[R], dy[R], pl[R], v0[R][4], tx[R], ty[R];
       uint32_t spos[R], sneg[R];  // biprism b: bit b set when sign(x) > 0 / < 0
       int idx[R];
       bool inr[R];
+      if (it + per < cnt) prefetch(it + per, st ^ 1);
+      else asm volatile("cp.async.commit_group;" ::: "memory");
+      asm volatile("cp.async.wait_group 1;" ::: "memory");
 #pragma unroll
       for (int k = 0; k < R; ++k) {
         idx[k] = it + (int)threadIdx.x + k * (int)blockDim.x;  // coalesced per k
         inr[k] = idx[k] < cnt;
-        const int i = inr[k] ? idx[k] : 0;
-        v0[k][0] = gx[i]; v0[k][1] = gy[i]; v0[k][2] = gdx[i]; v0[k][3] = gdy[i];
-        if (adj) {
+        const float* pb = pf + (st * 4 * R + k) * (int)blockDim.x + (int)threadIdx.x;
+        const int fsf = R * (int)blockDim.x;
+        x[k] = pb[0]; y[k] = pb[fsf]; dx[k] = pb[2 * fsf]; dy[k] = pb[3 * fsf];
+        if (adj) {  // needed only after the chain: the chain hides the load latency
+          const int i = inr[k] ? idx[k] : 0;
           tx[k] = gtx[i];
           ty[k] = gty[i];
         }
-        x[k] = v0[k][0]; y[k] = v0[k][1]; dx[k] = v0[k][2]; dy[k] = v0[k][3];
         pl[k] = 0.f;
         spos[k] = sneg[k] = 0u;
       }
@@ -414,6 +449,10 @@ k_batch(const uint8_t* __restrict__ plan, const __grid_constant__ BatchIO io,
       float lx[R], ly[R];
 #pragma unroll
       for (int k = 0; k < R; ++k) {
+        // inputs re-read from the stage (not held in registers through the chain)
+        const float* pb = pf + (st * 4 * R + k) * (int)blockDim.x + (int)threadIdx.x;
+        const int fsf = R * (int)blockDim.x;
+        v0[k][0] = pb[0]; v0[k][1] = pb[fsf]; v0[k][2] = pb[2 * fsf]; v0[k][3] = pb[3 * fsf];
         lx[k] = inr[k] ? 2.f * (x[k] - tx[k]) : 0.f;
         ly[k] = inr[k] ? 2.f * (y[k] - ty[k]) : 0.f;
 #pragma unroll
@@ -648,7 +687,13 @@ extern "C" int tg_batch_run(const void* plan_dev, const tg_batch_info* info, con
                           : 0;
   size_t dyn = (size_t)(block / 32) * mom * sizeof(float);
   if (tail > dyn) dyn = tail;
-  if (dyn > 48 * 1024) return TG_ERR_TOO_LARGE;
+  dyn = (dyn + 15) & ~(size_t)15;
+  const int pf_off = (int)(dyn / sizeof(float));
+  dyn += (size_t)2 * 4 * rays_per_thread * block * sizeof(float);
+  if (dyn > 200 * 1024) return TG_ERR_TOO_LARGE;
+  if (rays_per_thread == 1) cudaFuncSetAttribute(k_batch<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+  else if (rays_per_thread == 2) cudaFuncSetAttribute(k_batch<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+  else cudaFuncSetAttribute(k_batch<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
   int per_sm = 1;
   if (rays_per_thread == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<1>, block, dyn);
   else if (rays_per_thread == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<2>, block, dyn);
@@ -656,9 +701,9 @@ extern "C" int tg_batch_run(const void* plan_dev, const tg_batch_info* info, con
   if (per_sm < 1) per_sm = 1;
   int grid = sm_count_batch() * per_sm;
   if (grid > info->n_tiles) grid = info->n_tiles;
-  if (rays_per_thread == 1) k_batch<1><<<grid, block, dyn, s>>>(plan, A, counter, done, partial, moments);
-  else if (rays_per_thread == 2) k_batch<2><<<grid, block, dyn, s>>>(plan, A, counter, done, partial, moments);
-  else k_batch<4><<<grid, block, dyn, s>>>(plan, A, counter, done, partial, moments);
+  if (rays_per_thread == 1) k_batch<1><<<grid, block, dyn, s>>>(plan, A, counter, done, partial, moments, pf_off);
+  else if (rays_per_thread == 2) k_batch<2><<<grid, block, dyn, s>>>(plan, A, counter, done, partial, moments, pf_off);
+  else k_batch<4><<<grid, block, dyn, s>>>(plan, A, counter, done, partial, moments, pf_off);
   return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
 }
 
