@@ -577,12 +577,21 @@ def secondary_trace_large(torch, dev, hbm):
     ws = torch.empty(lib.tg_trace_vjp_workspace(n, C.byref(m)) + 256, dtype=torch.uint8, device=dev)
     sp = N.stream_ptr()
     fwd = lambda: lib.tg_trace_fwd(C.byref(m), C.byref(rin), C.byref(rout), None, None, None, None, None, 0, sp)  # noqa: E731
-    fwd_bin = lambda: lib.tg_trace_fwd(C.byref(m), C.byref(rin), C.byref(rout), None, C.byref(grid),  # noqa: E731
-                                       py.data_ptr(), px.data_ptr(), hist.data_ptr(), 1, sp)
+    ws_bytes = lib.tg_trace_image_workspace(n, C.byref(grid))
+    hws = torch.empty(max(ws_bytes, 16), dtype=torch.uint8, device=dev)
+    fwd_bin = lambda: lib.tg_trace_image(C.byref(m), C.byref(rin), C.byref(rout), None, C.byref(grid),  # noqa: E731
+                                         py.data_ptr(), px.data_ptr(), hist.data_ptr(), 1, hws.data_ptr(),
+                                         ws_bytes, sp)
+    fwd_bin_global = lambda: lib.tg_trace_fwd(C.byref(m), C.byref(rin), C.byref(rout), None,  # noqa: E731
+                                              C.byref(grid), py.data_ptr(), px.data_ptr(), hist.data_ptr(),
+                                              1, sp)
     vjp = lambda: lib.tg_trace_vjp(C.byref(m), C.byref(rin), C.byref(gout), C.byref(gin), raw.data_ptr(),  # noqa: E731
                                    ws.data_ptr(), ws.numel(), sp)
     res = {"workload": "fused chain, 16,777,216 rays, Lens + Detector 256x256"}
-    for name, fn, bpr in (("forward", fwd, 40), ("forward_pixels_histogram", fwd_bin, 48), ("adjoint", vjp, 48)):
+    res["histogram_path"] = ("per-SM shared-memory histograms (tg_trace_image)" if ws_bytes else
+                             "global atomics")
+    for name, fn, bpr in (("forward", fwd, 40), ("forward_pixels_histogram", fwd_bin, 48),
+                          ("forward_pixels_histogram_global_atomics", fwd_bin_global, 48), ("adjoint", vjp, 48)):
         ms = _time(torch, fn, 20)
         res[name] = {"ms": ms, "rays_per_s": n / (ms * 1e-3), "bytes_per_ray": bpr,
                      "achieved_gbs": n * bpr / (ms * 1e-3) / 1e9, "frac_of_hbm": n * bpr / (ms * 1e-3) / 1e9 / hbm}

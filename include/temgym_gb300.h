@@ -155,6 +155,23 @@ int tg_trace_fwd(const tg_model *model, const tg_rays *in, tg_rays *out,
                  int32_t *pix_x, void *hist, int32_t hist_i64, void *stream);
 
 /*
+ * tg_trace_image - tg_trace_fwd with a caller workspace for the histogram.
+ * Same replacement (run.py:85-116 + grid.py:120-153 + grid.py:231-280,
+ * Detector.into_image) and same results: the histogram is ADDED to.  When
+ * tg_trace_image_workspace(n, grid) is non-zero and workspace holds that many
+ * bytes (16-byte aligned device memory), each SM keeps a private copy of the
+ * detector in shared memory and the copies are summed at the end (one shared
+ * atomic per warp and bin instead of one global atomic); otherwise the call
+ * is tg_trace_fwd.  The workspace query is 0 for detectors above ~100k pixels
+ * or fewer than 32 rays per pixel, where global atomics are the better choice.
+ */
+size_t tg_trace_image_workspace(int64_t n, const tg_grid *grid);
+int tg_trace_image(const tg_model *model, const tg_rays *in, tg_rays *out,
+                   double *z_out, const tg_grid *grid, int32_t *pix_y,
+                   int32_t *pix_x, void *hist, int32_t hist_i64, void *workspace,
+                   size_t ws_bytes, void *stream);
+
+/*
  * tg_bin - metres->pixels + histogram for existing rays (no trace).
  * Replaces grid.py:120-153 and grid.py:231-280 (+ utils.py:83-114).
  * mask: optional device uint8 (0 = do not count), may be NULL.

@@ -61,6 +61,11 @@ _SIGS = {
     "tg_trace_fwd": (C.c_int, [C.POINTER(TgModel), C.POINTER(TgRays), C.POINTER(TgRays),
                                C.POINTER(C.c_double), C.POINTER(TgGrid), C.c_void_p,
                                C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
+    "tg_trace_image_workspace": (C.c_size_t, [C.c_int64, C.POINTER(TgGrid)]),
+    "tg_trace_image": (C.c_int, [C.POINTER(TgModel), C.POINTER(TgRays), C.POINTER(TgRays),
+                                 C.POINTER(C.c_double), C.POINTER(TgGrid), C.c_void_p,
+                                 C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_size_t,
+                                 C.c_void_p]),
     "tg_bin": (C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(TgGrid),
                          C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
     "tg_abcd_compose": (C.c_int, [C.POINTER(TgModel), C.POINTER(C.c_double),

@@ -116,12 +116,16 @@ def _fwd_launch(model, soa: _Soa, grid=None, want_pix=False, hist=None, want_amp
             px = torch.empty(n, dtype=torch.int32, device=dev)
     if hist is not None and hist.dtype not in (torch.int32, torch.int64):
         raise TypeError("histogram accumulator must be int32 or int64")
-    st = N.lib().tg_trace_fwd(C.byref(m), C.byref(soa.struct()), C.byref(out), C.byref(zout),
-                              C.byref(g) if g is not None else None, N.ptr(py), N.ptr(px),
-                              N.ptr(hist), 1 if (hist is not None and hist.dtype == torch.int64) else 0,
-                              N.stream_ptr())
+    lib = N.lib()
+    # many rays per pixel: per-SM shared-memory histograms summed at the end
+    ws_bytes = lib.tg_trace_image_workspace(n, C.byref(g)) if (hist is not None and g is not None) else 0
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev) if ws_bytes else None
+    st = lib.tg_trace_image(C.byref(m), C.byref(soa.struct()), C.byref(out), C.byref(zout),
+                            C.byref(g) if g is not None else None, N.ptr(py), N.ptr(px),
+                            N.ptr(hist), 1 if (hist is not None and hist.dtype == torch.int64) else 0,
+                            N.ptr(ws), ws_bytes, N.stream_ptr())
     del keep
-    N.check(st, "tg_trace_fwd")
+    N.check(st, "tg_trace_image")
     return ox, oy, odx, ody, opl, zout.value, oamp, py, px
 
 
@@ -468,10 +472,14 @@ class TracePlan:
         self.image = None
         self.pix = None
         self._g = None
+        self._ws, self._ws_bytes = None, 0
         if detector is not None:
             self._g = detector._tg_grid()
             h, w = int(detector.shape[0]), int(detector.shape[1])
             self.image = torch.zeros((h, w), dtype=hist_dtype, device=dev)
+            ws_bytes = N.lib().tg_trace_image_workspace(self.n, C.byref(self._g))
+            self._ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev) if ws_bytes else None
+            self._ws_bytes = ws_bytes
             if pixels:
                 self.pix = (torch.empty(self.n, dtype=torch.int32, device=dev),
                             torch.empty(self.n, dtype=torch.int32, device=dev))
@@ -480,12 +488,12 @@ class TracePlan:
 
     def run(self):
         pix = self.pix or (None, None)
-        st = self._lib.tg_trace_fwd(C.byref(self._m), C.byref(self._in), C.byref(self._o),
-                                    C.byref(self._zout), C.byref(self._g) if self._g is not None else None,
-                                    N.ptr(pix[0]), N.ptr(pix[1]), N.ptr(self.image),
-                                    1 if (self.image is not None and self.image.dtype == torch.int64) else 0,
-                                    N.stream_ptr())
-        N.check(st, "tg_trace_fwd")
+        st = self._lib.tg_trace_image(C.byref(self._m), C.byref(self._in), C.byref(self._o),
+                                      C.byref(self._zout), C.byref(self._g) if self._g is not None else None,
+                                      N.ptr(pix[0]), N.ptr(pix[1]), N.ptr(self.image),
+                                      1 if (self.image is not None and self.image.dtype == torch.int64) else 0,
+                                      N.ptr(self._ws), self._ws_bytes, N.stream_ptr())
+        N.check(st, "tg_trace_image")
         return self
 
     def capture(self):
