@@ -181,6 +181,31 @@ int tg_bin(int64_t n, const float *x, const float *y, const uint8_t *mask,
            int32_t hist_i64, void *stream);
 
 /*
+ * tg_hist_workspace - workspace bytes for the per-SM shared-memory histogram
+ * path of tg_trace_image, tg_bin_image and tg_hist_pixels: non-zero for
+ * detectors of at most 102,400 pixels with at least 32 rays per pixel, 0
+ * otherwise (the calls then use global atomics).  tg_trace_image_workspace
+ * is this query for a grid.
+ */
+size_t tg_hist_workspace(int64_t n, int32_t h, int32_t w);
+
+/* tg_bin_image - tg_bin with the histogram workspace (same results). */
+int tg_bin_image(int64_t n, const float *x, const float *y, const uint8_t *mask,
+                 const tg_grid *grid, int32_t *pix_y, int32_t *pix_x, void *hist,
+                 int32_t hist_i64, void *workspace, size_t ws_bytes, void *stream);
+
+/*
+ * tg_hist_pixels - histogram of existing integer pixel indices.
+ * Replaces grid.py:231-280 Detector.into_image given (pixels_y, pixels_x)
+ * (utils.py:83-114): indices outside [0, h) x [0, w) are dropped, the counts
+ * are ADDED to hist [h][w].  idx_i64: indices are int64 (else int32);
+ * hist_i64: counts are int64 (else int32).  workspace as tg_hist_workspace.
+ */
+int tg_hist_pixels(int64_t n, const void *pix_y, const void *pix_x, int32_t idx_i64,
+                   int32_t h, int32_t w, void *hist, int32_t hist_i64, void *workspace,
+                   size_t ws_bytes, void *stream);
+
+/*
  * tg_abcd_compose - float64 5x5 ABCD about a central ray, composed from the
  * per-step component matrices (host code, no GPU needed).
  * Replaces jax.jacobian(run_to_end) + utils.py:7-43 custom_jacobian_matrix

@@ -66,6 +66,12 @@ _SIGS = {
                                  C.POINTER(C.c_double), C.POINTER(TgGrid), C.c_void_p,
                                  C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_size_t,
                                  C.c_void_p]),
+    "tg_hist_workspace": (C.c_size_t, [C.c_int64, C.c_int32, C.c_int32]),
+    "tg_bin_image": (C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(TgGrid),
+                               C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_size_t,
+                               C.c_void_p]),
+    "tg_hist_pixels": (C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32,
+                                 C.c_void_p, C.c_int32, C.c_void_p, C.c_size_t, C.c_void_p]),
     "tg_bin": (C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(TgGrid),
                          C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
     "tg_abcd_compose": (C.c_int, [C.POINTER(TgModel), C.POINTER(C.c_double),

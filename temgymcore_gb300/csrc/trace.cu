@@ -248,12 +248,23 @@ struct BinArgs {
   int32_t *pix_y, *pix_x;
   void* hist;
   int32_t h, w;
+  uint32_t* rows;  // shared-histogram variant: per-CTA uint32 histograms
 };
 
-template <typename CountT>
-__global__ void __launch_bounds__(256)
+// kSh: the shared-memory histogram variant (as for k_trace_fwd).
+template <typename CountT, bool kSh = false>
+__global__ void __launch_bounds__(kSh ? kShThreads : 256)
 k_bin(const __grid_constant__ BinArgs A, const __grid_constant__ BinCoef B) {
+  extern __shared__ uint32_t shw[];
+  constexpr int kShFlush = 65535 / kShThreads;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int bins = A.h * A.w;
+  int since = 0;
+  bool first = true;
+  if (kSh) {
+    for (int i = threadIdx.x; i < ((bins + 1) >> 1); i += blockDim.x) shw[i] = 0u;
+    __syncthreads();
+  }
   for (int64_t blk = (int64_t)blockIdx.x * blockDim.x; blk < A.n; blk += stride) {
     const int64_t i = blk + threadIdx.x;
     const bool inr = i < A.n;
@@ -267,9 +278,49 @@ k_bin(const __grid_constant__ BinArgs A, const __grid_constant__ BinCoef B) {
     }
     if (A.hist) {
       bool ok = inr && (!A.mask || A.mask[i]) && py >= 0 && py < A.h && px >= 0 && px < A.w;
-      hist_add_warp<CountT>(reinterpret_cast<CountT*>(A.hist), ok ? py * A.w + px : 0, ok);
+      if (kSh) hist_add_warp_sh(shw, ok ? py * A.w + px : 0, ok);
+      else hist_add_warp<CountT>(reinterpret_cast<CountT*>(A.hist), ok ? py * A.w + px : 0, ok);
+    }
+    if (kSh && ++since == kShFlush) {  // block-uniform
+      sh_flush(shw, A.rows + (size_t)blockIdx.x * bins, bins, first);
+      since = 0;
+      first = false;
     }
   }
+  if (kSh && (since > 0 || first)) sh_flush(shw, A.rows + (size_t)blockIdx.x * bins, bins, first);
+}
+
+// Histogram of existing pixel indices (grid.py:231-280 into_image given
+// (py, px)): out-of-range indices are dropped.  kSh as for k_trace_fwd.
+template <typename IdxT, typename CountT, bool kSh = false>
+__global__ void __launch_bounds__(kSh ? kShThreads : 256)
+k_hist_pix(int64_t n, const IdxT* __restrict__ pix_y, const IdxT* __restrict__ pix_x, int h, int w,
+           CountT* __restrict__ hist, uint32_t* __restrict__ rows) {
+  extern __shared__ uint32_t shw[];
+  constexpr int kShFlush = 65535 / kShThreads;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int bins = h * w;
+  int since = 0;
+  bool first = true;
+  if (kSh) {
+    for (int i = threadIdx.x; i < ((bins + 1) >> 1); i += blockDim.x) shw[i] = 0u;
+    __syncthreads();
+  }
+  for (int64_t blk = (int64_t)blockIdx.x * blockDim.x; blk < n; blk += stride) {  // block-uniform
+    const int64_t i = blk + threadIdx.x;
+    const bool inr = i < n;
+    const long long py = inr ? (long long)pix_y[i] : -1, px = inr ? (long long)pix_x[i] : -1;
+    const bool ok = py >= 0 && py < h && px >= 0 && px < w;
+    const int bin = ok ? (int)(py * w + px) : 0;
+    if (kSh) hist_add_warp_sh(shw, bin, ok);
+    else hist_add_warp<CountT>(hist, bin, ok);
+    if (kSh && ++since == kShFlush) {
+      sh_flush(shw, rows + (size_t)blockIdx.x * bins, bins, first);
+      since = 0;
+      first = false;
+    }
+  }
+  if (kSh && (since > 0 || first)) sh_flush(shw, rows + (size_t)blockIdx.x * bins, bins, first);
 }
 
 static int sm_count() {
@@ -291,10 +342,14 @@ using namespace tg;
 
 // The shared-histogram variant applies to histograms of at most kShMaxBins
 // bins when there are enough rays per bin for the L2 atomics to dominate.
-static bool use_shared_hist(int64_t n, const tg_grid* grid) {
-  if (!grid || grid->h <= 0 || grid->w <= 0) return false;
-  const int64_t bins = (int64_t)grid->h * grid->w;
+static bool use_shared_hist(int64_t n, int64_t h, int64_t w) {
+  if (h <= 0 || w <= 0) return false;
+  const int64_t bins = h * w;
   return bins <= kShMaxBins && n >= 32 * bins;
+}
+
+static bool use_shared_hist(int64_t n, const tg_grid* grid) {
+  return grid && use_shared_hist(n, grid->h, grid->w);
 }
 
 // Opt a shared-histogram kernel into the full shared-memory budget, once per
@@ -306,9 +361,11 @@ static cudaError_t shared_hist_attr() {
   return done;
 }
 
-static size_t shared_hist_bytes(const tg_grid* grid) {
-  return (size_t)sm_count() * (size_t)grid->h * (size_t)grid->w * sizeof(uint32_t);
+static size_t shared_hist_bytes(int64_t h, int64_t w) {
+  return (size_t)sm_count() * (size_t)h * (size_t)w * sizeof(uint32_t);
 }
+
+static size_t shared_hist_bytes(const tg_grid* grid) { return shared_hist_bytes(grid->h, grid->w); }
 
 static int trace_fwd_impl(const tg_model* model, const tg_rays* in, tg_rays* out,
                           double* z_out, const tg_grid* grid, int32_t* pix_y,
@@ -428,17 +485,39 @@ extern "C" int tg_trace_image(const tg_model* model, const tg_rays* in, tg_rays*
                         ws_bytes, stream);
 }
 
-extern "C" int tg_bin(int64_t n, const float* x, const float* y, const uint8_t* mask,
-                      const tg_grid* grid, int32_t* pix_y, int32_t* pix_x, void* hist,
-                      int32_t hist_i64, void* stream) {
+static int bin_impl(int64_t n, const float* x, const float* y, const uint8_t* mask,
+                    const tg_grid* grid, int32_t* pix_y, int32_t* pix_x, void* hist,
+                    int32_t hist_i64, void* workspace, size_t ws_bytes, void* stream) {
   if (n < 0 || !grid || grid->h <= 0 || grid->w <= 0) return TG_ERR_INVALID;
   if (n > 0 && (!x || !y)) return TG_ERR_INVALID;
   if (n == 0) return TG_OK;
   BinArgs A;
+  std::memset(&A, 0, sizeof(A));
   A.n = n; A.x = x; A.y = y; A.mask = mask; A.pix_y = pix_y; A.pix_x = pix_x;
   A.hist = hist; A.h = grid->h; A.w = grid->w;
   BinCoef B = make_bincoef(grid);
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (hist && workspace && use_shared_hist(n, grid) && ws_bytes >= shared_hist_bytes(grid) &&
+      (reinterpret_cast<uintptr_t>(workspace) & 15) == 0) {
+    const int bins = grid->h * grid->w;
+    const size_t smem = (size_t)((bins + 1) / 2) * sizeof(uint32_t);
+    const int64_t need = (n + kShThreads - 1) / kShThreads;
+    const int blocks = (int)(need < sm_count() ? need : sm_count());
+    A.rows = reinterpret_cast<uint32_t*>(workspace);
+    cudaError_t e;
+    if (hist_i64) {
+      e = shared_hist_attr<k_bin<long long, true>>();
+      if (e == cudaSuccess) k_bin<long long, true><<<blocks, kShThreads, smem, s>>>(A, B);
+    } else {
+      e = shared_hist_attr<k_bin<int, true>>();
+      if (e == cudaSuccess) k_bin<int, true><<<blocks, kShThreads, smem, s>>>(A, B);
+    }
+    if (e != cudaSuccess || cudaGetLastError() != cudaSuccess) return TG_ERR_CUDA;
+    const int rb = (bins + 255) / 256;
+    if (hist_i64) k_hist_rows<long long><<<rb, 256, 0, s>>>(A.rows, blocks, bins, reinterpret_cast<long long*>(hist));
+    else k_hist_rows<int><<<rb, 256, 0, s>>>(A.rows, blocks, bins, reinterpret_cast<int*>(hist));
+    return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
+  }
   int64_t need = (n + 255) / 256;
   int per_sm = 1;
   if (hist_i64) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bin<long long>, 256, 0);
@@ -449,6 +528,65 @@ extern "C" int tg_bin(int64_t n, const float* x, const float* y, const uint8_t* 
   if (hist_i64) k_bin<long long><<<blocks, 256, 0, s>>>(A, B);
   else k_bin<int><<<blocks, 256, 0, s>>>(A, B);
   return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
+}
+
+extern "C" int tg_bin(int64_t n, const float* x, const float* y, const uint8_t* mask,
+                      const tg_grid* grid, int32_t* pix_y, int32_t* pix_x, void* hist,
+                      int32_t hist_i64, void* stream) {
+  return bin_impl(n, x, y, mask, grid, pix_y, pix_x, hist, hist_i64, nullptr, 0, stream);
+}
+
+extern "C" int tg_bin_image(int64_t n, const float* x, const float* y, const uint8_t* mask,
+                            const tg_grid* grid, int32_t* pix_y, int32_t* pix_x, void* hist,
+                            int32_t hist_i64, void* workspace, size_t ws_bytes, void* stream) {
+  return bin_impl(n, x, y, mask, grid, pix_y, pix_x, hist, hist_i64, workspace, ws_bytes, stream);
+}
+
+extern "C" size_t tg_hist_workspace(int64_t n, int32_t h, int32_t w) {
+  return use_shared_hist(n, h, w) ? shared_hist_bytes(h, w) : 0;
+}
+
+template <typename IdxT, typename CountT>
+static int hist_pix_launch(int64_t n, const void* py, const void* px, int h, int w, void* hist,
+                           void* workspace, size_t ws_bytes, cudaStream_t s) {
+  const IdxT* y = reinterpret_cast<const IdxT*>(py);
+  const IdxT* x = reinterpret_cast<const IdxT*>(px);
+  CountT* hh = reinterpret_cast<CountT*>(hist);
+  const int bins = h * w;
+  if (workspace && use_shared_hist(n, h, w) && ws_bytes >= shared_hist_bytes(h, w) &&
+      (reinterpret_cast<uintptr_t>(workspace) & 15) == 0) {
+    const size_t smem = (size_t)((bins + 1) / 2) * sizeof(uint32_t);
+    const int64_t need = (n + kShThreads - 1) / kShThreads;
+    const int blocks = (int)(need < sm_count() ? need : sm_count());
+    uint32_t* rows = reinterpret_cast<uint32_t*>(workspace);
+    const cudaError_t e = shared_hist_attr<k_hist_pix<IdxT, CountT, true>>();
+    if (e != cudaSuccess) return TG_ERR_CUDA;
+    k_hist_pix<IdxT, CountT, true><<<blocks, kShThreads, smem, s>>>(n, y, x, h, w, hh, rows);
+    if (cudaGetLastError() != cudaSuccess) return TG_ERR_CUDA;
+    k_hist_rows<CountT><<<(bins + 255) / 256, 256, 0, s>>>(rows, blocks, bins, hh);
+  } else {
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hist_pix<IdxT, CountT>, 256, 0);
+    if (per_sm < 1) per_sm = 1;
+    const int64_t need = (n + 255) / 256, cap = (int64_t)sm_count() * per_sm;
+    k_hist_pix<IdxT, CountT><<<(int)(need < cap ? need : cap), 256, 0, s>>>(n, y, x, h, w, hh, nullptr);
+  }
+  return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
+}
+
+extern "C" int tg_hist_pixels(int64_t n, const void* pix_y, const void* pix_x, int32_t idx_i64,
+                              int32_t h, int32_t w, void* hist, int32_t hist_i64, void* workspace,
+                              size_t ws_bytes, void* stream) {
+  if (n < 0 || h <= 0 || w <= 0 || !hist) return TG_ERR_INVALID;
+  if ((int64_t)h * w > 0x7fffffff) return TG_ERR_TOO_LARGE;
+  if (n > 0 && (!pix_y || !pix_x)) return TG_ERR_INVALID;
+  if (n == 0) return TG_OK;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (idx_i64)
+    return hist_i64 ? hist_pix_launch<long long, long long>(n, pix_y, pix_x, h, w, hist, workspace, ws_bytes, s)
+                    : hist_pix_launch<long long, int>(n, pix_y, pix_x, h, w, hist, workspace, ws_bytes, s);
+  return hist_i64 ? hist_pix_launch<int, long long>(n, pix_y, pix_x, h, w, hist, workspace, ws_bytes, s)
+                  : hist_pix_launch<int, int>(n, pix_y, pix_x, h, w, hist, workspace, ws_bytes, s);
 }
 
 // =====================================================================

@@ -392,22 +392,32 @@ def image_from(grid: Grid, ray, acc=None):
         raise ValueError(f"accumulator shape {tuple(acc.shape)} != grid shape {(h, w)}")
     if acc.dtype not in (torch.int32, torch.int64) or not acc.is_cuda or not acc.is_contiguous():
         raise TypeError("accumulator must be a contiguous int32/int64 CUDA tensor")
+    lib = N.lib()
     if isinstance(ray, Ray):
         n = ray.size
         xs = as_f32(ray.x, n, dev)
         ys = as_f32(ray.y, n, dev)
         g = grid._tg_grid()
-        N.check(N.lib().tg_bin(n, N.ptr(xs), N.ptr(ys), None, C.byref(g), None, None,
-                               N.ptr(acc), 1 if acc.dtype == torch.int64 else 0,
-                               N.stream_ptr()), "tg_bin")
+        ws_bytes = lib.tg_hist_workspace(n, h, w)
+        ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev) if ws_bytes else None
+        N.check(lib.tg_bin_image(n, N.ptr(xs), N.ptr(ys), None, C.byref(g), None, None,
+                                 N.ptr(acc), 1 if acc.dtype == torch.int64 else 0,
+                                 N.ptr(ws), ws_bytes, N.stream_ptr()), "tg_bin_image")
         return acc
-    # PixelsYX input: integer indices already computed
+    # PixelsYX input: integer indices already computed (int32 kept, others as int64)
     py, px = ray
-    py = torch.as_tensor(py, device=dev).reshape(-1).long()
-    px = torch.as_tensor(px, device=dev).reshape(-1).long()
-    ok = (py >= 0) & (py < h) & (px >= 0) & (px < w)
-    acc.view(-1).index_put_((py[ok] * w + px[ok],),
-                            torch.ones(int(ok.sum()), dtype=acc.dtype, device=dev), accumulate=True)
+    py = torch.as_tensor(py, device=dev).reshape(-1)
+    px = torch.as_tensor(px, device=dev).reshape(-1)
+    if py.numel() != px.numel():
+        raise ValueError("pixel index arrays differ in length")
+    idt = torch.int32 if (py.dtype == torch.int32 and px.dtype == torch.int32) else torch.int64
+    py, px = py.to(idt).contiguous(), px.to(idt).contiguous()
+    n = py.numel()
+    ws_bytes = lib.tg_hist_workspace(n, h, w)
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev) if ws_bytes else None
+    N.check(lib.tg_hist_pixels(n, N.ptr(py), N.ptr(px), 1 if idt == torch.int64 else 0, h, w,
+                               N.ptr(acc), 1 if acc.dtype == torch.int64 else 0, N.ptr(ws), ws_bytes,
+                               N.stream_ptr()), "tg_hist_pixels")
     return acc
 
 

@@ -93,3 +93,47 @@ def test_trace_image_workspace_policy(cuda):
     assert lib.tg_trace_image_workspace(1 << 24, C.byref(g_small)) > 0
     assert lib.tg_trace_image_workspace(65536, C.byref(g_small)) == 0   # few rays per pixel
     assert lib.tg_trace_image_workspace(1 << 26, C.byref(g_big)) == 0   # detector above the shared budget
+
+
+@pytest.mark.parametrize("idt", [torch.int32, torch.int64])
+def test_into_image_pixel_indices(cuda, idt):
+    """Detector.into_image given (py, px): tg_hist_pixels (shared-memory path
+    at this size, global atomics below it) equals a host bincount; indices
+    outside the detector, including beyond int32 for int64 input, are dropped."""
+    import temgymcore_gb300 as t
+    rng = np.random.default_rng(3)
+    det = t.Detector(z=1.0, pixel_size=(1e-5, 1e-5), shape=(40, 56))
+    for n in (1 << 21, 5000):
+        py = rng.integers(-3, 44, n)
+        px = rng.integers(-5, 60, n)
+        if idt == torch.int64:
+            py[::97] = 2 ** 33 + 5   # would wrap into range if narrowed to int32
+            px[::89] = -(2 ** 40)
+        acc = torch.full((40, 56), 2, dtype=torch.int64, device=cuda)
+        out = det.into_image((torch.tensor(py, dtype=idt), torch.tensor(px, dtype=idt)), acc)
+        ok = (py >= 0) & (py < 40) & (px >= 0) & (px < 56)
+        ref = np.bincount(py[ok] * 56 + px[ok], minlength=40 * 56).reshape(40, 56) + 2
+        assert np.array_equal(out.cpu().numpy(), ref), n
+
+
+def test_into_image_rays_shared_vs_global(cuda):
+    """Detector.into_image given rays (tg_bin_image, shared-memory path) equals
+    tg_bin (global atomics) and the oracle's binning of the same coordinates."""
+    import oracle
+    import temgymcore_gb300 as t
+    from temgymcore_gb300 import _native as N
+    rng = np.random.default_rng(4)
+    n = (1 << 21) + 7
+    det = t.Detector(z=1.0, pixel_size=(1e-5, 1e-5), shape=(48, 48))
+    x = torch.tensor(rng.normal(0, 1.5e-4, n).astype(np.float32), device=cuda)
+    y = torch.tensor(rng.normal(0, 1.5e-4, n).astype(np.float32), device=cuda)
+    assert N.lib().tg_hist_workspace(n, 48, 48) > 0
+    img = det.into_image(t.Ray(x=x, y=y, dx=0.0, dy=0.0, z=0.0, pathlength=0.0))
+    g = det._tg_grid()
+    ref_gl = torch.zeros((48, 48), dtype=torch.int64, device=cuda)
+    N.check(N.lib().tg_bin(n, N.ptr(x), N.ptr(y), None, C.byref(g), None, None, N.ptr(ref_gl), 1,
+                           N.stream_ptr()), "tg_bin")
+    assert torch.equal(img, ref_gl)
+    gd = {"pixel_size": (1e-5, 1e-5), "shape": (48, 48)}
+    py, px = oracle.metres_to_pixels(gd, x.cpu().numpy().astype(np.float64), y.cpu().numpy().astype(np.float64))
+    assert np.array_equal(img.cpu().numpy(), oracle.into_image(gd, py, px))
