@@ -470,6 +470,11 @@ def run_only(args):
                     z=0.0, pathlength=0.0)
         acc = torch.zeros((256, 256), dtype=torch.int64, device=dev)
         fn = lambda: t.trace_to_image(ray, model, acc=acc)  # noqa: E731
+    elif args.only in ("trace-forward", "trace-image", "trace-image-global", "trace-adjoint"):
+        calls = _trace_large_calls(torch, dev, args.rays or (1 << 24))
+        fn = calls[{"trace-forward": "forward", "trace-image": "forward_pixels_histogram",
+                    "trace-image-global": "forward_pixels_histogram_global_atomics",
+                    "trace-adjoint": "adjoint"}[args.only]]
     else:
         raise SystemExit(f"unknown --only {args.only}")
     for _ in range(args.warmup):
@@ -544,17 +549,17 @@ def secondary_batched(torch, dev, hbm):
             "plain_per_model_ms": ms_plain, "speedup_vs_plain_per_model": ms_plain / ms}
 
 
-def secondary_trace_large(torch, dev, hbm):
-    """The fused chain at 16,777,216 rays (Lens + Detector): forward with
-    pathlength (40 B/ray), forward + pixels + int64 histogram (48 B/ray), and
-    the adjoint with input gradients and per-step sums (48 B/ray), through
-    the C ABI on device buffers."""
+def _trace_large_calls(torch, dev, n):
+    """The fused chain (Lens + Detector 256x256) on n rays through the C ABI on
+    device buffers: callables for the forward with pathlength, the forward +
+    pixels + int64 histogram (shared-memory histograms when the workspace
+    query allows, and the global-atomic path), and the adjoint with input
+    gradients and per-step sums.  The returned dict keeps the buffers alive."""
     import ctypes as C
 
     from temgymcore_gb300 import _native as N
     from temgymcore_gb300.run import _rays_struct, pack_model
     from temgymcore_gb300.workloads import build_model
-    n = 1 << 24
     rng = np.random.default_rng(0)
     x, y = (torch.tensor(rng.uniform(-1e-3, 1e-3, n).astype(np.float32), device=dev) for _ in range(2))
     dx, dy = (torch.tensor(rng.normal(0, 1e-3, n).astype(np.float32), device=dev) for _ in range(2))
@@ -575,27 +580,41 @@ def secondary_trace_large(torch, dev, hbm):
     raw = torch.zeros((4, 4), dtype=torch.float64, device=dev)
     lib = N.lib()
     ws = torch.empty(lib.tg_trace_vjp_workspace(n, C.byref(m)) + 256, dtype=torch.uint8, device=dev)
-    sp = N.stream_ptr()
-    fwd = lambda: lib.tg_trace_fwd(C.byref(m), C.byref(rin), C.byref(rout), None, None, None, None, None, 0, sp)  # noqa: E731
     ws_bytes = lib.tg_trace_image_workspace(n, C.byref(grid))
     hws = torch.empty(max(ws_bytes, 16), dtype=torch.uint8, device=dev)
-    fwd_bin = lambda: lib.tg_trace_image(C.byref(m), C.byref(rin), C.byref(rout), None, C.byref(grid),  # noqa: E731
-                                         py.data_ptr(), px.data_ptr(), hist.data_ptr(), 1, hws.data_ptr(),
-                                         ws_bytes, sp)
-    fwd_bin_global = lambda: lib.tg_trace_fwd(C.byref(m), C.byref(rin), C.byref(rout), None,  # noqa: E731
-                                              C.byref(grid), py.data_ptr(), px.data_ptr(), hist.data_ptr(),
-                                              1, sp)
-    vjp = lambda: lib.tg_trace_vjp(C.byref(m), C.byref(rin), C.byref(gout), C.byref(gin), raw.data_ptr(),  # noqa: E731
-                                   ws.data_ptr(), ws.numel(), sp)
-    res = {"workload": "fused chain, 16,777,216 rays, Lens + Detector 256x256"}
-    res["histogram_path"] = ("per-SM shared-memory histograms (tg_trace_image)" if ws_bytes else
-                             "global atomics")
-    for name, fn, bpr in (("forward", fwd, 40), ("forward_pixels_histogram", fwd_bin, 48),
-                          ("forward_pixels_histogram_global_atomics", fwd_bin_global, 48), ("adjoint", vjp, 48)):
-        ms = _time(torch, fn, 20)
+    sp = N.stream_ptr()
+    return {
+        "forward": lambda: lib.tg_trace_fwd(C.byref(m), C.byref(rin), C.byref(rout), None, None, None, None,
+                                            None, 0, sp),
+        "forward_pixels_histogram": lambda: lib.tg_trace_image(
+            C.byref(m), C.byref(rin), C.byref(rout), None, C.byref(grid), py.data_ptr(), px.data_ptr(),
+            hist.data_ptr(), 1, hws.data_ptr(), ws_bytes, sp),
+        "forward_pixels_histogram_global_atomics": lambda: lib.tg_trace_fwd(
+            C.byref(m), C.byref(rin), C.byref(rout), None, C.byref(grid), py.data_ptr(), px.data_ptr(),
+            hist.data_ptr(), 1, sp),
+        "adjoint": lambda: lib.tg_trace_vjp(C.byref(m), C.byref(rin), C.byref(gout), C.byref(gin),
+                                            raw.data_ptr(), ws.data_ptr(), ws.numel(), sp),
+        "_shared_hist": ws_bytes > 0,
+        "_keep": (keep, x, y, dx, dy, o, opl, py, px, hist, g, gi, raw, ws, hws, rin, rout, gout, gin, grid),
+    }
+
+
+def secondary_trace_large(torch, dev, hbm):
+    """The fused chain at 16,777,216 rays (Lens + Detector): forward with
+    pathlength (40 B/ray), forward + pixels + int64 histogram (48 B/ray; per-SM
+    shared-memory histograms, and the global-atomic path beside it), and the
+    adjoint with input gradients and per-step sums (48 B/ray), through the C
+    ABI on device buffers."""
+    n = 1 << 24
+    calls = _trace_large_calls(torch, dev, n)
+    res = {"workload": "fused chain, 16,777,216 rays, Lens + Detector 256x256",
+           "histogram_path": ("per-SM shared-memory histograms (tg_trace_image)" if calls["_shared_hist"] else
+                              "global atomics")}
+    for name, bpr in (("forward", 40), ("forward_pixels_histogram", 48),
+                      ("forward_pixels_histogram_global_atomics", 48), ("adjoint", 48)):
+        ms = _time(torch, calls[name], 20)
         res[name] = {"ms": ms, "rays_per_s": n / (ms * 1e-3), "bytes_per_ray": bpr,
                      "achieved_gbs": n * bpr / (ms * 1e-3) / 1e9, "frac_of_hbm": n * bpr / (ms * 1e-3) / 1e9 / hbm}
-    del keep
     return res
 
 
@@ -776,7 +795,8 @@ def main():
                     help="skip the secondary workloads, e2e and CPU baseline")
     ap.add_argument("--only", default=None,
                     help="profile one workload alone: field-separable, field-direct, field-astig, "
-                         "field-fp64, field-input, field-input-astig, fit, batched, plain")
+                         "field-fp64, field-input, field-input-astig, fit, batched, plain, "
+                         "trace-forward, trace-image, trace-image-global, trace-adjoint (--rays N)")
     ap.add_argument("--beams", type=int, default=None)
     ap.add_argument("--rays", type=int, default=None)
     ap.add_argument("--models", type=int, default=None)
