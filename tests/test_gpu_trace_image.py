@@ -137,3 +137,29 @@ def test_into_image_rays_shared_vs_global(cuda):
     gd = {"pixel_size": (1e-5, 1e-5), "shape": (48, 48)}
     py, px = oracle.metres_to_pixels(gd, x.cpu().numpy().astype(np.float64), y.cpu().numpy().astype(np.float64))
     assert np.array_equal(img.cpu().numpy(), oracle.into_image(gd, py, px))
+
+
+def test_trace_plan_shared_hist_graph(cuda):
+    """TracePlan on the shared-memory histogram path (workspace held by the
+    plan) equals trace_to_image, and replays inside a CUDA graph."""
+    import temgymcore_gb300 as t
+    from temgymcore_gb300 import _native as N
+    rng = np.random.default_rng(8)
+    n = 1 << 22
+    model = [t.Lens(z=0.5, focal_length=0.2),
+             t.Detector(z=1.0, pixel_size=(1e-5, 1e-5), shape=(64, 64))]
+    xs = [torch.tensor((rng.uniform(-1, 1, n) * s).astype(np.float32), device=cuda)
+          for s in (8e-5, 8e-5, 8e-5, 8e-5)]
+    assert N.lib().tg_trace_image_workspace(n, C.byref(model[-1]._tg_grid())) > 0
+    out, pix, img = t.trace_to_image(t.Ray(x=xs[0], y=xs[1], dx=xs[2], dy=xs[3], z=0.0, pathlength=0.0),
+                                     model)
+    assert int(img.sum()) > n // 2
+    plan = t.TracePlan(model, *xs, detector=model[-1], pixels=True)
+    plan.run()
+    assert torch.equal(plan.image, img) and torch.equal(plan.pix[0], pix.y)
+    g = plan.capture()
+    plan.image.zero_()
+    g.replay()
+    g.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(plan.image, 2 * img)
