@@ -60,10 +60,11 @@ def _run(n, shape, spread, dtype=torch.int64, offset=0, prefill=0):
     return h_sh.cpu().numpy(), h_gl.cpu().numpy(), ref
 
 
-@pytest.mark.parametrize("shape", [(64, 64), (63, 65)])
+@pytest.mark.parametrize("shape", [(64, 64), (63, 65), (320, 320)])
 def test_trace_image_spread(cuda, shape):
-    n = (1 << 22) + 3
-    h_sh, h_gl, ref = _run(n, shape, spread=0.08)
+    # 320 x 320 = 102,400 pixels: the largest detector of the shared path (200 KB)
+    n = max((1 << 22) + 3, 33 * shape[0] * shape[1])
+    h_sh, h_gl, ref = _run(n, shape, spread=0.08 * shape[0] / 64)
     assert np.array_equal(h_sh, ref) and np.array_equal(h_gl, ref)
     assert ref.sum() > n // 2
 
