@@ -445,6 +445,18 @@ int tg_adam_step(double *theta, const double *grad, double *m, double *v, int64_
                  double lr, double beta1, double beta2, double eps, const double *scale,
                  const uint8_t *mask, void *stream);
 
+/*
+ * tg_stem_fit_step - one whole optimisation step in two launches:
+ * tg_stem_fit_loss_grad into out, then the tg_adam_step update of the 21
+ * parameters (theta updated in place, gradients out[1..21]), applied by the
+ * reduction block that completes the last output.  Same results as the two
+ * calls.  Replaces one step of an optax/Adam loop over jax.value_and_grad.
+ */
+int tg_stem_fit_step(const tg_stem_fit *cfg, double *theta, double *out, double *m, double *v,
+                     int64_t *t, double lr, double beta1, double beta2, double eps,
+                     const double *scale, const uint8_t *mask, void *workspace, size_t ws_bytes,
+                     void *stream);
+
 /* ---- Gaussian-beamlet detector field ----------------------------------- */
 /* Beamlets (GaussianRay, gaussian.py:113-177): central rays and beam shape,
  * all device arrays.  amplitude is complex64 (re, im pairs); waist_xy and

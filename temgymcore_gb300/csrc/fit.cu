@@ -13,10 +13,13 @@
 // scan step, M (4x4 row-major: rows x, y, dx, dy; cols spx, spy, stx, sty).
 // Loss = sum over probes and rays of |r_det - r_target|^2.
 //
-// k_stem_fit: one CTA per probe at a time; each thread runs the chain and its
-// hand-derived adjoint for its rays in registers, the CTA reduces the probe's
-// sums, and one thread applies the chain rule through the scan geometry in
-// float64.  Per-CTA partials are reduced in fixed order (deterministic).
+// k_stem_fit: one CTA per probe at a time; it derives the probe's scan
+// geometry in float64, each thread runs the chain and its hand-derived
+// adjoint for its rays in registers, and the CTA reduces the probe's sums.
+// k_fit_reduce applies the chain rule through the scan geometry in float64
+// and reduces in fixed order (deterministic); for a whole optimisation step
+// (tg_stem_fit_step) the block that completes the last output also applies
+// the Adam update, so a step is two launches.
 #include <cstring>
 
 #include "tg_common.cuh"
@@ -36,15 +39,39 @@ struct FitArgs {
   float *ox, *oy;        // forward mode outputs [n_probes][n] (may be NULL)
   const double* theta;
   double gap;
-  float4* shift;         // [n_probes] per-probe combined scanner+descanner shift
   double2* sp;           // [n_probes] scan position (x, y)
-  float* fpar;           // [4] D, Lp, 1/f, gap (float32 copies)
   double* psum;          // [n_probes][8] per-probe sums
-  double2* rot;          // [1] cos, sin of the scan rotation (written by k_fit_setup)
+  double2* rot;          // [1] cos, sin of the scan rotation (written by k_stem_fit)
   double* part;          // [kFitOut][kRedChunks] reduction partials
-  int32_t* cnt;          // [kFitOut] chunks counted per output (zeroed by k_fit_setup)
+  int32_t* cnt;          // [kFitOut + 1] chunks counted per output, outputs done
+                         // (zeroed by k_stem_fit before k_fit_reduce runs)
   int32_t forward_only;
+  // Adam hand-off (tg_stem_fit_step): the block of k_fit_reduce that
+  // completes the last output updates theta in place
+  int32_t adam;
+  double* theta_w;
+  double *m, *v;
+  int64_t* t;
+  double lr, b1, b2, eps;
+  const double* scale;
+  const uint8_t* mask;
 };
+
+// One Adam update of parameter i < n (the step counter tt already advanced):
+// gradients w.r.t. parameters normalised by their scale (Adam in relative
+// units); mask: 1 = parameter is fitted.
+__device__ __forceinline__ void adam_update(int i, double* theta, double g_raw, double* m, double* v,
+                                            double lr, double b1, double b2, double eps,
+                                            double c1, double c2, const double* scale,
+                                            const uint8_t* mask) {
+  if (mask && !mask[i]) return;
+  const double sc = scale ? scale[i] : 1.0;
+  const double g = g_raw * sc;
+  m[i] = b1 * m[i] + (1.0 - b1) * g;
+  v[i] = b2 * v[i] + (1.0 - b2) * g * g;
+  const double mh = m[i] / c1, vh = v[i] / c2;
+  theta[i] -= sc * lr * mh / (sqrt(vh) + eps);
+}
 
 __device__ __forceinline__ float warp_sumf(float v) {
 #pragma unroll
@@ -52,45 +79,47 @@ __device__ __forceinline__ float warp_sumf(float v) {
   return v;
 }
 
-// Scan geometry in float64, once per probe (and the float32 copies of the
-// distances / focal power once): the streaming kernel then issues no float64.
-__global__ void __launch_bounds__(256) k_fit_setup(const __grid_constant__ FitArgs A) {
-  __shared__ double cs[2];
+// One CTA per probe (grid-stride).  The CTA first derives, in float64, its
+// constants (float32 copies of the distances and the focal power, the scan
+// rotation) and its probe's scan position and combined Scanner + Descanner
+// shift (grid.py:155-182 ScanGrid map, the descan rows), so no separate
+// set-up launch runs; then the chain and its hand-derived adjoint per ray in
+// float32 registers; the probe's eight sums leave as float64.
+__global__ void __launch_bounds__(kFitThreads) k_stem_fit(const __grid_constant__ FitArgs A) {
+  __shared__ float wsum[kFitThreads / 32][8];
+  __shared__ float4 s_shift;
+  __shared__ float s_par[4];
+  __shared__ double s_rot[2];
+  // the reduction's counters, zeroed before it runs (stream order)
+  if (blockIdx.x == 0 && threadIdx.x <= kFitOut) A.cnt[threadIdx.x] = 0;
   if (threadIdx.x == 0) {
     double sr, cr;
     sincos(A.theta[3] * (3.141592653589793 / 180.0), &sr, &cr);
-    cs[0] = cr;
-    cs[1] = sr;
-    if (blockIdx.x == 0) {
-      A.rot[0] = make_double2(cr, sr);
-      A.fpar[0] = (float)A.theta[1];
-      A.fpar[1] = (float)(A.theta[2] - A.gap);
-      A.fpar[2] = (float)(1.0 / A.theta[0]);
-      A.fpar[3] = (float)A.gap;
-    }
+    s_rot[0] = cr;
+    s_rot[1] = sr;
+    s_par[0] = (float)A.theta[1];
+    s_par[1] = (float)(A.theta[2] - A.gap);
+    s_par[2] = (float)(1.0 / A.theta[0]);
+    s_par[3] = (float)A.gap;
+    if (blockIdx.x == 0) A.rot[0] = make_double2(cr, sr);
   }
-  if (blockIdx.x == 0 && threadIdx.x < kFitOut) A.cnt[threadIdx.x] = 0;
   __syncthreads();
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= A.n_probes) return;
-  const double cr = cs[0], sr = cs[1], step = A.theta[4];
-  const double u = (double)(p / A.cols) - 0.5 * (A.rows - 1), v = (double)(p % A.cols) - 0.5 * (A.cols - 1);
-  const double spx = step * (-sr * u + cr * v);
-  const double spy = -step * (cr * u + sr * v);
-  A.sp[p] = make_double2(spx, spy);
-  const double* M = A.theta + 5;
-  A.shift[p] = make_float4((float)(M[0] * spx + M[1] * spy), (float)(M[4] * spx + M[5] * spy),
-                           (float)(M[8] * spx + M[9] * spy), (float)(M[12] * spx + M[13] * spy));
-}
-
-// One CTA per probe (grid-stride): the chain and its hand-derived adjoint per
-// ray in float32 registers; the probe's eight sums leave as float64.
-__global__ void __launch_bounds__(kFitThreads) k_stem_fit(const __grid_constant__ FitArgs A) {
-  __shared__ float wsum[kFitThreads / 32][8];
-  const float D = A.fpar[0], Lp = A.fpar[1], invf = A.fpar[2], G = A.fpar[3];
+  const float D = s_par[0], Lp = s_par[1], invf = s_par[2], G = s_par[3];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int p = blockIdx.x; p < A.n_probes; p += gridDim.x) {
-    const float4 sh = A.shift[p];
+    __syncthreads();  // the previous probe's threads have read s_shift
+    if (threadIdx.x == 0) {
+      const double cr = s_rot[0], sr = s_rot[1], step = A.theta[4];
+      const double u = (double)(p / A.cols) - 0.5 * (A.rows - 1), v = (double)(p % A.cols) - 0.5 * (A.cols - 1);
+      const double spx = step * (-sr * u + cr * v);
+      const double spy = -step * (cr * u + sr * v);
+      A.sp[p] = make_double2(spx, spy);
+      const double* M = A.theta + 5;
+      s_shift = make_float4((float)(M[0] * spx + M[1] * spy), (float)(M[4] * spx + M[5] * spy),
+                            (float)(M[8] * spx + M[9] * spy), (float)(M[12] * spx + M[13] * spy));
+    }
+    __syncthreads();
+    const float4 sh = s_shift;
     // per-thread sums: loss, dL/dLp, dL/df, dL/dD, Gx, Gy, Gdx, Gdy
     float s[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     for (int i = threadIdx.x; i < A.n; i += blockDim.x) {
@@ -187,11 +216,37 @@ __global__ void __launch_bounds__(128) k_fit_reduce(const __grid_constant__ FitA
     s_last = atomicAdd(A.cnt + j, 1) == kRedChunks - 1;
   }
   __syncthreads();
-  if (s_last && threadIdx.x == 0) {
+  __shared__ int s_adam;
+  if (threadIdx.x == 0) {
+    s_adam = 0;
+    if (s_last) {
+      __threadfence();
+      double t = 0.0;
+      for (int c = 0; c < kRedChunks; ++c) t += __ldcg(A.part + j * kRedChunks + c);
+      out[j] = t;
+      // the block completing the last output runs the Adam update: every
+      // block has finished reading theta by then
+      if (A.adam) {
+        __threadfence();
+        s_adam = atomicAdd(A.cnt + kFitOut, 1) == kFitOut - 1;
+      }
+    }
+  }
+  __syncthreads();
+  if (s_adam) {
     __threadfence();
-    double t = 0.0;
-    for (int c = 0; c < kRedChunks; ++c) t += __ldcg(A.part + j * kRedChunks + c);
-    out[j] = t;
+    __shared__ double s_c[2];
+    __shared__ int64_t s_tt;
+    if (threadIdx.x == 0) {
+      s_tt = *A.t + 1;
+      s_c[0] = 1.0 - pow(A.b1, (double)s_tt);
+      s_c[1] = 1.0 - pow(A.b2, (double)s_tt);
+    }
+    __syncthreads();
+    if (threadIdx.x < kFitOut - 1)
+      adam_update(threadIdx.x, A.theta_w, __ldcg(out + 1 + threadIdx.x), A.m, A.v, A.lr, A.b1, A.b2,
+                  A.eps, s_c[0], s_c[1], A.scale, A.mask);
+    if (threadIdx.x == 0) *A.t = s_tt;
   }
 }
 
@@ -202,19 +257,15 @@ __global__ void k_adam(double* __restrict__ theta, const double* __restrict__ gr
                        double b2, double eps, const double* __restrict__ scale,
                        const uint8_t* __restrict__ mask) {
   __shared__ int64_t tt;
-  if (threadIdx.x == 0) tt = *t + 1;
+  __shared__ double c[2];
+  if (threadIdx.x == 0) {
+    tt = *t + 1;
+    c[0] = 1.0 - pow(b1, (double)tt);
+    c[1] = 1.0 - pow(b2, (double)tt);
+  }
   __syncthreads();
   const int i = threadIdx.x;
-  if (i < n && (!mask || mask[i])) {
-    // gradients w.r.t. parameters normalised by their scale (Adam in relative units)
-    const double sc = scale ? scale[i] : 1.0;
-    const double g = grad[i] * sc;
-    m[i] = b1 * m[i] + (1.0 - b1) * g;
-    v[i] = b2 * v[i] + (1.0 - b2) * g * g;
-    const double mh = m[i] / (1.0 - pow(b1, (double)tt));
-    const double vh = v[i] / (1.0 - pow(b2, (double)tt));
-    theta[i] -= sc * lr * mh / (sqrt(vh) + eps);
-  }
+  if (i < n) adam_update(i, theta, grad[i], m, v, lr, b1, b2, eps, c[0], c[1], scale, mask);
   __syncthreads();
   if (threadIdx.x == 0) *t = tt;
 }
@@ -232,8 +283,8 @@ static int fit_grid(int n_probes) {
   return g < n_probes ? g : (n_probes > 0 ? n_probes : 1);
 }
 
-// workspace: shift [n_probes] float4 | sp [n_probes] double2 | psum [n_probes][8] |
-// fpar[4] + rot (256 B) | part [kFitOut][kRedChunks] | cnt [kFitOut] (256 B)
+// workspace: reserved [n_probes] float4 | sp [n_probes] double2 | psum [n_probes][8] |
+// rot (256 B) | part [kFitOut][kRedChunks] | cnt [kFitOut + 1] (256 B)
 static size_t fit_ws(int32_t n_probes) {
   return (size_t)n_probes * (16 + 16 + 64) + 256 + kFitOut * kRedChunks * sizeof(double) + 256;
 }
@@ -264,10 +315,8 @@ static int fit_args(const tg_stem_fit* c, const double* theta, void* ws, size_t 
   A->theta = theta;
   A->gap = c->lens_gap;
   char* w = reinterpret_cast<char*>(ws);
-  A->shift = reinterpret_cast<float4*>(w);
   A->sp = reinterpret_cast<double2*>(w + (size_t)A->n_probes * 16);
   A->psum = reinterpret_cast<double*>(w + (size_t)A->n_probes * 32);
-  A->fpar = reinterpret_cast<float*>(w + (size_t)A->n_probes * 96);
   A->rot = reinterpret_cast<double2*>(w + (size_t)A->n_probes * 96 + 16);
   A->part = reinterpret_cast<double*>(w + (size_t)A->n_probes * 96 + 256);
   A->cnt = reinterpret_cast<int32_t*>(w + (size_t)A->n_probes * 96 + 256 + kFitOut * kRedChunks * sizeof(double));
@@ -284,7 +333,6 @@ extern "C" int tg_stem_fit_forward(const tg_stem_fit* cfg, const double* theta, 
   A.ox = det_x;
   A.oy = det_y;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-  k_fit_setup<<<(A.n_probes + 255) / 256, 256, 0, s>>>(A);
   k_stem_fit<<<fit_grid(A.n_probes), kFitThreads, 0, s>>>(A);
   return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
 }
@@ -296,7 +344,31 @@ extern "C" int tg_stem_fit_loss_grad(const tg_stem_fit* cfg, const double* theta
   if (st != TG_OK) return st;
   if (!out || (A.n > 0 && (!A.tx || !A.ty))) return TG_ERR_INVALID;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-  k_fit_setup<<<(A.n_probes + 255) / 256, 256, 0, s>>>(A);
+  k_stem_fit<<<fit_grid(A.n_probes), kFitThreads, 0, s>>>(A);
+  k_fit_reduce<<<dim3(kFitOut, kRedChunks), 128, 0, s>>>(A, out);
+  return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
+}
+
+extern "C" int tg_stem_fit_step(const tg_stem_fit* cfg, double* theta, double* out, double* m,
+                                double* v, int64_t* t, double lr, double beta1, double beta2,
+                                double eps, const double* scale, const uint8_t* mask,
+                                void* workspace, size_t ws_bytes, void* stream) {
+  FitArgs A;
+  int st = fit_args(cfg, theta, workspace, ws_bytes, &A);
+  if (st != TG_OK) return st;
+  if (!out || !m || !v || !t || (A.n > 0 && (!A.tx || !A.ty))) return TG_ERR_INVALID;
+  A.adam = 1;
+  A.theta_w = theta;
+  A.m = m;
+  A.v = v;
+  A.t = t;
+  A.lr = lr;
+  A.b1 = beta1;
+  A.b2 = beta2;
+  A.eps = eps;
+  A.scale = scale;
+  A.mask = mask;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   k_stem_fit<<<fit_grid(A.n_probes), kFitThreads, 0, s>>>(A);
   k_fit_reduce<<<dim3(kFitOut, kRedChunks), 128, 0, s>>>(A, out);
   return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;

@@ -4,9 +4,11 @@ rotation, scan step, focal length, defocus).
 The reference fits these by differentiating a loss over ``run_to_end`` with
 ``jax.grad`` (README.md:113-160) and stepping an optimiser on the host.  Here
 the parameters stay in device memory: one fused forward+adjoint kernel
-produces the loss and all 21 gradients (``tg_stem_fit_loss_grad``), an Adam
-kernel updates the parameters (``tg_adam_step``), and the pair is captured
-once in a CUDA graph and replayed for every optimisation step.
+produces the loss and all 21 gradients (``tg_stem_fit_loss_grad``), and a
+whole optimisation step (``tg_stem_fit_step``: the same pass, with the Adam
+update applied by the reduction's last block) is two launches, captured once
+in a CUDA graph and replayed for every step.  ``tg_adam_step`` alone updates
+from any gradient.
 """
 from __future__ import annotations
 
@@ -35,6 +37,10 @@ N.register("tg_stem_fit_loss_grad", C.c_int, [C.POINTER(TgStemFit), C.c_void_p, 
 N.register("tg_adam_step", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                      C.c_int32, C.c_double, C.c_double, C.c_double, C.c_double,
                                      C.c_void_p, C.c_void_p, C.c_void_p])
+N.register("tg_stem_fit_step", C.c_int, [C.POINTER(TgStemFit), C.c_void_p, C.c_void_p, C.c_void_p,
+                                         C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double,
+                                         C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t,
+                                         C.c_void_p])
 
 PARAM_NAMES = (["focal_length", "defocus", "camera_length", "scan_rotation", "scan_step"]
                + [f"M[{r}][{c}]" for r in range(4) for c in range(4)])
@@ -108,9 +114,14 @@ class StemFit:
                                      eps, self.scale.data_ptr(), self.mask.data_ptr(),
                                      N.stream_ptr()), "tg_adam_step")
 
-    def step(self, lr=1e-3):
-        self.loss_grad()
-        self.adam(lr)
+    def step(self, lr=1e-3, betas=(0.9, 0.999), eps=1e-8):
+        """loss_grad + adam in two launches (out holds the loss and gradient
+        at the parameters before the update)."""
+        N.check(N.lib().tg_stem_fit_step(C.byref(self._cfg()), self.theta.data_ptr(), self.out.data_ptr(),
+                                         self.m.data_ptr(), self.v.data_ptr(), self.t.data_ptr(), lr,
+                                         betas[0], betas[1], eps, self.scale.data_ptr(),
+                                         self.mask.data_ptr(), self.ws.data_ptr(), self.ws.numel(),
+                                         N.stream_ptr()), "tg_stem_fit_step")
 
     def capture(self, lr=1e-3):
         """Capture one loss/gradient/Adam step as a CUDA graph."""
@@ -121,8 +132,7 @@ class StemFit:
         torch.cuda.current_stream().wait_stream(s)
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g):
-            self.loss_grad()
-            self.adam(lr)
+            self.step(lr)
         self.graph = g
         return g
 

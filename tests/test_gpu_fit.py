@@ -104,3 +104,23 @@ def test_graph_replay_equals_eager_and_converges(cuda):
     # residual), not on recovering each parameter
     assert out[0] < 1e-4 * hist[0], (hist[0], out[0])
     assert np.all(np.isfinite(fa.theta.cpu().numpy()))
+
+
+def test_fused_step_equals_loss_grad_then_adam(cuda):
+    """tg_stem_fit_step (two launches, Adam in the reduction's last block)
+    gives bit-identical parameters, moments and outputs to tg_stem_fit_loss_grad
+    followed by tg_adam_step."""
+    w, fa = _setup(cuda, scan=(16, 16), rays=512)
+    _, fb = _setup(cuda, scan=(16, 16), rays=512)
+    sc = np.abs(w["theta0"])
+    sc[sc < 1e-2] = 1e-3
+    for f in (fa, fb):
+        f.scale.copy_(torch.as_tensor(sc))
+    for _ in range(5):
+        fa.step(lr=2e-3)
+        fb.loss_grad()
+        fb.adam(lr=2e-3)
+    torch.cuda.synchronize()
+    assert torch.equal(fa.theta, fb.theta)
+    assert torch.equal(fa.m, fb.m) and torch.equal(fa.v, fb.v) and torch.equal(fa.t, fb.t)
+    assert torch.equal(fa.out, fb.out)
