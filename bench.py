@@ -444,14 +444,14 @@ def run_only(args):
         meth = {"field-separable": "separable", "field-direct": "direct", "field-astig": "direct",
                 "field-fp64": "fp64"}[args.only]
         fn = lambda: plan.evaluate(meth)  # noqa: E731
-    elif args.only == "fit":
+    elif args.only in ("fit", "fit-step"):
         from temgymcore_gb300.fit import StemFit
         from temgymcore_gb300.workloads import stem_fit
         w = stem_fit(seed=0)
         fit = StemFit(t.Ray(x=w["x"], y=w["y"], dx=w["dx"], dy=w["dy"], z=0.0, pathlength=0.0),
                       w["rows"], w["cols"], w["gap"], w["theta0"])
         fit.set_targets(w["theta_true"])
-        fn = fit.loss_grad
+        fn = fit.loss_grad if args.only == "fit" else fit.step
     elif args.only == "batched":
         from temgymcore_gb300.batched import BatchedTrace
         from temgymcore_gb300.workloads import batched_sweep, build_model
@@ -795,7 +795,7 @@ def main():
                     help="skip the secondary workloads, e2e and CPU baseline")
     ap.add_argument("--only", default=None,
                     help="profile one workload alone: field-separable, field-direct, field-astig, "
-                         "field-fp64, field-input, field-input-astig, fit, batched, plain, "
+                         "field-fp64, field-input, field-input-astig, fit, fit-step, batched, plain, "
                          "trace-forward, trace-image, trace-image-global, trace-adjoint (--rays N)")
     ap.add_argument("--beams", type=int, default=None)
     ap.add_argument("--rays", type=int, default=None)

@@ -57,6 +57,17 @@ struct FitArgs {
   const uint8_t* mask;
 };
 
+// b^n (n >= 0) by repeated squaring: the Adam bias corrections in at most 63
+// float64 multiplies on the critical path instead of the pow library call.
+__device__ __forceinline__ double powi(double b, int64_t n) {
+  double r = 1.0;
+  for (; n > 0; n >>= 1) {
+    if (n & 1) r *= b;
+    b *= b;
+  }
+  return r;
+}
+
 // One Adam update of parameter i < n (the step counter tt already advanced):
 // gradients w.r.t. parameters normalised by their scale (Adam in relative
 // units); mask: 1 = parameter is fitted.
@@ -92,16 +103,18 @@ __global__ void __launch_bounds__(kFitThreads) k_stem_fit(const __grid_constant_
   __shared__ double s_rot[2];
   // the reduction's counters, zeroed before it runs (stream order)
   if (blockIdx.x == 0 && threadIdx.x <= kFitOut) A.cnt[threadIdx.x] = 0;
+  // two float64 chains in two warps, so they run side by side
   if (threadIdx.x == 0) {
     double sr, cr;
-    sincos(A.theta[3] * (3.141592653589793 / 180.0), &sr, &cr);
+    sincospi(A.theta[3] / 180.0, &sr, &cr);  // degrees: an exact argument reduction
     s_rot[0] = cr;
     s_rot[1] = sr;
+    if (blockIdx.x == 0) A.rot[0] = make_double2(cr, sr);
+  } else if (threadIdx.x == 32) {
     s_par[0] = (float)A.theta[1];
     s_par[1] = (float)(A.theta[2] - A.gap);
     s_par[2] = (float)(1.0 / A.theta[0]);
     s_par[3] = (float)A.gap;
-    if (blockIdx.x == 0) A.rot[0] = make_double2(cr, sr);
   }
   __syncthreads();
   const float D = s_par[0], Lp = s_par[1], invf = s_par[2], G = s_par[3];
@@ -239,8 +252,8 @@ __global__ void __launch_bounds__(128) k_fit_reduce(const __grid_constant__ FitA
     __shared__ int64_t s_tt;
     if (threadIdx.x == 0) {
       s_tt = *A.t + 1;
-      s_c[0] = 1.0 - pow(A.b1, (double)s_tt);
-      s_c[1] = 1.0 - pow(A.b2, (double)s_tt);
+      s_c[0] = 1.0 - powi(A.b1, s_tt);
+      s_c[1] = 1.0 - powi(A.b2, s_tt);
     }
     __syncthreads();
     if (threadIdx.x < kFitOut - 1)
@@ -260,8 +273,8 @@ __global__ void k_adam(double* __restrict__ theta, const double* __restrict__ gr
   __shared__ double c[2];
   if (threadIdx.x == 0) {
     tt = *t + 1;
-    c[0] = 1.0 - pow(b1, (double)tt);
-    c[1] = 1.0 - pow(b2, (double)tt);
+    c[0] = 1.0 - powi(b1, tt);
+    c[1] = 1.0 - powi(b2, tt);
   }
   __syncthreads();
   const int i = threadIdx.x;
