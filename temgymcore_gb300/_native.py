@@ -115,14 +115,27 @@ def check(status: int, what: str = "") -> None:
         raise RuntimeError(f"temgym_gb300 {what}: {STATUS.get(status, status)} (status {status})")
 
 
+_cuda_ok = False
+
+
 def require_cuda(t: torch.Tensor | None = None) -> None:
-    if not torch.cuda.is_available():
-        raise RuntimeError("temgymcore_gb300 needs a CUDA device (sm_103a); there is no CPU path")
+    global _cuda_ok
+    if not _cuda_ok:  # checked until it first succeeds (a per-call check costs microseconds)
+        if not torch.cuda.is_available():
+            raise RuntimeError("temgymcore_gb300 needs a CUDA device (sm_103a); there is no CPU path")
+        _cuda_ok = True
     if t is not None and not t.is_cuda:
         raise RuntimeError("temgymcore_gb300: tensors must live on the CUDA device")
 
 
+# the current stream's raw handle without building a Stream object (the
+# public call is the fallback where torch does not offer the raw one)
+_raw_stream = getattr(torch._C, "_cuda_getCurrentRawStream", None)
+
+
 def stream_ptr() -> int:
+    if _raw_stream is not None:
+        return _raw_stream(torch.cuda.current_device())
     return torch.cuda.current_stream().cuda_stream
 
 

@@ -302,9 +302,12 @@ extern "C" int tg_scan_hist(const tg_model* model, const tg_rays* bundle, const 
       return TG_ERR_INVALID;  // unregistered host memory
   }
   BinCoef B = make_bincoef(grid);
-  int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scan_hist, kScanThreads, 0);
-  if (per_sm < 1) per_sm = 1;
+  static int per_sm = 0;  // residency, queried once
+  if (!per_sm) {
+    int q = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, k_scan_hist, kScanThreads, 0);
+    per_sm = q > 0 ? q : 1;
+  }
   int blocks = sm_count_scan() * per_sm;
   if (blocks > kScanBands * scan->n_probes) blocks = kScanBands * scan->n_probes;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);

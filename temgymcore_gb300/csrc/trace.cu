@@ -38,7 +38,7 @@ struct FwdArgs {
 
 // Shared-histogram variant of the forward kernel: each CTA (kShThreads
 // threads, one per SM) keeps the whole detector in shared memory as uint16
-// counters packed in pairs, adds hits with warp-aggregated shared atomics, and
+// counters packed in pairs, adds each hit with one shared atomic, and
 // every kShFlush iterations (at most 65535 rays per CTA, so no counter can
 // wrap) adds the counters into its own uint32 row of the workspace; k_hist_rows
 // then sums the rows into the caller's histogram.  Global atomics (even
@@ -340,6 +340,17 @@ static inline bool al16(const void* p) { return (reinterpret_cast<uintptr_t>(p) 
 
 using namespace tg;
 
+template <auto Kernel>
+static int fwd_per_sm(int threads) {
+  static int v = 0;
+  if (!v) {
+    int q = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, Kernel, threads, 0);
+    v = q > 0 ? q : 1;
+  }
+  return v;
+}
+
 // The shared-histogram variant applies to histograms of at most kShMaxBins
 // bins when there are enough rays per bin for the L2 atomics to dominate.
 static bool use_shared_hist(int64_t n, int64_t h, int64_t w) {
@@ -444,15 +455,11 @@ static int trace_fwd_impl(const tg_model* model, const tg_rays* in, tg_rays* out
   int64_t blocks_needed = (A.n + (int64_t)threads * R - 1) / ((int64_t)threads * R);
   // every block resident at once: with the grid-stride loop each block has
   // the same share, so blocks waiting for a slot would lengthen the tail
-  int per_sm = 1;
-  if (vec) {
-    if (hist_i64) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_fwd<4, long long>, threads, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_fwd<4, int>, threads, 0);
-  } else {
-    if (hist_i64) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_fwd<1, long long>, threads, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_fwd<1, int>, threads, 0);
-  }
-  if (per_sm < 1) per_sm = 1;
+  // residency per variant, queried once (a per-call query costs host time)
+  const int per_sm = vec ? (hist_i64 ? fwd_per_sm<k_trace_fwd<4, long long>>(threads)
+                                     : fwd_per_sm<k_trace_fwd<4, int>>(threads))
+                         : (hist_i64 ? fwd_per_sm<k_trace_fwd<1, long long>>(threads)
+                                     : fwd_per_sm<k_trace_fwd<1, int>>(threads));
   int64_t cap = (int64_t)sm_count() * per_sm;
   int blocks = (int)(blocks_needed < cap ? blocks_needed : cap);
   if (vec) {

@@ -112,8 +112,8 @@ def _fwd_launch(model, soa: _Soa, grid=None, want_pix=False, hist=None, want_amp
     if grid is not None:
         g = grid._tg_grid()
         if want_pix:
-            py = torch.empty(n, dtype=torch.int32, device=dev)
-            px = torch.empty(n, dtype=torch.int32, device=dev)
+            pyx = torch.empty((2, n), dtype=torch.int32, device=dev)  # one allocation, two views
+            py, px = pyx[0], pyx[1]
     if hist is not None and hist.dtype not in (torch.int32, torch.int64):
         raise TypeError("histogram accumulator must be int32 or int64")
     lib = N.lib()
