@@ -2,10 +2,16 @@
 // (transfer.py:6-112): every ray through the cumulative products of a matrix
 // sequence, and a point source's fan through one matrix.
 //
-// Both are float64 on purpose (the reference's helpers are float64 NumPy /
-// JAX): 25 float64 multiply-adds per (ray, plane) against 40 written bytes
-// makes the transfer float64-pipe bound on GB300 (float64 is ~1/64 of the
-// float32 rate), not HBM bound.
+// The reference's helpers are float64 NumPy / JAX.  25 float64 multiply-adds
+// per (ray, plane) against 40 written bytes would make the transfer float64-
+// pipe bound on GB300 (float64 issues at ~1/64 of the float32 rate), so the
+// stack transfer runs in double-float arithmetic: every matrix entry and ray
+// component as an unevaluated float32 pair (hi + lo, 48 significant bits),
+// products with their exact rounding error (FMA), sums with TwoSum, and the
+// result rounded back to float64 with integer operations.  Errors stay at a
+// few 2^-47 of the sum of the term magnitudes; a ray or matrix with a nonzero
+// entry outside [2^-39, 2^62] (where a product's error term would leave the
+// normal float32 range) takes the float64 path.
 #include <cstring>
 
 #include "tg_common.cuh"
@@ -19,6 +25,97 @@ struct TransferMats {
   int32_t pad;
   double c[kMaxTransfer][25];  // cumulative products, row-major
 };
+
+// ---------------------------------------------------------------- double-float
+struct DF {
+  float h, l;
+};
+
+// a float64 value inside the double-float range (zero, or |v| in [2^-39, 2^62])
+__host__ __device__ inline bool df_range(double v) {
+  const double a = v < 0 ? -v : v;
+  return v == 0.0 || (a >= 1.8189894035458565e-12 && a <= 4.611686018427388e18);
+}
+
+__device__ __forceinline__ DF df_split(double v) {
+  const float h = __double2float_rn(v);
+  return DF{h, __double2float_rn(v - (double)h)};  // v - h is exact in float64
+}
+
+// a * b: the product of the heads with its exact rounding error, plus the
+// cross terms (lo * lo is below the precision kept)
+__device__ __forceinline__ DF df_mul(DF a, DF b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  return DF{p, e};
+}
+
+// a + b: TwoSum of the heads, the tails added to the error, renormalised
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+  const float s = __fadd_rn(a.h, b.h);
+  const float bb = __fsub_rn(s, a.h);
+  const float err = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(b.h, bb));
+  const float l = __fadd_rn(err, __fadd_rn(a.l, b.l));
+  const float h = __fadd_rn(s, l);
+  return DF{h, __fsub_rn(l, __fsub_rn(h, s))};
+}
+
+__device__ __forceinline__ double df_to_double(DF a) {
+  return add_f64_f32(f32_to_f64(a.h), a.l);
+}
+
+constexpr int kTrRays = 64;  // rays staged per block iteration
+
+// out[n][p][i] = sum_j C[p][i][j] ray[n][j] in double-float.  A block splits
+// the matrices into float32 pairs once, then per group of kTrRays rays stages
+// their split components in shared memory (the split is shared by all
+// planes) and runs one (ray, plane) pair per thread: a warp writes 32
+// consecutive 40-byte records.
+__global__ void __launch_bounds__(256)
+k_transfer_rays_df(const __grid_constant__ TransferMats T, int64_t n, const double* __restrict__ rays,
+                   double* __restrict__ out) {
+  extern __shared__ DF tsm[];  // [m * 25] matrix pairs, then [kTrRays * 5] ray pairs
+  __shared__ int s_ok[kTrRays];
+  const int m = T.m;
+  DF* mc = tsm;
+  DF* rv = tsm + m * 25;
+  for (int i = threadIdx.x; i < m * 25; i += blockDim.x) mc[i] = df_split((&T.c[0][0])[i]);
+  for (int64_t g = (int64_t)blockIdx.x * kTrRays; g < n; g += (int64_t)gridDim.x * kTrRays) {
+    const int nr = (int)((n - g) < kTrRays ? (n - g) : kTrRays);
+    __syncthreads();  // the previous group's pairs are done with rv / s_ok
+    for (int i = threadIdx.x; i < nr * 5; i += blockDim.x) rv[i] = df_split(rays[g * 5 + i]);
+    for (int i = threadIdx.x; i < nr; i += blockDim.x) {
+      const double* v = rays + (g + i) * 5;
+      s_ok[i] = df_range(v[0]) && df_range(v[1]) && df_range(v[2]) && df_range(v[3]) && df_range(v[4]);
+    }
+    __syncthreads();
+    const int pairs = nr * m;
+    for (int q = threadIdx.x; q < pairs; q += blockDim.x) {
+      const int r = q / m, p = q - r * m;
+      double* o = out + ((g + r) * m + p) * 5;
+      if (s_ok[r]) {
+        const DF* c = mc + p * 25;
+        const DF* v = rv + r * 5;
+#pragma unroll
+        for (int i = 0; i < 5; ++i) {
+          DF acc = df_mul(c[5 * i], v[0]);
+#pragma unroll
+          for (int j = 1; j < 5; ++j) acc = df_add(acc, df_mul(c[5 * i + j], v[j]));
+          o[i] = df_to_double(acc);
+        }
+      } else {  // outside the double-float range: float64
+        const double* v = rays + (g + r) * 5;
+        const double* c = T.c[p];
+#pragma unroll
+        for (int i = 0; i < 5; ++i)
+          o[i] = c[5 * i + 0] * v[0] + c[5 * i + 1] * v[1] + c[5 * i + 2] * v[2] +
+                 c[5 * i + 3] * v[3] + c[5 * i + 4] * v[4];
+      }
+    }
+  }
+}
 
 // out[n][p][i] = sum_j C[p][i][j] ray[n][j], one (ray, plane) pair per thread:
 // a warp writes 32 consecutive 40-byte records.
@@ -118,11 +215,22 @@ extern "C" int tg_transfer_rays(int64_t n, const double* rays, int32_t m, const 
   int st = tg_transfer_cumulative(m, matrices, &T.c[0][0]);
   if (st != TG_OK) return st;
   if (n == 0) return TG_OK;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  bool df = true;
+  for (int i = 0; i < m * 25 && df; ++i) df = df_range((&T.c[0][0])[i]);
+  if (df) {
+    const size_t smem = (size_t)(m * 25 + kTrRays * 5) * sizeof(DF);  // <= 26.6 KB
+    int64_t blocks = (n + kTrRays - 1) / kTrRays;
+    const int64_t cap = (int64_t)sm_count_transfer() * 8;
+    if (blocks > cap) blocks = cap;
+    k_transfer_rays_df<<<(int)blocks, 256, smem, s>>>(T, n, rays, out);
+    return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
+  }
   const int64_t total = n * (int64_t)m;
   int64_t blocks = (total + 255) / 256;
   const int64_t cap = (int64_t)sm_count_transfer() * 8;
   if (blocks > cap) blocks = cap;
-  k_transfer_rays<<<(int)blocks, 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(T, n, rays, out);
+  k_transfer_rays<<<(int)blocks, 256, 0, s>>>(T, n, rays, out);
   return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
 }
 

@@ -143,3 +143,37 @@ def test_dircos_rejected_by_batched_and_field(cuda):
     cnt = (C.c_int64 * 1)(16)
     info = TgBatchInfo()
     assert N.lib().tg_batch_plan(1, arr, cnt, None, 512, None, 0, C.byref(info)) == -2
+
+
+def test_transfer_rays_double_float_range_and_fallback(cuda):
+    """The double-float stack transfer against the float64 oracle at float64
+    tolerance, for rays spanning many binades; rays with a component outside
+    the double-float range ([2^-39, 2^62] or zero: tiny, huge) and matrices
+    with such an entry take the float64 path and are just as close."""
+    import temgymcore_gb300 as t
+    rng = np.random.default_rng(6)
+    n = 20000
+    rays = np.hstack([rng.normal(0, 1, (n, 4)) * 10.0 ** rng.uniform(-9, 3, (n, 4)), np.ones((n, 1))])
+    rays[:, :4][rng.random((n, 4)) < 0.05] = 0.0      # exact zeros
+    rays[::97, 0] = 3e-15                             # below 2^-39: float64 path
+    rays[::89, 2] = -7e20                             # above 2^62: float64 path
+    rays[::61, 1] = 2.0 ** -39                        # the range's ends: double-float
+    rays[::67, 3] = -(2.0 ** 62) / 1e6
+
+    def in_range(v):
+        a = np.abs(v)
+        return (v == 0) | ((a >= 2.0 ** -39) & (a <= 2.0 ** 62))
+
+    for scale in (1.0, 1e-14):                        # 1e-14: matrix entries outside the range
+        mats = np.eye(5) + rng.normal(0, 0.5, (16, 5, 5))
+        mats[:, 4, :] = [0, 0, 0, 0, 1]
+        mats[-1, 0, 1] = scale                        # cumulative[0] is the last matrix itself
+        cum = OT.accumulate_matrices_cumulative(mats)
+        assert bool(np.all(in_range(cum))) == (scale == 1.0)   # which path the call takes
+        got = np_(t.transfer_rays(rays, mats))
+        ref = OT.transfer_rays(rays, mats)
+        # per (ray, plane) record: error against the sum of the term magnitudes
+        mag = np.einsum("pij,nj->npi", np.abs(cum), np.abs(rays))
+        err = np.abs(got - ref)
+        assert np.all(err <= 1e-13 * mag), (scale, float(np.max(err / np.maximum(mag, 1e-300))))
+        np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-13 * np.abs(ref).max())
