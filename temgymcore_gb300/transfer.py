@@ -1,7 +1,9 @@
 """Transfer-matrix helpers (drop-in for temgym_core.transfer, transfer.py:6-183).
 
-``transfer_rays`` and ``transfer_rays_pt_src`` run on the GPU in float64
-(``csrc/transfer.cu``); ``accumulate_matrices`` and
+``transfer_rays`` (in double-float arithmetic: float32 pairs with exact
+product errors, results within 1e-13 of the sum of the term magnitudes;
+float64 for values outside [2^-39, 2^62]) and ``transfer_rays_pt_src``
+(float64) run on the GPU (``csrc/transfer.cu``); ``accumulate_matrices`` and
 ``accumulate_matrices_cumulative`` are host float64 products of a few 5x5
 matrices (the latter through the C ABI, in the reference's order).
 Outputs are float64 CUDA tensors.
