@@ -62,8 +62,25 @@ __device__ __forceinline__ DF df_add(DF a, DF b) {
   return DF{h, __fsub_rn(l, __fsub_rn(h, s))};
 }
 
+// hi + lo as a float64, faithfully rounded (within one float64 ulp: far below
+// the pair's own 2^-47), with a few integer operations.  For a renormalised
+// pair |lo| <= ulp32(hi) / 2, so in units of hi's float64 ulp lo is its
+// 24-bit significand shifted by sh = e_lo - e_hi + 29 <= 4, and the sum can
+// leave hi's binade only downwards and only when hi is a power of two: then
+// the grid below is twice as fine and lo counts double.  Zero, denormal and
+// non-finite parts take the general rounding.
 __device__ __forceinline__ double df_to_double(DF a) {
-  return add_f64_f32(f32_to_f64(a.h), a.l);
+  const uint32_t hb = __float_as_uint(a.h), lb = __float_as_uint(a.l);
+  const int eh = (int)((hb >> 23) & 0xffu), el = (int)((lb >> 23) & 0xffu);
+  if ((lb << 1) == 0u) return f32_to_f64(a.h);
+  if (eh == 0 || eh == 0xff || el == 0 || el == 0xff) return add_f64_f32(f32_to_f64(a.h), a.l);
+  const long long d = __double_as_longlong(f32_to_f64(a.h));
+  const uint32_t ml = (lb & 0x7fffffu) | 0x800000u;
+  const bool shrink = (hb >> 31) != (lb >> 31);  // lo reduces hi's magnitude
+  int sh = el - eh + 29;
+  if (shrink && (d & 0xfffffffffffffLL) == 0) ++sh;  // below a power of two: half-ulp grid
+  const long long n = sh >= 0 ? (long long)ml << sh : (sh > -25 ? (long long)(ml >> -sh) : 0LL);
+  return __longlong_as_double(d + (shrink ? -n : n));
 }
 
 constexpr int kTrRays = 64;  // rays staged per block iteration
