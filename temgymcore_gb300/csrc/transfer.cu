@@ -52,14 +52,20 @@ __device__ __forceinline__ DF df_mul(DF a, DF b) {
   return DF{p, e};
 }
 
-// a + b: TwoSum of the heads, the tails added to the error, renormalised
+// a + b: TwoSum of the heads, the tails added to the error; the pair is
+// left unrenormalised (a short sum of products stays within a few 2^-47 of
+// the term magnitudes) and df_norm is applied once per result
 __device__ __forceinline__ DF df_add(DF a, DF b) {
   const float s = __fadd_rn(a.h, b.h);
   const float bb = __fsub_rn(s, a.h);
   const float err = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(b.h, bb));
-  const float l = __fadd_rn(err, __fadd_rn(a.l, b.l));
-  const float h = __fadd_rn(s, l);
-  return DF{h, __fsub_rn(l, __fsub_rn(h, s))};
+  return DF{s, __fadd_rn(err, __fadd_rn(a.l, b.l))};
+}
+
+// Fast2Sum renormalisation: |lo| <= ulp(hi) / 2 afterwards
+__device__ __forceinline__ DF df_norm(DF a) {
+  const float h = __fadd_rn(a.h, a.l);
+  return DF{h, __fsub_rn(a.l, __fsub_rn(h, a.h))};
 }
 
 // hi + lo as a float64, faithfully rounded (within one float64 ulp: far below
@@ -120,7 +126,7 @@ k_transfer_rays_df(const __grid_constant__ TransferMats T, int64_t n, const doub
           DF acc = df_mul(c[5 * i], v[0]);
 #pragma unroll
           for (int j = 1; j < 5; ++j) acc = df_add(acc, df_mul(c[5 * i + j], v[j]));
-          o[i] = df_to_double(acc);
+          o[i] = df_to_double(df_norm(acc));
         }
       } else {  // outside the double-float range: float64
         const double* v = rays + (g + r) * 5;
