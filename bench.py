@@ -470,6 +470,12 @@ def run_only(args):
                     z=0.0, pathlength=0.0)
         acc = torch.zeros((256, 256), dtype=torch.int64, device=dev)
         fn = lambda: t.trace_to_image(ray, model, acc=acc)  # noqa: E731
+    elif args.only == "transfer":
+        rng = np.random.default_rng(0)
+        n, m = args.rays or (1 << 20), 16
+        rays = torch.tensor(np.hstack([rng.normal(0, 1e-3, (n, 4)), np.ones((n, 1))]), device=dev)
+        mats = rng.normal(0, 1, (m, 5, 5))
+        fn = lambda: t.transfer_rays(rays, mats)  # noqa: E731
     elif args.only in ("trace-forward", "trace-image", "trace-image-global", "trace-adjoint"):
         calls = _trace_large_calls(torch, dev, args.rays or (1 << 24))
         fn = calls[{"trace-forward": "forward", "trace-image": "forward_pixels_histogram",
@@ -796,7 +802,7 @@ def main():
     ap.add_argument("--only", default=None,
                     help="profile one workload alone: field-separable, field-direct, field-astig, "
                          "field-fp64, field-input, field-input-astig, fit, fit-step, batched, plain, "
-                         "trace-forward, trace-image, trace-image-global, trace-adjoint (--rays N)")
+                         "trace-forward, trace-image, trace-image-global, trace-adjoint, transfer (--rays N)")
     ap.add_argument("--beams", type=int, default=None)
     ap.add_argument("--rays", type=int, default=None)
     ap.add_argument("--models", type=int, default=None)
