@@ -335,6 +335,48 @@ int tg_decompose_q_inv(int64_t n, const double *q_inv, const double *wavelength,
                        double wavelength_scalar, double eps, double *waist, double *radii,
                        double *theta, void *stream);
 
+/*
+ * tg_beam_q_inv - GaussianRay.q_inv and .Q_inv (gaussian.py:138-177) for n
+ * beams: waist, radii (device float64 [n][2]; an infinite radius is a flat
+ * wavefront), wavelength / theta (device float64 [n] or NULL = the scalar)
+ * -> q_xy (device complex128 [n][2]: 1/qx, 1/qy; or NULL) and q_inv (device
+ * complex128 [n][2][2] = R(theta) diag(1/qx, 1/qy) R(theta)^T; or NULL).
+ */
+int tg_beam_q_inv(int64_t n, const double *waist, const double *radii, const double *wavelength,
+                  double wavelength_scalar, const double *theta, double theta_scalar,
+                  double *q_xy, double *q_inv, void *stream);
+
+/*
+ * tg_qinv_abcd - Qinv_ABCD (gaussian.py:92-96) for n systems:
+ * out = (A + B Q)^-1 (C + D Q), q_inv and out device complex128 [n][2][2],
+ * A, B, C, D device float64 [n][2][2].  Solved by 2x2 LU with partial
+ * pivoting, as linalg.solve does; a singular A + B Q gives inf / nan.
+ */
+int tg_qinv_abcd(int64_t n, const double *q_inv, const double *a, const double *b, const double *c,
+                 const double *d, double *out, void *stream);
+
+/*
+ * tg_beam_profile - the Gaussian-beam helpers (gaussian.py:13-28, 99-109)
+ * elementwise over n entries (device float64 [n] inputs, NULL where unused):
+ *   z_r   = zR(w0, wavelength), or the given z_r_in copied;
+ *   w_z   = w_z(w0, z, zR) and r = R(z, zR), with zR = z_r_in when given,
+ *           else zR(w0, wavelength);
+ *   q_inv = q_inv(z, w0, wavelength) (complex128 [n]; z_r_in must be NULL).
+ * Each output may be NULL; an output whose inputs are missing is
+ * TG_ERR_INVALID.  |z| < 1e-10 is the focus (R = inf).
+ */
+int tg_beam_profile(int64_t n, const double *z, const double *w0, const double *wavelength,
+                    const double *z_r_in, double *z_r, double *w_z, double *r, double *q_inv,
+                    void *stream);
+
+/*
+ * tg_gaussian_beam - gaussian_beam (gaussian.py:31-32) elementwise:
+ * out = exp(1j k ((x + offset_x)^2 + (y + offset_y)^2) / 2 q_inv); x, y, k,
+ * offsets device float64 [n], q_inv and out device complex128 [n].
+ */
+int tg_gaussian_beam(int64_t n, const double *x, const double *y, const double *q_inv, const double *k,
+                     const double *offset_x, const double *offset_y, double *out, void *stream);
+
 /* ---- many models in one persistent launch ------------------------------ */
 typedef struct tg_batch_info {
   size_t plan_bytes;       /* bytes of the packed plan (copy it to the device) */

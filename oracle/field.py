@@ -4,6 +4,8 @@ Follows:
   - ``GaussianRay.q_inv`` / ``Q_inv``            gaussian.py:138-177
     (Q_inv = R(theta) diag(1/q) R(theta)^T via the einsum at gaussian.py:221-222)
   - ``Qinv_ABCD``                                gaussian.py:92-96
+  - ``zR``, ``w_z``, ``R``, ``q_inv(z, w0, wl)``, ``gaussian_beam``
+                                                 gaussian.py:13-32, 99-109
   - ``make_gaussian_image``                      gaussian.py:225-273
   - ``_beam_field``                              gaussian.py:276-316
   - ``propagate_misaligned_gaussian_jax_scan``   gaussian.py:319-337
@@ -73,6 +75,42 @@ def inv2(m):
 def Qinv_ABCD(q1, A, B, C, D):
     """gaussian.py:92-96: solve(A + B Q1, C + D Q1)."""
     return inv2(A + B @ q1) @ (C + D @ q1)
+
+
+def zR(w0, wavelength):
+    """gaussian.py:17-18: Rayleigh range pi w0^2 / wavelength."""
+    return (np.pi * np.asarray(w0, np.float64) ** 2) / wavelength
+
+
+def w_z(w0, z, z_r):
+    """gaussian.py:13-14: beam radius at distance z from the waist."""
+    return w0 * np.sqrt(1 + (np.asarray(z, np.float64) / z_r) ** 2)
+
+
+def R_of_z(z, z_r):
+    """gaussian.py:21-28: wavefront radius z (1 + (z_r / z)^2); infinite for
+    |z| < 1e-10 (elementwise here; the reference's lax.cond takes a scalar)."""
+    z = np.asarray(z, np.float64)
+    focus = np.abs(z) < 1e-10
+    with np.errstate(divide="ignore", invalid="ignore"):
+        ratio = np.where(focus, 0.0, z_r / np.where(focus, 1.0, z))
+        return np.where(focus, np.inf, z * (1 + ratio ** 2))
+
+
+def q_inv_z(z, w0, wl):
+    """gaussian.py:99-109: 1/q of a beam of waist w0 at distance z."""
+    z_r = zR(w0, wl)
+    focus = np.abs(np.asarray(z, np.float64)) < 1e-10
+    wz = w_z(w0, z, z_r)
+    r = R_of_z(z, z_r)
+    with np.errstate(divide="ignore"):
+        return np.where(focus, 1j * wl / (np.pi * np.asarray(w0, np.float64) ** 2),
+                        -(1.0 / r) + 1j * wl / (np.pi * wz ** 2))
+
+
+def gaussian_beam(x, y, q, k, offset_x=0, offset_y=0):
+    """gaussian.py:31-32: exp(1j k ((x + ox)^2 + (y + oy)^2) / 2 q)."""
+    return np.exp(1j * k * ((np.asarray(x, np.float64) + offset_x) ** 2 + (y + offset_y) ** 2) / 2 * q)
 
 
 def beam_abcd(x, y, dx, dy, z, model):

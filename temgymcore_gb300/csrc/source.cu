@@ -14,6 +14,15 @@
 //                       generator), and exactly the requested count.
 //   k_decompose_q       gaussian.py:35-89 decompose_Q_inv for a batch of
 //                       2x2 complex Q^-1: waists, radii, rotation.
+//   k_beam_q_inv        the other direction, GaussianRay.q_inv / Q_inv
+//                       (gaussian.py:138-177): per-axis 1/q and
+//                       R(theta) diag(1/qx, 1/qy) R(theta)^T.
+//   k_qinv_abcd         Qinv_ABCD (gaussian.py:92-96): (A + B Q)^-1 (C + D Q)
+//                       by 2x2 LU with partial pivoting, as the reference's
+//                       linalg.solve does it.
+//   k_beam_profile      the textbook helpers zR, w_z, R, q_inv(z, w0, wl)
+//                       (gaussian.py:13-28, 99-109) elementwise.
+//   k_gaussian_beam     gaussian_beam (gaussian.py:31-32) elementwise.
 #include <cmath>
 #include <cstring>
 
@@ -208,6 +217,163 @@ __global__ void __launch_bounds__(128) k_decompose_q(const __grid_constant__ Dec
   A.theta[b] = atan2(v[1][0], v[0][0]);
 }
 
+// ---------------------------------------------------------------- Q^-1 of beams
+// Complex float64 with the products written out; the reference's einsum adds
+// the same terms (R diag R^T has two non-zero terms per entry).
+struct BeamQArgs {
+  int64_t n;
+  const double* waist;  // [n][2]
+  const double* radii;  // [n][2]
+  const double* wl;     // [n] or NULL (wl_scalar)
+  double wl_scalar;
+  const double* theta;  // [n] or NULL (theta_scalar)
+  double theta_scalar;
+  double* qxy;          // [n][2] complex128, or NULL
+  double* q;            // [n][2][2] complex128, or NULL
+};
+
+__global__ void __launch_bounds__(128) k_beam_q_inv(const __grid_constant__ BeamQArgs A) {
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= A.n) return;
+  const double PI = 3.141592653589793;
+  const double wl = A.wl ? A.wl[b] : A.wl_scalar;
+  double re[2], im[2];
+  for (int k = 0; k < 2; ++k) {
+    const double w = A.waist[2 * b + k], r = A.radii[2 * b + k];
+    im[k] = wl / (PI * (w * w));
+    re[k] = isinf(r) ? 0.0 : -1.0 / r;
+  }
+  if (A.qxy) {
+    A.qxy[4 * b + 0] = re[0]; A.qxy[4 * b + 1] = im[0];
+    A.qxy[4 * b + 2] = re[1]; A.qxy[4 * b + 3] = im[1];
+  }
+  if (A.q) {
+    double s, c;
+    sincos(A.theta ? A.theta[b] : A.theta_scalar, &s, &c);
+    // R = [[c, -s], [s, c]]:  (R D R^T)_ip = R_i0 d0 R_p0 + R_i1 d1 R_p1
+    const double R[2][2] = {{c, -s}, {s, c}};
+    double* o = A.q + 8 * b;
+    for (int i = 0; i < 2; ++i)
+      for (int p = 0; p < 2; ++p) {
+        const double a0 = R[i][0] * R[p][0], a1 = R[i][1] * R[p][1];
+        o[4 * i + 2 * p + 0] = a0 * re[0] + a1 * re[1];
+        o[4 * i + 2 * p + 1] = a0 * im[0] + a1 * im[1];
+      }
+  }
+}
+
+// ---------------------------------------------------------------- Qinv_ABCD
+struct zc {
+  double re, im;
+};
+__device__ __forceinline__ zc zadd(zc a, zc b) { return zc{a.re + b.re, a.im + b.im}; }
+__device__ __forceinline__ zc zsub(zc a, zc b) { return zc{a.re - b.re, a.im - b.im}; }
+__device__ __forceinline__ zc zmul(zc a, zc b) { return zc{a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
+// Smith's complex division (Smith 1962): scales by the larger component of
+// the divisor, so no intermediate overflows where the quotient does not.
+__device__ __forceinline__ zc zdiv(zc a, zc b) {
+  if (fabs(b.re) >= fabs(b.im)) {
+    const double r = b.im / b.re, d = b.re + b.im * r;
+    return zc{(a.re + a.im * r) / d, (a.im - a.re * r) / d};
+  }
+  const double r = b.re / b.im, d = b.re * r + b.im;
+  return zc{(a.re * r + a.im) / d, (a.im * r - a.re) / d};
+}
+__device__ __forceinline__ double cabs1(zc a) { return fabs(a.re) + fabs(a.im); }
+
+struct QabcdArgs {
+  int64_t n;
+  const double* q;                // [n][2][2] complex128
+  const double *a, *b, *c, *d;    // [n][2][2] float64
+  double* out;                    // [n][2][2] complex128
+};
+
+__global__ void __launch_bounds__(128) k_qinv_abcd(const __grid_constant__ QabcdArgs A) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= A.n) return;
+  zc Q[2][2];
+  for (int i = 0; i < 2; ++i)
+    for (int j = 0; j < 2; ++j) Q[i][j] = zc{A.q[8 * t + 4 * i + 2 * j], A.q[8 * t + 4 * i + 2 * j + 1]};
+  const double *a = A.a + 4 * t, *b = A.b + 4 * t, *c = A.c + 4 * t, *d = A.d + 4 * t;
+  zc L[2][2], Rh[2][2];  // lhs = A + B Q, rhs = C + D Q
+  for (int i = 0; i < 2; ++i)
+    for (int j = 0; j < 2; ++j) {
+      zc bq = zadd(zmul(zc{b[2 * i], 0.0}, Q[0][j]), zmul(zc{b[2 * i + 1], 0.0}, Q[1][j]));
+      zc dq = zadd(zmul(zc{d[2 * i], 0.0}, Q[0][j]), zmul(zc{d[2 * i + 1], 0.0}, Q[1][j]));
+      L[i][j] = zadd(zc{a[2 * i + j], 0.0}, bq);
+      Rh[i][j] = zadd(zc{c[2 * i + j], 0.0}, dq);
+    }
+  // LU with partial pivoting on |re| + |im| (the LAPACK getrf pivot rule)
+  if (cabs1(L[1][0]) > cabs1(L[0][0])) {
+    for (int j = 0; j < 2; ++j) {
+      zc s = L[0][j]; L[0][j] = L[1][j]; L[1][j] = s;
+      s = Rh[0][j]; Rh[0][j] = Rh[1][j]; Rh[1][j] = s;
+    }
+  }
+  const zc l10 = zdiv(L[1][0], L[0][0]);
+  const zc u11 = zsub(L[1][1], zmul(l10, L[0][1]));
+  double* o = A.out + 8 * t;
+  for (int j = 0; j < 2; ++j) {
+    const zc y1 = zsub(Rh[1][j], zmul(l10, Rh[0][j]));
+    const zc x1 = zdiv(y1, u11);
+    const zc x0 = zdiv(zsub(Rh[0][j], zmul(L[0][1], x1)), L[0][0]);
+    o[2 * j] = x0.re; o[2 * j + 1] = x0.im;
+    o[4 + 2 * j] = x1.re; o[4 + 2 * j + 1] = x1.im;
+  }
+}
+
+// ---------------------------------------------------------------- textbook helpers
+struct ProfileArgs {
+  int64_t n;
+  const double *z, *w0, *wl;  // [n] each (broadcast on the host), NULL where unused
+  const double* zr_in;        // [n] Rayleigh ranges given (w_z, R), or NULL: from w0, wl
+  double *zr, *wz, *r;        // [n] each, or NULL
+  double* qinv;               // [n] complex128, or NULL
+};
+
+__global__ void __launch_bounds__(256) k_beam_profile(const __grid_constant__ ProfileArgs A) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= A.n) return;
+  const double PI = 3.141592653589793;
+  const double z = A.z ? A.z[i] : 0.0, w0 = A.w0 ? A.w0[i] : 0.0, wl = A.wl ? A.wl[i] : 0.0;
+  const double zr = A.zr_in ? A.zr_in[i] : (PI * (w0 * w0)) / wl;  // zR
+  const double q = z / zr;
+  const double wz = w0 * sqrt(1.0 + q * q);                          // w_z
+  const bool focus = fabs(z) < 1e-10;
+  const double ratio = focus ? 0.0 : zr / z;
+  const double r = focus ? INFINITY : z * (1.0 + ratio * ratio);     // R
+  if (A.zr) A.zr[i] = zr;
+  if (A.wz) A.wz[i] = wz;
+  if (A.r) A.r[i] = r;
+  if (A.qinv) {  // q_inv(z, w0, wl): i wl / (pi w0^2) at the focus, else -1/R + i wl / (pi w(z)^2)
+    A.qinv[2 * i] = focus ? 0.0 : -1.0 / r;
+    A.qinv[2 * i + 1] = focus ? wl / (PI * (w0 * w0)) : wl / (PI * (wz * wz));
+  }
+}
+
+struct BeamArgs {
+  int64_t n;
+  const double *x, *y, *ox, *oy;  // [n] each (broadcast on the host)
+  const double* qinv;             // [n] complex128
+  const double* k;                // [n]
+  double* out;                    // [n] complex128
+};
+
+// exp(1j * k * ((x + ox)^2 + (y + oy)^2) / 2 * q_inv), left to right as written
+__global__ void __launch_bounds__(256) k_gaussian_beam(const __grid_constant__ BeamArgs A) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= A.n) return;
+  const double u = A.x[i] + A.ox[i], v = A.y[i] + A.oy[i];
+  const double s = (A.k[i] * (u * u + v * v)) / 2.0;  // real factor of 1j * s * q
+  const double qr = A.qinv[2 * i], qi = A.qinv[2 * i + 1];
+  // 1j * s * (qr + 1j qi) = -s qi + 1j s qr
+  const double mag = exp(-(s * qi));
+  double sn, cs;
+  sincos(s * qr, &sn, &cs);
+  A.out[2 * i] = mag * cs;
+  A.out[2 * i + 1] = mag * sn;
+}
+
 static int sm_count_source() {
   static int cached = 0;
   if (!cached) {
@@ -283,5 +449,63 @@ extern "C" int tg_decompose_q_inv(int64_t n, const double* q_inv, const double* 
   A.radii = radii;
   A.theta = theta;
   k_decompose_q<<<(int)((n + 127) / 128), 128, 0, reinterpret_cast<cudaStream_t>(stream)>>>(A);
+  return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
+}
+
+extern "C" int tg_beam_q_inv(int64_t n, const double* waist, const double* radii, const double* wavelength,
+                             double wavelength_scalar, const double* theta, double theta_scalar,
+                             double* q_xy, double* q_inv, void* stream) {
+  if (n < 0) return TG_ERR_INVALID;
+  if (n > 0 && (!waist || !radii || (!q_xy && !q_inv))) return TG_ERR_INVALID;
+  if (n == 0) return TG_OK;
+  BeamQArgs A;
+  A.n = n;
+  A.waist = waist;
+  A.radii = radii;
+  A.wl = wavelength;
+  A.wl_scalar = wavelength_scalar;
+  A.theta = theta;
+  A.theta_scalar = theta_scalar;
+  A.qxy = q_xy;
+  A.q = q_inv;
+  k_beam_q_inv<<<(int)((n + 127) / 128), 128, 0, reinterpret_cast<cudaStream_t>(stream)>>>(A);
+  return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
+}
+
+extern "C" int tg_qinv_abcd(int64_t n, const double* q_inv, const double* a, const double* b,
+                            const double* c, const double* d, double* out, void* stream) {
+  if (n < 0) return TG_ERR_INVALID;
+  if (n > 0 && (!q_inv || !a || !b || !c || !d || !out)) return TG_ERR_INVALID;
+  if (n == 0) return TG_OK;
+  QabcdArgs A{n, q_inv, a, b, c, d, out};
+  k_qinv_abcd<<<(int)((n + 127) / 128), 128, 0, reinterpret_cast<cudaStream_t>(stream)>>>(A);
+  return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
+}
+
+extern "C" int tg_beam_profile(int64_t n, const double* z, const double* w0, const double* wavelength,
+                               const double* z_r_in, double* z_r, double* w_z, double* r, double* q_inv,
+                               void* stream) {
+  if (n < 0) return TG_ERR_INVALID;
+  if (n == 0) return TG_OK;
+  // every requested output has its inputs (q_inv takes its own zR from w0, wavelength)
+  const bool zr_src = z_r_in || (w0 && wavelength);
+  if (!z_r && !w_z && !r && !q_inv) return TG_ERR_INVALID;
+  if (z_r && !zr_src) return TG_ERR_INVALID;
+  if (w_z && !(w0 && z && zr_src)) return TG_ERR_INVALID;
+  if (r && !(z && zr_src)) return TG_ERR_INVALID;
+  if (q_inv && (z_r_in || !(z && w0 && wavelength))) return TG_ERR_INVALID;
+  ProfileArgs A{n, z, w0, wavelength, z_r_in, z_r, w_z, r, q_inv};
+  k_beam_profile<<<(int)((n + 255) / 256), 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(A);
+  return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
+}
+
+extern "C" int tg_gaussian_beam(int64_t n, const double* x, const double* y, const double* q_inv,
+                                const double* k, const double* offset_x, const double* offset_y,
+                                double* out, void* stream) {
+  if (n < 0) return TG_ERR_INVALID;
+  if (n > 0 && (!x || !y || !q_inv || !k || !offset_x || !offset_y || !out)) return TG_ERR_INVALID;
+  if (n == 0) return TG_OK;
+  BeamArgs A{n, x, y, offset_x, offset_y, q_inv, k, out};
+  k_gaussian_beam<<<(int)((n + 255) / 256), 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(A);
   return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
 }

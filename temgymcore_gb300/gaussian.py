@@ -234,6 +234,125 @@ def decompose_Q_inv(Q_inv, wavelength, eps: float = 1e-12):
     return rs(waist[:, 0]), rs(waist[:, 1]), rs(radii[:, 0]), rs(radii[:, 1]), rs(theta)
 
 
+N.register("tg_beam_q_inv", C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
+                                      C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p])
+N.register("tg_qinv_abcd", C.c_int, [C.c_int64] + [C.c_void_p] * 7)
+N.register("tg_beam_profile", C.c_int, [C.c_int64] + [C.c_void_p] * 9)
+N.register("tg_gaussian_beam", C.c_int, [C.c_int64] + [C.c_void_p] * 8)
+
+
+def beam_q_inv(rays: GaussianRay, full: bool):
+    """GaussianRay.q_inv (``full=False``: the per-axis 1/qx, 1/qy, each (n,))
+    and GaussianRay.Q_inv (``full=True``: (n, 2, 2) = R diag R^T), complex128
+    on the device (gaussian.py:138-177)."""
+    dev = _device()
+    n = rays.size
+    waist = _f64(rays.waist_xy, n, dev, 2)
+    radii = _f64(rays.radii_of_curv, n, dev, 2)
+    wl = _f64(rays.wavelength, n, dev)
+    theta = _f64(rays.theta, n, dev)
+    if full:
+        out = torch.empty((n, 2, 2), dtype=torch.complex128, device=dev)
+        qxy_p, q_p = None, torch.view_as_real(out).data_ptr()
+    else:
+        out = torch.empty((n, 2), dtype=torch.complex128, device=dev)
+        qxy_p, q_p = torch.view_as_real(out).data_ptr(), None
+    N.check(N.lib().tg_beam_q_inv(n, waist.data_ptr(), radii.data_ptr(), wl.data_ptr(), 0.0,
+                                  theta.data_ptr(), 0.0, qxy_p, q_p, N.stream_ptr()), "tg_beam_q_inv")
+    if full:
+        return out
+    if np.ndim(rays.waist_xy) <= 1:  # one beam given as (2,): scalars, as waist_xy.T unpacks
+        return out[0, 0], out[0, 1]
+    return out[:, 0], out[:, 1]
+
+
+def _dev_tensor(v, dtype, dev):
+    if isinstance(v, torch.Tensor):
+        return v.detach().to(device=dev, dtype=dtype)
+    npt = np.complex128 if dtype == torch.complex128 else np.float64
+    return torch.as_tensor(np.asarray(v, dtype=npt), device=dev)
+
+
+def Qinv_ABCD(Qinv, A, B, C_, D):
+    """gaussian.py:92-96: (A + B Q)^-1 (C + D Q) for 2x2 blocks with leading
+    batch axes (broadcast), Q complex, A-D real; complex128 on the device."""
+    dev = _device()
+    q = _dev_tensor(Qinv, torch.complex128, dev)
+    mats = []
+    for m in (A, B, C_, D):
+        t = m.detach() if isinstance(m, torch.Tensor) else torch.as_tensor(np.asarray(m))
+        if t.is_complex():
+            if bool((t.imag != 0).any()):
+                raise NotImplementedError("Qinv_ABCD takes real A, B, C, D (ABCD matrices are real)")
+            t = t.real
+        mats.append(t.to(device=dev, dtype=torch.float64))
+    if any(t.shape[-2:] != (2, 2) for t in [q] + mats):
+        raise ValueError("Qinv_ABCD needs 2x2 blocks in the last two axes")
+    batch = torch.broadcast_shapes(*(t.shape[:-2] for t in [q] + mats))
+    q = q.expand(*batch, 2, 2).reshape(-1, 2, 2).contiguous()
+    mats = [t.expand(*batch, 2, 2).reshape(-1, 2, 2).contiguous() for t in mats]
+    n = q.shape[0]
+    out = torch.empty((n, 2, 2), dtype=torch.complex128, device=dev)
+    N.check(N.lib().tg_qinv_abcd(n, torch.view_as_real(q).data_ptr(), *(t.data_ptr() for t in mats),
+                                 torch.view_as_real(out).data_ptr(), N.stream_ptr()), "tg_qinv_abcd")
+    return out.reshape(*batch, 2, 2)
+
+
+def _profile(which: str, z=None, w0=None, wl=None, z_r=None):
+    dev = _device()
+    given = {k: _dev_tensor(v, torch.float64, dev) for k, v in
+             (("z", z), ("w0", w0), ("wl", wl), ("z_r", z_r)) if v is not None}
+    shape = torch.broadcast_shapes(*(t.shape for t in given.values()))
+    flat = {k: t.expand(shape).reshape(-1).contiguous() for k, t in given.items()}
+    n = int(np.prod(shape)) if len(shape) else 1
+    out = torch.empty(n, dtype=torch.complex128 if which == "q_inv" else torch.float64, device=dev)
+    optr = torch.view_as_real(out).data_ptr() if which == "q_inv" else out.data_ptr()
+    outs = {k: (optr if k == which else None) for k in ("z_r_out", "w_z", "r", "q_inv")}
+    p = lambda k: flat[k].data_ptr() if k in flat else None  # noqa: E731
+    N.check(N.lib().tg_beam_profile(n, p("z"), p("w0"), p("wl"), p("z_r"), outs["z_r_out"], outs["w_z"],
+                                    outs["r"], outs["q_inv"], N.stream_ptr()), "tg_beam_profile")
+    return out.reshape(shape)
+
+
+def zR(w0, wavelength):
+    """Rayleigh range pi w0^2 / wavelength (gaussian.py:17-18), on the device."""
+    return _profile("z_r_out", w0=w0, wl=wavelength)
+
+
+def w_z(w0, z, z_r):
+    """Beam radius w0 sqrt(1 + (z / z_r)^2) (gaussian.py:13-14), on the device."""
+    return _profile("w_z", z=z, w0=w0, z_r=z_r)
+
+
+def R(z, z_r):
+    """Wavefront radius z (1 + (z_r / z)^2), infinite for |z| < 1e-10
+    (gaussian.py:21-28), on the device."""
+    return _profile("r", z=z, z_r=z_r)
+
+
+def q_inv(z, w0, wl):
+    """Complex 1/q of a beam of waist w0 at distance z from its focus
+    (gaussian.py:99-109), elementwise, on the device."""
+    return _profile("q_inv", z=z, w0=w0, wl=wl)
+
+
+def gaussian_beam(x, y, q_inv, k, offset_x=0, offset_y=0):
+    """exp(1j k ((x + offset_x)^2 + (y + offset_y)^2) / 2 q_inv)
+    (gaussian.py:31-32), elementwise, complex128 on the device."""
+    dev = _device()
+    ts = [_dev_tensor(v, torch.float64, dev) for v in (x, y, k, offset_x, offset_y)]
+    q = _dev_tensor(q_inv, torch.complex128, dev)
+    shape = torch.broadcast_shapes(q.shape, *(t.shape for t in ts))
+    xs, ys, ks, oxs, oys = (t.expand(shape).reshape(-1).contiguous() for t in ts)
+    qs = q.expand(shape).reshape(-1).contiguous()
+    n = xs.numel()
+    out = torch.empty(n, dtype=torch.complex128, device=dev)
+    N.check(N.lib().tg_gaussian_beam(n, xs.data_ptr(), ys.data_ptr(), torch.view_as_real(qs).data_ptr(),
+                                     ks.data_ptr(), oxs.data_ptr(), oys.data_ptr(),
+                                     torch.view_as_real(out).data_ptr(), N.stream_ptr()), "tg_gaussian_beam")
+    return out.reshape(shape)
+
+
 def fibonacci_spiral(nb_samples: int, radius: float, alpha=2):
     """Golden-angle (Vogel) spiral sample positions in a disc (utils.py:297-325)."""
     ga = np.pi * (3.0 - np.sqrt(5.0))

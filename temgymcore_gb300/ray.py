@@ -135,6 +135,21 @@ class GaussianRay(Ray):
         return dataclasses.replace(self, **{k: (v(self) if callable(v) else v)
                                             for k, v in updates.items()})
 
+    @property
+    def q_inv(self):
+        """(1/qx, 1/qy) on the principal axes, complex128 on the device
+        (gaussian.py:138-157): i wavelength / (pi w^2), minus 1/R where the
+        radius is finite."""
+        from .gaussian import beam_q_inv
+        return beam_q_inv(self, full=False)
+
+    @property
+    def Q_inv(self):
+        """(n, 2, 2) complex128 R(theta) diag(1/qx, 1/qy) R(theta)^T on the
+        device (gaussian.py:159-177)."""
+        from .gaussian import beam_q_inv
+        return beam_q_inv(self, full=True)
+
 
 # ------------------------------------------------------------- device layout
 

@@ -115,6 +115,25 @@ def test_quadrant_of_tilted_beam(kats, cuda):
         assert np.sign(xm - xc) == np.sign(dx) and np.sign(ym - yc) == np.sign(dy)
 
 
+@pytest.mark.parametrize("n,shape", [(1, (1, 1)), (3, (5, 37)), (130, (37, 53)), (300, (129, 7))])
+def test_ragged_beams_and_detectors(n, shape, cuda):
+    """Beam counts and detector shapes that are not multiples of any tile (the
+    separable GEMM pads M, N and K; the direct kernels' last tiles are partial)."""
+    import temgymcore_gb300 as t
+    from temgymcore_gb300.workloads import build_model, gaussian_rays
+    w = _small(False, n=n, shape=shape)
+    ref = OF.make_gaussian_image(w["rays"], w["model"])
+    assert ref.shape == shape and np.max(np.abs(ref)) > 0
+    plan = t.FieldPlan(gaussian_rays(w["rays"]), build_model(w["model"]))
+    assert plan.separable
+    _cmp(_np(plan.evaluate("fp64")), ref, 5e-7, 5e-7)
+    for meth in ("direct", "separable"):
+        got = _np(plan.evaluate(meth))
+        assert got.shape == shape
+        _cmp(got, ref, 1e-4)
+    assert t._native.error_word() == 0
+
+
 def test_separable_rejects_astigmatic_beams(cuda):
     import temgymcore_gb300 as t
     from temgymcore_gb300.workloads import build_model, gaussian_rays

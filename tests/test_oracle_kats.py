@@ -162,6 +162,28 @@ def test_gauss_free_space_closed_form(kats):
     np.testing.assert_allclose(OF.Qinv_ABCD(q1, A, np.zeros((1, 2, 2)), C, D), q1, rtol=1e-12)
 
 
+def test_gauss_profile_helpers():
+    """zR, w_z, R, q_inv(z, w0, wl) and gaussian_beam against their closed
+    forms (tests/test_gaussians.py:167-214: 1 mm waist, 500 nm)."""
+    w0, wl = 1e-3, 500e-9
+    zr = float(OF.zR(w0, wl))
+    assert np.isclose(zr, np.pi * w0 * w0 / wl, rtol=1e-9, atol=0)
+    assert np.isclose(OF.w_z(w0, 0.0, zr), w0, rtol=1e-9, atol=0)
+    assert np.isclose(OF.w_z(w0, zr, zr), w0 * np.sqrt(2.0), rtol=1e-9, atol=0)
+    assert np.isclose(OF.R_of_z(zr, zr), 2 * zr, rtol=1e-9, atol=0) and np.isinf(OF.R_of_z(0.0, zr))
+    assert np.allclose(OF.q_inv_z(0.0, w0, wl), 1j * wl / (np.pi * w0 * w0), rtol=1e-12, atol=0)
+    exp = -(1.0 / (2 * zr)) + 1j * wl / (np.pi * (w0 * np.sqrt(2.0)) ** 2)
+    assert np.allclose(OF.q_inv_z(zr, w0, wl), exp, rtol=1e-12, atol=0)
+    k = 2 * np.pi / wl
+    assert np.allclose(OF.gaussian_beam(0.0, 0.0, 1j * 1e-6, k), 1.0, rtol=1e-12, atol=0)
+    assert np.allclose(OF.gaussian_beam(1e-3, -2e-3, 1j * 1e-6, k, offset_x=-1e-3, offset_y=2e-3), 1.0,
+                       rtol=1e-12, atol=0)
+    # the per-beam q_inv at a waist (R = inf) is q_inv(0, w0, wl)
+    qx, qy = OF.q_inv(np.array([[w0, 2 * w0]]), np.array([[np.inf, np.inf]]), wl)
+    assert np.allclose(qx, OF.q_inv_z(0.0, w0, wl), rtol=1e-15) and np.allclose(
+        qy, OF.q_inv_z(0.0, 2 * w0, wl), rtol=1e-15)
+
+
 def test_gauss_quadrant(kats):
     g = kats["gauss_quadrant"]
     det = {"kind": "detector", "z": g["z"], "pixel_size": g["pixel_size"], "shape": g["shape"]}
