@@ -336,6 +336,33 @@ int tg_decompose_q_inv(int64_t n, const double *q_inv, const double *wavelength,
                        double *theta, void *stream);
 
 /*
+ * The beamlet field from per-beam ABCD blocks at arbitrary sample points
+ * (complex128 out, float64 throughout, deterministic):
+ *
+ * tg_propagate_misaligned_gaussian - propagate_misaligned_gaussian_jax_scan
+ *   (gaussian.py:319-337, _beam_field gaussian.py:276-316).  Device inputs:
+ *   amp (complex128 [n]), phase_offset ([n], radians), q1_inv (complex128
+ *   [n][2][2]), a, b, c, d (float64 [n][2][2]), e, f, r1m, theta1m ([n][2]),
+ *   k ([n]); r2 ([n_points][2]: x, y) -> out (complex128 [n_points]).
+ * tg_evaluate_misaligned_input_gaussian -
+ *   evaluate_misaligned_input_gaussian_jax_scan (gaussian.py:410-427,
+ *   _input_beam_field gaussian.py:402-409): the same without a, b, c, d, e, f.
+ * Workspace: tg_misaligned_gaussian_workspace(n, n_points) bytes, 16-byte
+ * aligned.  B^-1 and Q1 are zeroed where singular, as the reference does.
+ */
+size_t tg_misaligned_gaussian_workspace(int64_t n_beams, int64_t n_points);
+int tg_propagate_misaligned_gaussian(int64_t n, const double *amp, const double *phase_offset,
+                                     const double *q1_inv, const double *a, const double *b,
+                                     const double *c, const double *d, const double *e, const double *f,
+                                     const double *r1m, const double *theta1m, const double *k,
+                                     int64_t n_points, const double *r2, double *out, void *workspace,
+                                     size_t ws_bytes, void *stream);
+int tg_evaluate_misaligned_input_gaussian(int64_t n, const double *amp, const double *phase_offset,
+                                          const double *q1_inv, const double *r1m, const double *theta1m,
+                                          const double *k, int64_t n_points, const double *r1, double *out,
+                                          void *workspace, size_t ws_bytes, void *stream);
+
+/*
  * tg_beam_q_inv - GaussianRay.q_inv and .Q_inv (gaussian.py:138-177) for n
  * beams: waist, radii (device float64 [n][2]; an infinite radius is a flat
  * wavefront), wavelength / theta (device float64 [n] or NULL = the scalar)

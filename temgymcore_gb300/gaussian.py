@@ -273,13 +273,13 @@ def _dev_tensor(v, dtype, dev):
     return torch.as_tensor(np.asarray(v, dtype=npt), device=dev)
 
 
-def Qinv_ABCD(Qinv, A, B, C_, D):
+def Qinv_ABCD(Qinv, A, B, C, D):  # noqa: N803 - the reference's names (ctypes unused here)
     """gaussian.py:92-96: (A + B Q)^-1 (C + D Q) for 2x2 blocks with leading
     batch axes (broadcast), Q complex, A-D real; complex128 on the device."""
     dev = _device()
     q = _dev_tensor(Qinv, torch.complex128, dev)
     mats = []
-    for m in (A, B, C_, D):
+    for m in (A, B, C, D):
         t = m.detach() if isinstance(m, torch.Tensor) else torch.as_tensor(np.asarray(m))
         if t.is_complex():
             if bool((t.imag != 0).any()):
@@ -363,3 +363,70 @@ def fibonacci_spiral(nb_samples: int, radius: float, alpha=2):
     rr[0] = 0.0
     phi = ii * ga
     return rr * np.cos(phi), rr * np.sin(phi)
+
+
+N.register("tg_misaligned_gaussian_workspace", C.c_size_t, [C.c_int64, C.c_int64])
+N.register("tg_propagate_misaligned_gaussian", C.c_int,
+           [C.c_int64] + [C.c_void_p] * 12 + [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t,
+                                              C.c_void_p])
+N.register("tg_evaluate_misaligned_input_gaussian", C.c_int,
+           [C.c_int64] + [C.c_void_p] * 6 + [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t,
+                                             C.c_void_p])
+
+
+def _per_beam(v, n, tail, dtype, dev):
+    """(n, *tail) contiguous device tensor; a value without the beam axis is
+    broadcast to every beam."""
+    t = _dev_tensor(v, dtype, dev)
+    return t.expand(n, *tail).contiguous() if t.dim() < 1 + len(tail) else t.reshape(n, *tail).contiguous()
+
+
+def _points(r, dev):
+    t = _dev_tensor(r, torch.float64, dev).reshape(-1, 2).contiguous()
+    return t, t.shape[0]
+
+
+def _run_points(fn, n, npts, dev, args, r):
+    out = torch.empty(npts, dtype=torch.complex128, device=dev)
+    if n == 0 or npts == 0:
+        out.zero_()
+        return out
+    ws = torch.empty(N.lib().tg_misaligned_gaussian_workspace(n, npts), dtype=torch.uint8, device=dev)
+    ptrs = [torch.view_as_real(a).data_ptr() if a.is_complex() else a.data_ptr() for a in args]
+    N.check(getattr(N.lib(), fn)(n, *ptrs, npts, r.data_ptr(), torch.view_as_real(out).data_ptr(),
+                                 ws.data_ptr(), ws.numel(), N.stream_ptr()), fn)
+    return out
+
+
+def propagate_misaligned_gaussian_jax_scan(amp, phase_offset, Q1_inv, A, B, C, D, e, f, r1m, theta1m,  # noqa: N803
+                                           k, r2, batch_size=128):
+    """gaussian.py:319-337: the field of n beams with per-beam ABCD blocks
+    (A, B, C, D: (n, 2, 2); e, f, r1m, theta1m: (n, 2); amp, phase_offset, k:
+    (n,)) at the points r2 (npix, 2) = (x, y), summed over beams; complex128
+    (npix,) on the device, every term in float64.  ``batch_size`` is accepted
+    for signature compatibility (the kernel needs no (batch, npix) temporary)."""
+    dev = _device()
+    a = _dev_tensor(amp, torch.complex128, dev).reshape(-1).contiguous()
+    n = a.numel()
+    args = [a, _per_beam(phase_offset, n, (), torch.float64, dev),
+            _per_beam(Q1_inv, n, (2, 2), torch.complex128, dev)]
+    args += [_per_beam(m, n, (2, 2), torch.float64, dev) for m in (A, B, C, D)]
+    args += [_per_beam(v, n, (2,), torch.float64, dev) for v in (e, f, r1m, theta1m)]
+    args.append(_per_beam(k, n, (), torch.float64, dev))
+    r, npts = _points(r2, dev)
+    return _run_points("tg_propagate_misaligned_gaussian", n, npts, dev, args, r)
+
+
+def evaluate_misaligned_input_gaussian_jax_scan(amp, phase_offset, Q1_inv, r1m, theta1m, k, r1,  # noqa: N803
+                                                batch_size=128):
+    """gaussian.py:410-427: the field of n beams in their own plane at the
+    points r1 (npix, 2) = (x, y); complex128 (npix,) on the device."""
+    dev = _device()
+    a = _dev_tensor(amp, torch.complex128, dev).reshape(-1).contiguous()
+    n = a.numel()
+    args = [a, _per_beam(phase_offset, n, (), torch.float64, dev),
+            _per_beam(Q1_inv, n, (2, 2), torch.complex128, dev),
+            _per_beam(r1m, n, (2,), torch.float64, dev), _per_beam(theta1m, n, (2,), torch.float64, dev),
+            _per_beam(k, n, (), torch.float64, dev)]
+    r, npts = _points(r1, dev)
+    return _run_points("tg_evaluate_misaligned_input_gaussian", n, npts, dev, args, r)
