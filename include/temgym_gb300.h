@@ -336,6 +336,17 @@ int tg_decompose_q_inv(int64_t n, const double *q_inv, const double *wavelength,
                        double *theta, void *stream);
 
 /*
+ * tg_inplace_sum - inplace_sum (utils.py:83-114): buffer[py, px] += frame[i]
+ * for every hit i with mask[i] != 0 (mask NULL: all) and (py, px) inside the
+ * h x w buffer (row-major, device).  pix_y / pix_x: device int32, or int64
+ * when idx_i64.  dtype of frame and buffer: 0 int32, 1 int64, 2 float32,
+ * 3 float64; frame NULL adds 1.  Integer buffers are exact; float buffers
+ * round per add in the order the atomics land.
+ */
+int tg_inplace_sum(int64_t n, const void *pix_y, const void *pix_x, int32_t idx_i64, const uint8_t *mask,
+                   const void *frame, int32_t dtype, int32_t h, int32_t w, void *buffer, void *stream);
+
+/*
  * The beamlet field from per-beam ABCD blocks at arbitrary sample points
  * (complex128 out, float64 throughout, deterministic):
  *

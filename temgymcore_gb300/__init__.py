@@ -69,7 +69,9 @@ from .transfer import (  # noqa: E402,F401
 from .propagator import FreeSpaceParaxial, FreeSpaceDirCosine, Propagator, BasePropagator  # noqa: E402,F401
 from .run import (  # noqa: E402,F401
     run_to_end, run_iter, solve_model, abcd_matrix, trace_to_image, pack_model, TracePlan,
+    run_with_grads, calculate_derivatives, passthrough_transform, jacobian_transform, jacobian_and_value,
 )
+from .tree_utils import PathBuilder, HasParamsMixin  # noqa: E402,F401
 from .scan import scan_images, scan_positions, scan_shard, probe_model  # noqa: E402,F401
 from .gaussian import (  # noqa: E402,F401
     make_gaussian_image, evaluate_gaussian_input_image, FieldPlan, fibonacci_spiral, decompose_Q_inv)

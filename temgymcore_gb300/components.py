@@ -18,6 +18,7 @@ import torch
 from . import _native as N
 from .coordinate_transforms import metres_to_pixels_transform, pixels_to_metres_transform
 from .ray import Ray
+from .tree_utils import HasParamsMixin
 
 
 def _f(v) -> float:
@@ -26,7 +27,7 @@ def _f(v) -> float:
     return float(v)
 
 
-class Component:
+class Component(HasParamsMixin):
     """Base component: ``__call__(ray) -> Ray`` (components.py:12-24)."""
 
     z: Any

@@ -9,6 +9,19 @@ from __future__ import annotations
 from typing import NamedTuple
 
 
+def _step(ray, distance, propagator):
+    """Free space over ``distance`` for every ray: one launch of the chain
+    kernel with a single no-op plane at z + distance (the propagator the
+    kernel inserts before it is the step)."""
+    from .components import Plane
+    from .ray import is_uniform
+    from .run import run_to_end
+    if not is_uniform(ray.z):
+        raise NotImplementedError("a propagator call needs one z for all rays")
+    # tensors stay tensors, so a requires_grad distance or z gets its gradient
+    return run_to_end(ray, [Plane(z=ray.z + distance)], propagator=propagator)
+
+
 class BasePropagator:
     """propagator.py:8-19."""
 
@@ -32,10 +45,7 @@ class FreeSpaceParaxial(BasePropagator):
     """x += dx*d, y += dy*d, z += d, pathlength += d (propagator.py:51-72)."""
 
     def __call__(self, ray, distance):
-        from .components import Plane
-        from .run import run_component
-        z = ray.z if not hasattr(ray.z, "reshape") else ray.z
-        return run_component(Plane(z=z + distance), ray)
+        return _step(ray, distance, self)
 
     @staticmethod
     def propagate(ray, distance):
@@ -50,9 +60,7 @@ class FreeSpaceDirCosine(BasePropagator):
     propagator=FreeSpaceDirCosine())``), forward and adjoint."""
 
     def __call__(self, ray, distance):
-        from .components import Plane
-        from .run import run_to_end
-        return run_to_end(ray, [Plane(z=ray.z + distance)], propagator=self)
+        return _step(ray, distance, self)
 
     @staticmethod
     def propagate(ray, distance):

@@ -15,6 +15,8 @@ from typing import Any
 import numpy as np
 import torch
 
+from .tree_utils import HasParamsMixin
+
 
 def _size(v) -> int:
     if isinstance(v, torch.Tensor):
@@ -29,7 +31,7 @@ def _is_vec(v) -> bool:
 
 
 @dataclass(frozen=True)
-class Ray:
+class Ray(HasParamsMixin):
     """Parametric ray(s): positions x, y (m), slopes dx, dy (rad), axial z (m),
     accumulated pathlength (m) and the homogeneous carrier ``_one``
     (ray.py:8-45).  Vector rays hold 1-D arrays of equal length."""

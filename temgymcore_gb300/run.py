@@ -320,15 +320,92 @@ def run_component(component: Component, ray: Ray) -> Ray:
     return out
 
 
-def run_iter(ray: Ray, components: Sequence[Component], propagator=FreeSpaceParaxial()):
-    """run.py:47-82: yields (Propagator, ray) then (component, ray) per element."""
+def passthrough_transform(component):
+    """run.py:26-32: wraps one step as ray -> (ray_out, ray_out)."""
+
+    def inner(ray: Ray):
+        out = _apply_step(component, ray)
+        return out, out
+
+    return inner
+
+
+def jacobian_transform(component):
+    """run.py:35-41: wraps one step as ray -> (ray_out, jac), jac the step's
+    Jacobian in the Ray-of-Rays form that ``custom_jacobian_matrix`` reads
+    (see ``step_jacobian``)."""
+
+    def inner(ray: Ray):
+        return _apply_step(component, ray), step_jacobian(component, ray)
+
+    return inner
+
+
+def jacobian_and_value(fn, argnums: int = 0, **jac_kwargs):
+    """run.py:17-23 for one model step (a component or a Propagator): returns a
+    function ray -> (jac, value).  Only the ray argument is differentiated
+    (argnums=0)."""
+    if argnums != 0:
+        raise NotImplementedError("jacobian_and_value differentiates the ray (argnums=0)")
+
+    def inner(ray: Ray):
+        return step_jacobian(fn, ray), _apply_step(fn, ray)
+
+    return inner
+
+
+def _apply_step(step, ray: Ray) -> Ray:
+    if isinstance(step, Propagator):
+        return step(ray)
+    if isinstance(step, Component):
+        return run_component(step, ray)
+    raise TypeError(f"not a model step: {type(step).__name__}")
+
+
+def _ray_of_rays(m: np.ndarray) -> Ray:
+    """5x5 (rows and columns x, y, dx, dy, _one) -> Ray of Rays; the z and
+    pathlength entries are not formed (None)."""
+    names = ("x", "y", "dx", "dy", "_one")
+
+    def row(i):
+        return Ray(**{n: float(m[i, j]) for j, n in enumerate(names)}, z=None, pathlength=None)
+
+    return Ray(x=row(0), y=row(1), dx=row(2), dy=row(3), z=None, pathlength=None, _one=row(4))
+
+
+def step_jacobian(step, ray: Ray) -> Ray:
+    """Jacobian of one model step (a component call at the ray's plane, or a
+    Propagator of fixed distance) about the central ray, as a Ray of Rays:
+    ``jac.<out>.<in>`` = d out / d in for out, in in x, y, dx, dy, _one
+    (float64, composed on the host from the step's exact matrix, as
+    tg_abcd_compose does for the whole model).  The z and pathlength entries,
+    which ``custom_jacobian_matrix`` does not read, are None."""
     from .components import Plane
+    import dataclasses as _dc
+    z0 = _central(ray)[4]
+    if isinstance(step, Propagator):
+        comps, prop = [Plane(z=z0 + _f(step.distance))], step.propagator
+    elif isinstance(step, ThickLens):
+        comps, prop = [_dc.replace(step, z_po=z0, z_pi=z0 - (_f(step.z_po) - _f(step.z_pi)))], None
+    elif isinstance(step, Component) and _dc.is_dataclass(step) and "z" in step.__dataclass_fields__:
+        comps, prop = [_dc.replace(step, z=z0)], None
+    else:
+        raise TypeError(f"not a model step: {type(step).__name__}")
+    return _ray_of_rays(abcd_matrix(ray, comps, prop))
+
+
+def run_iter(ray: Ray, components: Sequence[Component], transform=passthrough_transform,
+             propagator=FreeSpaceParaxial()):
+    """run.py:47-82: yields (Propagator, out) then (component, out) per
+    element, out = the second value of ``transform(step)(ray)`` (the ray
+    itself for passthrough_transform, its Jacobian for jacobian_transform)."""
     for c in _check_model(components):
         d = _f(c.z) - _f(ray.z)
-        ray = run_to_end(ray, [Plane(z=_f(c.z))], propagator=propagator)
-        yield Propagator(d, propagator), ray
-        ray = run_component(c, ray)
-        yield c, ray
+        step = Propagator(d, propagator)
+        ray, out = transform(step)(ray)
+        yield step, out
+        ray, out = transform(c)(ray)
+        yield c, out
 
 
 def _central(ray: Ray):
@@ -360,6 +437,205 @@ def solve_model(ray: Ray, model: Sequence[Component], propagator=FreeSpaceParaxi
     N.check(N.lib().tg_abcd_compose(C.byref(m), cen, out, steps), "tg_abcd_compose")
     del keep
     return np.array(steps[:50 * len(comps)], dtype=np.float64).reshape(-1, 5, 5)
+
+
+def calculate_derivatives(ray: Ray, model: Sequence[Component], order: int):
+    """run.py:118-147 for order 1: [the Jacobian of run_to_end with respect to
+    the ray] as a Ray of Rays (x, y, dx, dy, _one entries, float64, about the
+    central ray).  The adjoint kernels are first order: order > 1 raises."""
+    if order < 1:
+        return []
+    if order > 1:
+        raise NotImplementedError("derivatives beyond the first are not formed on the GPU")
+    return [_ray_of_rays(abcd_matrix(ray, model))]
+
+
+# ------------------------------------------------------------- run_with_grads
+_RAY_VARS = ("x", "y", "dx", "dy", "z", "pathlength")
+_OUT_FIELDS = ("x", "y", "dx", "dy", "pathlength")
+
+
+class _Ident:
+    """Dictionary key part for an unhashable root (a Ray holding arrays):
+    hashed and compared by identity."""
+
+    def __init__(self, obj):
+        self.obj = obj
+
+    def __hash__(self):
+        return id(self.obj)
+
+    def __eq__(self, other):
+        return self.obj is (other.obj if isinstance(other, _Ident) else other)
+
+    def __repr__(self):
+        return f"<{type(self.obj).__name__} at {id(self.obj):#x}>"
+
+
+def _key(root, *path):
+    try:
+        hash(root)
+        return (root,) + path
+    except TypeError:
+        return (_Ident(root),) + path
+
+
+def _param_paths(comp, path) -> list:
+    """Parameter names (as param_gradient spells them) under a path into a
+    component: a field, descan_error (all its coefficients) or one of them."""
+    from .components import DescanError
+    if len(path) == 1 and path[0] == "descan_error" and isinstance(getattr(comp, "descan_error", None),
+                                                                   DescanError):
+        return ["descan_error." + f for f in DescanError._fields]
+    if len(path) == 2 and path[0] == "descan_error" and path[1] in getattr(DescanError, "_fields", ()):
+        return ["descan_error." + path[1]]
+    fields = getattr(comp, "__dataclass_fields__", {})
+    if len(path) == 1 and (path[0] in fields or (isinstance(comp, ThickLens) and path[0] in ("z_po", "z_pi"))):
+        return [path[0]]
+    return []
+
+
+def _with_param(comp, name, t):
+    import dataclasses as _dc
+    if name.startswith("descan_error."):
+        dn = name.split(".", 1)[1]
+        return _dc.replace(comp, descan_error=comp.descan_error._replace(**{dn: t}))
+    return _dc.replace(comp, **{name: t})
+
+
+def run_with_grads(input_ray: Ray, model: Sequence[Component], grad_vars):
+    """run.py:182-267: run the model and return (value, grads), grads mapping
+    each selected variable's path (root object, keys...) to a Ray of
+    d(output field)/d(variable).
+
+    ``grad_vars``: the input ray itself (all of x, y, dx, dy, z, pathlength),
+    ``input_ray.params.<field>``, or ``component.params.<field>`` (also
+    ``descanner.params.descan_error[.<coefficient>]``) for components of
+    ``model``; an unknown path raises RuntimeError, as the reference does.
+    Shapes follow jax.jacobian: a per-ray input field gives (N, N) blocks
+    (diagonal: rays are independent), a shared scalar gives (N,).
+
+    The derivatives come from the adjoint kernel (tg_trace_vjp) through
+    torch.autograd: one pass per output field for per-ray inputs, and one
+    pass per output field and ray for shared parameters (the kernel sums a
+    parameter's sensitivity over rays).  d/d _one is not formed."""
+    from .ray import is_uniform
+    from .tree_utils import PathBuilder
+    import dataclasses as _dc
+    comps = list(_check_model(model))
+    ray_sel, comp_sel = [], []  # (key, field) / (key, component index, parameter name)
+    for var in grad_vars:
+        before = len(ray_sel) + len(comp_sel)
+        if var is input_ray:
+            ray_sel += [(_key(input_ray, f), f) for f in _RAY_VARS]
+        elif isinstance(var, PathBuilder):
+            root, path = var._resolve_root(), var._build()[1:]
+            if root is input_ray:
+                if path == ("_one",):
+                    raise NotImplementedError("derivatives with respect to _one are not formed")
+                if len(path) == 1 and path[0] in _RAY_VARS:
+                    ray_sel.append((_key(input_ray, *path), path[0]))
+            else:
+                for i, c in enumerate(comps):
+                    if c is root:
+                        comp_sel += [(_key(root, *tuple(nm.split("."))), i, nm) for nm in _param_paths(c, path)]
+                        break
+        if len(ray_sel) + len(comp_sel) == before:
+            raise RuntimeError(f"Cannot find {var!r} in parameters")
+
+    dev = _device()
+    shape = _in_shape(input_ray)
+    n = int(np.prod(shape)) if shape else 1
+    kw = {f.name: getattr(input_ray, f.name) for f in _dc.fields(input_ray)}
+    per_ray, shared = {}, {}  # leaf tensors
+    for _, f in ray_sel:
+        if f in per_ray or f in shared or f == "pathlength":
+            continue  # pathlength enters the output pathlength only: d = 1, done analytically
+        v = kw[f]
+        if f == "z":
+            if not is_uniform(v):
+                raise NotImplementedError("d/dz needs one z for all rays")
+            t = torch.tensor(_f(v), dtype=torch.float64, requires_grad=True)
+            shared["z"] = t
+        else:
+            src = v.detach() if isinstance(v, torch.Tensor) else torch.as_tensor(np.asarray(v, np.float32))
+            t = src.to(device=dev, dtype=torch.float32).expand(shape).contiguous().requires_grad_(True)
+            per_ray[f] = t
+        kw[f] = t
+    cm = list(comps)
+    for _, i, name in comp_sel:
+        if (i, name) in shared:
+            continue
+        cur = getattr(cm[i].descan_error, name.split(".", 1)[1]) if name.startswith("descan_error.") \
+            else getattr(cm[i], name)
+        t = torch.tensor(_f(cur), dtype=torch.float64, requires_grad=True)
+        shared[(i, name)] = t
+        cm[i] = _with_param(cm[i], name, t)
+    with torch.enable_grad():
+        out = run_to_end(type(input_ray)(**kw) if type(input_ray) is Ray else Ray(
+            **{k: kw[k] for k in ("x", "y", "dx", "dy", "z", "pathlength", "_one")}), cm)
+    outs = {k: getattr(out, k) for k in _OUT_FIELDS}
+    f64 = dict(dtype=torch.float64, device=dev)
+    d = {}  # (var id, out field) -> tensor shaped like the output field
+    pr_names = list(per_ray)
+    sh_keys = list(shared)
+    for k in _OUT_FIELDS:
+        o = outs[k]
+        if pr_names:
+            g = torch.autograd.grad(o, [per_ray[f] for f in pr_names], grad_outputs=torch.ones_like(o),
+                                    retain_graph=True, allow_unused=True)
+            for f, gv in zip(pr_names, g):
+                d[(f, k)] = torch.zeros(shape, **f64) if gv is None else gv.to(torch.float64)
+        if sh_keys:
+            cols = {s: torch.zeros(shape, **f64) for s in sh_keys}
+            for i in range(n):
+                seed = torch.zeros_like(o)
+                if shape:
+                    seed[i] = 1
+                else:
+                    seed.fill_(1)
+                g = torch.autograd.grad(o, [shared[s] for s in sh_keys], grad_outputs=seed,
+                                        retain_graph=True, allow_unused=True)
+                for s, gv in zip(sh_keys, g):
+                    if gv is not None:
+                        if shape:
+                            cols[s][i] = gv.to(torch.float64).to(dev)
+                        else:
+                            cols[s] = gv.to(torch.float64).to(dev).reshape(())
+            for s in sh_keys:
+                d[(s, k)] = cols[s]
+    last = len(comps) - 1
+    z_var = (last, "z_pi") if isinstance(comps[-1], ThickLens) else (last, "z")
+
+    def jac(var, field_shared: bool):
+        """Ray of d(out)/d(var); per-ray inputs become (N, N) diagonal blocks."""
+        def blk(v):
+            return torch.diag_embed(v) if (shape and not field_shared) else v
+        fields = {}
+        for k in _OUT_FIELDS:
+            if var == "pathlength":
+                v = torch.ones(shape, **f64) if k == "pathlength" else torch.zeros(shape, **f64)
+            else:
+                v = d[(var, k)]
+            fields[k] = blk(v)
+        fields["z"] = blk(torch.ones(shape, **f64) if var == z_var else torch.zeros(shape, **f64))
+        fields["_one"] = blk(torch.zeros(shape, **f64))
+        return Ray(**fields)
+
+    grads = {}
+    for key, f in ray_sel:
+        shared_field = f == "z" or (shape and not _is_per_ray(getattr(input_ray, f), n))
+        # a scalar field given for vector rays is shared: its column is the per-ray derivative
+        grads[key] = jac(f, bool(shared_field))
+    for key, i, name in comp_sel:
+        grads[key] = jac((i, name), True)
+    value = Ray(**{k: (v.detach() if isinstance(v, torch.Tensor) else v)
+                   for k, v in ((f.name, getattr(out, f.name)) for f in _dc.fields(out))})
+    return value, grads
+
+
+def _is_per_ray(v, n) -> bool:
+    return isinstance(v, (torch.Tensor, np.ndarray)) and v.ndim > 0 and int(np.prod(v.shape)) == n and n > 0
 
 
 # ------------------------------------------------------------------ binning

@@ -1,0 +1,89 @@
+"""Helpers of temgym_core.utils on the path (utils.py:7-43, 83-114, 285-294).
+
+``custom_jacobian_matrix`` turns a Ray-of-Rays Jacobian into the 5x5
+homogeneous matrix; ``inplace_sum`` is the detector accumulation of
+``Grid.into_image`` on the GPU; ``make_aperture`` is the image-plane disc mask
+used by the reference's tests.  Ray sources' ``concentric_rings`` /
+``random_coords`` and ``fibonacci_spiral`` are re-exported.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from .gaussian import fibonacci_spiral  # noqa: F401
+from .sources import concentric_rings, random_coords  # noqa: F401
+
+_ROWS = ("x", "y", "dx", "dy", "_one")
+
+
+def _val(v):
+    if isinstance(v, torch.Tensor):
+        return v.detach().cpu().numpy().astype(np.float64)
+    return np.asarray(v, dtype=np.float64)
+
+
+def custom_jacobian_matrix(ray_jac) -> np.ndarray:
+    """utils.py:7-43: rows and columns [x, y, dx, dy, _one] of a Ray-of-Rays
+    Jacobian (``jacobian_transform``, ``run_with_grads``) as a float64 array
+    (..., 5, 5)."""
+    rows = []
+    for r in _ROWS:
+        out_r = getattr(ray_jac, r)
+        rows.append(np.stack(np.broadcast_arrays(*[_val(getattr(out_r, c)) for c in _ROWS]), axis=-1))
+    return np.stack(np.broadcast_arrays(*rows), axis=-2)
+
+
+def make_aperture(X, Y, aperture_ratio: float = 0.1):
+    """utils.py:285-294: boolean disc of radius aperture_ratio * max|X| on the
+    coordinate grids X, Y (an image-plane mask)."""
+    Xt = X if isinstance(X, torch.Tensor) else torch.as_tensor(np.asarray(X))
+    Yt = Y if isinstance(Y, torch.Tensor) else torch.as_tensor(np.asarray(Y))
+    radius = aperture_ratio * Xt.abs().max()
+    return (Xt ** 2 + Yt ** 2) < radius ** 2
+
+
+_DTYPES = {torch.int32: 0, torch.int64: 1, torch.float32: 2, torch.float64: 3}
+
+
+def inplace_sum(px_y, px_x, mask, frame, buffer):
+    """utils.py:83-114 on the GPU: buffer[py, px] += frame[i] for every i with
+    mask[i] and (py, px) inside the buffer.  ``buffer`` (2-D, int32 / int64 /
+    float32 / float64) is updated in place: a contiguous CUDA tensor directly,
+    a NumPy array by a copy to the device and back.  ``mask`` / ``frame`` may
+    be None (all hits / add 1).  Integer buffers are exact; float buffers
+    match the serial sum to its rounding (the adds land in any order)."""
+    import ctypes as C
+
+    from . import _native as N
+    from .run import _device
+    dev = _device()
+    host = None
+    if isinstance(buffer, torch.Tensor):
+        if not (buffer.is_cuda and buffer.is_contiguous()):
+            raise ValueError("buffer must be a contiguous CUDA tensor (or a NumPy array)")
+        buf = buffer
+    else:
+        host = buffer
+        buf = torch.as_tensor(np.ascontiguousarray(buffer), device=dev)
+    if buf.dim() != 2 or buf.dtype not in _DTYPES:
+        raise TypeError("buffer must be 2-D int32, int64, float32 or float64")
+    h, w = buf.shape
+    idx = lambda v: torch.as_tensor(v, device=dev).to(torch.int64).reshape(-1).contiguous()  # noqa: E731
+    py, px = idx(px_y), idx(px_x)
+    n = py.numel()
+    if px.numel() != n:
+        raise ValueError("px_y and px_x differ in length")
+    m = None if mask is None else torch.as_tensor(mask, device=dev).reshape(-1).to(torch.uint8).contiguous()
+    f = None if frame is None else torch.as_tensor(frame, device=dev).reshape(-1).to(buf.dtype).contiguous()
+    if (m is not None and m.numel() != n) or (f is not None and f.numel() != n):
+        raise ValueError("mask / frame must have one entry per hit")
+    N.register("tg_inplace_sum", C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p,
+                                           C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
+                                           C.c_void_p])
+    N.check(N.lib().tg_inplace_sum(n, py.data_ptr(), px.data_ptr(), 1, N.ptr(m), N.ptr(f),
+                                   _DTYPES[buf.dtype], h, w, buf.data_ptr(), N.stream_ptr()),
+            "tg_inplace_sum")
+    if host is not None:
+        host[...] = buf.cpu().numpy()
+    return None

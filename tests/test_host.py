@@ -98,3 +98,25 @@ def test_workloads_are_seeded():
     assert s["dx"].shape == (1024,) and 0.0 <= s["scangrid"]["rotation"] < 360.0
     f = beamlet_field(seed=0, n_beams=16)
     assert f["rays"]["amplitude"].dtype == np.complex64
+
+
+def test_path_builder_and_custom_jacobian_matrix():
+    """PathBuilder paths (tree_utils.py:34-122) and custom_jacobian_matrix
+    (utils.py:7-43) on the host."""
+    import temgymcore_gb300 as t
+    from temgymcore_gb300.run import _param_paths, _ray_of_rays
+    from temgymcore_gb300.utils import custom_jacobian_matrix
+    lens = t.Lens(z=0.5, focal_length=0.2)
+    p = lens.params.focal_length
+    assert p._build() == (lens, "focal_length") and p._resolve() == 0.2 and p._resolve_root() is lens
+    d = t.Descanner(z=1.0, scan_pos_x=0.0, scan_pos_y=0.0, scan_tilt_x=0.0, scan_tilt_y=0.0)
+    q = d.params.descan_error.offsxi
+    assert q._build() == (d, "descan_error", "offsxi")
+    assert _param_paths(d, ("descan_error",)) == ["descan_error." + f for f in t.DescanError._fields]
+    assert _param_paths(d, ("descan_error", "offsxi")) == ["descan_error.offsxi"]
+    assert _param_paths(lens, ("focal_length",)) == ["focal_length"]
+    assert _param_paths(lens, ("nonexistent",)) == []
+    r = t.Ray(x=0.1, y=0.2, dx=0.3, dy=0.4, z=0.0, pathlength=0.0)
+    assert r.params._one._build() == (r, "_one")
+    m = np.arange(25, dtype=np.float64).reshape(5, 5)
+    np.testing.assert_array_equal(custom_jacobian_matrix(_ray_of_rays(m)), m)
