@@ -130,6 +130,18 @@ class DescanError(NamedTuple):
     def as_array(self) -> np.ndarray:
         return np.array([_f(v) for v in self[:12]])
 
+    def as_matrix(self) -> np.ndarray:
+        """components.py:93-115: the reference's 5x5 with the offsets in the
+        last column, entry for entry - including its dx row, which holds offsyi
+        where offsxi belongs (that matrix is informational: the descanner
+        applies offsets() = offpxi, offpyi, offsxi, offsyi)."""
+        v = [_f(a) for a in self[:12]]
+        return np.array([[v[0], v[1], 0.0, 0.0, v[8]],
+                         [v[2], v[3], 0.0, 0.0, v[9]],
+                         [v[4], v[5], 0.0, 0.0, v[11]],
+                         [v[6], v[7], 0.0, 0.0, v[11]],
+                         [0.0, 0.0, 0.0, 0.0, 1.0]])
+
     def as_matrix4(self) -> np.ndarray:
         """4x4 matrix: rows (x, y, dx, dy) out, cols (spx, spy, stx, sty) in."""
         v = [_f(a) for a in self]

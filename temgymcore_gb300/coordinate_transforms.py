@@ -42,3 +42,22 @@ def pixels_to_metres_transform(centre, pixel_size, shape, flip_y=False, rotation
 def metres_to_pixels_transform(centre, pixel_size, shape, flip_y=False, rotation=0.0):
     """grid.py:51-63: inverse (LU) of the pixels->metres transform."""
     return np.linalg.inv(pixels_to_metres_transform(centre, pixel_size, shape, flip_y, rotation))
+
+
+def apply_transformation(y, x, transformation):
+    """coordinate_transforms.py:104-140: [y', x', 1] = T [y, x, 1] for every
+    coordinate pair (any matching shapes).  Torch tensors stay on their
+    device; anything else is computed with NumPy in float64.  The per-ray
+    binning on the path does not come here: it runs in the GPU binner
+    (tg_bin / tg_trace_fwd), bit-exact with this float64 arithmetic."""
+    import torch
+    if isinstance(y, torch.Tensor) or isinstance(x, torch.Tensor):
+        dev = y.device if isinstance(y, torch.Tensor) else x.device
+        t = torch.as_tensor(np.asarray(transformation, dtype=np.float64), device=dev)
+        yt = torch.as_tensor(y, dtype=torch.float64, device=dev)
+        xt = torch.as_tensor(x, dtype=torch.float64, device=dev)
+        yt, xt = torch.broadcast_tensors(yt, xt)
+        return ((t[0, 0] * yt + t[0, 1] * xt) + t[0, 2], (t[1, 0] * yt + t[1, 1] * xt) + t[1, 2])
+    t = np.asarray(transformation, dtype=np.float64)
+    yy, xx = np.broadcast_arrays(np.asarray(y, np.float64), np.asarray(x, np.float64))
+    return (t[0, 0] * yy + t[0, 1] * xx) + t[0, 2], (t[1, 0] * yy + t[1, 1] * xx) + t[1, 2]

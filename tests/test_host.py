@@ -120,3 +120,20 @@ def test_path_builder_and_custom_jacobian_matrix():
     assert r.params._one._build() == (r, "_one")
     m = np.arange(25, dtype=np.float64).reshape(5, 5)
     np.testing.assert_array_equal(custom_jacobian_matrix(_ray_of_rays(m)), m)
+
+
+def test_apply_transformation_and_descan_matrix():
+    """apply_transformation (coordinate_transforms.py:104-140) and
+    DescanError.as_matrix (components.py:93-115) on the host."""
+    import temgymcore_gb300 as t
+    from temgymcore_gb300.coordinate_transforms import apply_transformation
+    y, x = np.array([0.0, 1.0]), np.array([2.0, 3.0])
+    y2, x2 = apply_transformation(y, x, np.eye(3))
+    assert np.array_equal(y2, y) and np.array_equal(x2, x)
+    det = t.Detector(z=0.0, pixel_size=(0.1, 0.1), shape=(11, 11))
+    py, px = apply_transformation(np.array([0.0, 5.0]), np.array([0.0, 5.0]), det.metres_to_pixels_mat)
+    np.testing.assert_allclose(py, [5.0, -45.0]) and np.testing.assert_allclose(px, [5.0, 55.0])
+    e = t.DescanError(*range(1, 13))
+    m = e.as_matrix()
+    assert m.shape == (5, 5) and m[0, 4] == 9 and m[1, 4] == 10 and m[2, 4] == 12 and m[3, 4] == 12
+    assert m[4, 4] == 1 and m[2, 0] == 5 and m[3, 1] == 8
