@@ -87,3 +87,34 @@ def inplace_sum(px_y, px_x, mask, frame, buffer):
     if host is not None:
         host[...] = buf.cpu().numpy()
     return None
+
+
+def try_ravel(val):
+    """utils.py:207-222: val.ravel() where it exists (torch: reshape(-1)),
+    else val."""
+    if isinstance(val, torch.Tensor):
+        return val.reshape(-1)
+    try:
+        return val.ravel()
+    except AttributeError:
+        return val
+
+
+def try_reshape(val, maybe_has_shape):
+    """utils.py:225-242: val reshaped to maybe_has_shape.shape where both
+    allow it, else val."""
+    try:
+        return val.reshape(tuple(maybe_has_shape.shape))
+    except AttributeError:
+        return val
+
+
+def zero_phase(u, idx_x, idx_y):
+    """utils.py:276-280: multiply the field u in place by the phase that makes
+    u[idx_x, idx_y] real and non-negative; returns u."""
+    c = u[idx_x, idx_y]
+    if isinstance(u, torch.Tensor):
+        u *= torch.exp(-1j * torch.angle(c))
+        return u
+    u *= np.exp(1j * (0 - np.angle(c)))
+    return u
