@@ -76,6 +76,16 @@ def _f64(v, n, dev, width=None):
     return t.contiguous()
 
 
+def _upload(a: np.ndarray, dev) -> torch.Tensor:
+    """Host array -> device tensor: staged in pinned memory and copied on the
+    current stream without a host wait when the target is a CUDA device."""
+    t = torch.from_numpy(np.ascontiguousarray(a))
+    dev = torch.device(dev)
+    if dev.type != "cuda":
+        return t.to(dev)
+    return t.pin_memory().to(dev, non_blocking=True)
+
+
 def pixel_map(grid: Grid) -> TgPixelMap:
     t = grid.pixels_to_metres_mat
     pm = TgPixelMap()
@@ -92,29 +102,40 @@ class BeamSet:
         r = rays
         n = r.size
         self.n = n
-        self.x = _f64(r.x, n, dev)
-        self.y = _f64(r.y, n, dev)
-        self.dx = _f64(r.dx, n, dev)
-        self.dy = _f64(r.dy, n, dev)
         zs = np.unique(np.asarray(r.z.detach().cpu() if isinstance(r.z, torch.Tensor) else r.z,
                                   dtype=np.float64).reshape(-1))
         if zs.size > 1:
             raise NotImplementedError("beams must start from one plane (uniform z)")
         self.z = float(zs[0]) if zs.size else 0.0
-        self.pl = _f64(r.pathlength, n, dev)
         a = r.amplitude
         if isinstance(a, torch.Tensor):
             at = a.detach().to(device=dev, dtype=torch.complex64).reshape(-1)
         else:
-            at = torch.as_tensor(np.asarray(a, dtype=np.complex64).reshape(-1), device=dev)
+            at = _upload(np.asarray(a, dtype=np.complex64).reshape(-1), dev)
         if at.numel() == 1 and n != 1:
             at = at.expand(n)
         self.amp = torch.view_as_real(at.contiguous()).contiguous()
-        self.waist = _f64(r.waist_xy, n, dev, 2)
-        self.radii = _f64(r.radii_of_curv, n, dev, 2)
-        wl = r.wavelength
-        self.wl = _f64(wl, n, dev)
-        self.theta = _f64(r.theta, n, dev)
+        cols = (r.x, r.y, r.dx, r.dy, r.pathlength, r.wavelength, r.theta)
+        pairs = (r.waist_xy, r.radii_of_curv)
+        if any(isinstance(v, torch.Tensor) for v in cols + pairs):
+            self.x, self.y, self.dx, self.dy, self.pl, self.wl, self.theta = (_f64(v, n, dev) for v in cols)
+            self.waist, self.radii = (_f64(v, n, dev, 2) for v in pairs)
+            return
+        # host values: packed into one float64 buffer, one copy to the device,
+        # and every field a contiguous view of it
+        host = np.empty(11 * n, dtype=np.float64)
+        for i, v in enumerate(cols):
+            a1 = np.asarray(v, dtype=np.float64).reshape(-1)
+            host[i * n:(i + 1) * n] = a1 if a1.size != 1 else np.broadcast_to(a1, (n,))
+        for i, v in enumerate(pairs):
+            a2 = np.asarray(v, dtype=np.float64).reshape(-1, 2)
+            host[(7 + 2 * i) * n:(9 + 2 * i) * n] = (a2 if a2.shape[0] != 1 else
+                                                     np.broadcast_to(a2, (n, 2))).reshape(-1)
+        buf = _upload(host, dev)
+        self.x, self.y, self.dx, self.dy, self.pl, self.wl, self.theta = (buf[i * n:(i + 1) * n]
+                                                                        for i in range(7))
+        self.waist = buf[7 * n:9 * n].view(n, 2)
+        self.radii = buf[9 * n:11 * n].view(n, 2)
 
     def struct(self) -> TgBeams:
         b = TgBeams()

@@ -137,3 +137,29 @@ def test_apply_transformation_and_descan_matrix():
     m = e.as_matrix()
     assert m.shape == (5, 5) and m[0, 4] == 9 and m[1, 4] == 10 and m[2, 4] == 12 and m[3, 4] == 12
     assert m[4, 4] == 1 and m[2, 0] == 5 and m[3, 1] == 8
+
+
+def test_beamset_packed_upload_matches_per_field():
+    """BeamSet packs host beam fields into one buffer (one copy): every view
+    equals the per-field conversion, scalars broadcast, wrong sizes raise."""
+    import torch
+    from temgymcore_gb300.gaussian import BeamSet, _f64
+    from temgymcore_gb300.workloads import beamlet_field, gaussian_rays
+    w = beamlet_field(seed=2, n_beams=37, det_shape=(8, 8), astigmatic=True)
+    r = gaussian_rays(w["rays"])
+    cpu = torch.device("cpu")
+    b = BeamSet(r, cpu)
+    n = 37
+    for name, v, width in (("x", r.x, None), ("y", r.y, None), ("dx", r.dx, None), ("dy", r.dy, None),
+                           ("pl", r.pathlength, None), ("wl", r.wavelength, None), ("theta", r.theta, None),
+                           ("waist", r.waist_xy, 2), ("radii", r.radii_of_curv, 2)):
+        got = getattr(b, name)
+        assert got.is_contiguous()
+        assert torch.equal(got, _f64(v, n, cpu, width)), name
+    # a per-beam tensor field takes the per-field path with the same values
+    r2 = r.derive(theta=torch.as_tensor(np.asarray(r.theta, np.float64)))
+    b2 = BeamSet(r2, cpu)
+    assert all(torch.equal(getattr(b, k), getattr(b2, k)) for k in ("x", "waist", "radii", "theta", "wl"))
+    import pytest
+    with pytest.raises((ValueError, AssertionError)):
+        BeamSet(r.derive(theta=np.zeros(5)), cpu)
