@@ -121,9 +121,12 @@ class BeamSet:
             self.x, self.y, self.dx, self.dy, self.pl, self.wl, self.theta = (_f64(v, n, dev) for v in cols)
             self.waist, self.radii = (_f64(v, n, dev, 2) for v in pairs)
             return
-        # host values: packed into one float64 buffer, one copy to the device,
+        # host values: packed into one float64 buffer (pinned, from the caching
+        # host allocator: no fresh pages to fault in), one copy to the device,
         # and every field a contiguous view of it
-        host = np.empty(11 * n, dtype=np.float64)
+        dev = torch.device(dev)
+        staging = torch.empty(11 * n, dtype=torch.float64, pin_memory=dev.type == "cuda")
+        host = staging.numpy()
         for i, v in enumerate(cols):
             a1 = np.asarray(v, dtype=np.float64).reshape(-1)
             host[i * n:(i + 1) * n] = a1 if a1.size != 1 else np.broadcast_to(a1, (n,))
@@ -131,7 +134,7 @@ class BeamSet:
             a2 = np.asarray(v, dtype=np.float64).reshape(-1, 2)
             host[(7 + 2 * i) * n:(9 + 2 * i) * n] = (a2 if a2.shape[0] != 1 else
                                                      np.broadcast_to(a2, (n, 2))).reshape(-1)
-        buf = _upload(host, dev)
+        buf = staging.to(dev, non_blocking=True) if dev.type == "cuda" else staging
         self.x, self.y, self.dx, self.dy, self.pl, self.wl, self.theta = (buf[i * n:(i + 1) * n]
                                                                         for i in range(7))
         self.waist = buf[7 * n:9 * n].view(n, 2)
