@@ -163,3 +163,36 @@ def test_beamset_packed_upload_matches_per_field():
     import pytest
     with pytest.raises((ValueError, AssertionError)):
         BeamSet(r.derive(theta=np.zeros(5)), cpu)
+
+
+def test_coordinate_tuples():
+    """tests/test_coordinates.py:7-41: PixelYX.to_pixels keeps the kind of
+    its values, CoordXY.to_coords gives length-1 float arrays."""
+    import temgymcore_gb300 as t
+    for v, kind in ((17, "i"), (17.0, "f")):
+        px = t.PixelYX(x=v, y=v + 6)
+        pxs = px.to_pixels()
+        assert isinstance(pxs, t.PixelsYX) and len(pxs.x) == 1 and len(pxs.y) == 1
+        assert pxs.x[0] == px.x and pxs.y[0] == px.y
+        assert pxs.x.dtype.kind == kind and pxs.y.dtype.kind == kind
+    c = t.CoordXY(x=17.0, y=23.0).to_coords()
+    assert isinstance(c, t.CoordsXY) and len(c.x) == 1 and c.x[0] == 17.0 and c.y[0] == 23.0
+    assert c.x.dtype.kind == "f" and c.y.dtype.kind == "f"
+
+
+def test_ray_to_vector_and_scan_grid_rotation():
+    """tests/test_rays.py:106-115 (to_vector gives arrays) and
+    tests/test_component.py:355-378 (one scan-grid column step is the pixel
+    size rotated by the grid rotation, y axis flipped)."""
+    import dataclasses
+    import temgymcore_gb300 as t
+    v = t.Ray(x=1.0, y=2.0, dx=0.1, dy=0.2, z=3.0, pathlength=4.0).to_vector()
+    for f in dataclasses.fields(v):
+        assert np.ndim(getattr(v, f.name)) == 1
+    rng = np.random.default_rng(11)
+    for rot in rng.uniform(-180.0, 180.0, 5):
+        g = t.ScanGrid(z=0.0, rotation=float(rot), pixel_size=(0.1, 0.1), shape=(11, 11))
+        mx0, my0 = g.pixels_to_metres((5, 5))
+        mx1, my1 = g.pixels_to_metres((5, 6))
+        th = np.deg2rad(rot)
+        np.testing.assert_allclose([mx1 - mx0, my1 - my0], [np.cos(th) * 0.1, -np.sin(th) * 0.1], atol=1e-12)
