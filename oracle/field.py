@@ -14,6 +14,9 @@ Follows:
   - ``evaluate_gaussian_input_image``            gaussian.py:372-400
   - ``_input_beam_field``                        gaussian.py:403-409
   - ``fibonacci_spiral``                         utils.py:297-325
+  - ``FresnelPropagator`` / ``fresnel_lens_imaging_solution`` (the
+    transfer-function Fresnel method the reference's tests check the
+    beamlet field against)                      utils.py:245-272
 
 2x2 inverses are written out explicitly (the reference calls
 jnp.linalg.solve); singular matrices give inf/nan which are zeroed with
@@ -301,3 +304,25 @@ def fibonacci_spiral(nb_samples: int, radius: float, alpha=2):
     rr[0] = 0.0
     phi = ii * ga
     return rr * np.cos(phi), rr * np.sin(phi)
+
+
+def fresnel_tf(u1, side, wavelength, z):
+    """utils.py:245-262: Fresnel propagation over z by the transfer-function
+    method on a square grid of physical side ``side``: U2 = IFFT(H FFT(u1)),
+    H = exp(-i pi wavelength z (fx^2 + fy^2)) (no exp(ikz) factor)."""
+    m, n = u1.shape
+    dx = side / m
+    fx = np.fft.fftfreq(n, d=dx)
+    fy = np.fft.fftfreq(m, d=dx)
+    FX, FY = np.meshgrid(fx, fy)
+    return np.fft.ifft2(np.exp(-1j * np.pi * wavelength * z * (FX ** 2 + FY ** 2)) * np.fft.fft2(u1))
+
+
+def fresnel_thin_lens(u0, X, Y, pixel, wavelength, z1, f, z2):
+    """utils.py:265-272: propagate z1, thin-lens phase exp(-i k r^2 / 2f),
+    propagate z2."""
+    k = 2 * np.pi / wavelength
+    side = u0.shape[0] * pixel
+    u = fresnel_tf(u0, side, wavelength, z1)
+    u = u * np.exp((-1j * k) / (2 * f) * (X ** 2 + Y ** 2))
+    return fresnel_tf(u, side, wavelength, z2)

@@ -277,3 +277,50 @@ def test_oracle_input_field_astigmatic_rotation():
                                                          waist=[2e-4, 1e-4]), det)
         phi = _principal_axis_angle(img, X, Y)
         assert abs(np.arctan2(np.sin(phi - th), np.cos(phi - th))) < 0.1
+
+
+def _fresnel_case(model, wavelength, w0, fresnel):
+    """The oracle's single-beam field against a Fresnel FFT propagation of
+    the same Gaussian input (tests/test_gaussians.py:276-519): both
+    normalised to unit peak and to zero phase at the centre pixel, compared
+    inside a disc of 0.4 of the half-width."""
+    from oracle.grid import grid_coords
+    det = model[-1]
+    h, w = det["shape"]
+    rays = {"x": 0.0, "y": 0.0, "dx": 0.0, "dy": 0.0, "z": 0.0, "pathlength": 0.0, "amplitude": 1.0,
+            "waist_xy": [[w0, w0]], "radii_of_curv": [[np.inf, np.inf]], "wavelength": wavelength,
+            "theta": 0.0}
+    a = OF.make_gaussian_image(rays, model, chunk=1)
+    xy = grid_coords(det)
+    X, Y = xy[:, 0].reshape(h, w), xy[:, 1].reshape(h, w)
+    g = OF.gaussian_beam(X, Y, OF.q_inv_z(0.0, w0, wavelength), 2 * np.pi / wavelength)
+    b = fresnel(g, X, Y)
+    out = []
+    for u in (a, b):
+        u = u * np.exp(-1j * np.angle(u[h // 2, w // 2]))
+        out.append(u / np.max(np.abs(u)))
+    mask = (X ** 2 + Y ** 2) < (0.4 * np.max(np.abs(X))) ** 2
+    amp = np.max(np.abs(np.abs(out[0][mask]) - np.abs(out[1][mask])))
+    ph = np.abs(np.angle(out[0][mask] * np.conj(out[1][mask])))
+    return amp, ph.max()
+
+
+def test_oracle_free_space_vs_fresnel():
+    d, px, n, wl, w0 = 1e-3, 5e-4, 2000, 1e-3, 0.1
+    model = [{"kind": "source", "z": 0.0},
+             {"kind": "detector", "z": d, "pixel_size": (px, px), "shape": (n, n)}]
+    amp, ph = _fresnel_case(model, wl, w0, lambda g, X, Y: OF.fresnel_tf(g, n * px, wl, d))
+    assert amp <= 1e-1 and ph <= 1e-1, (amp, ph)
+
+
+def test_oracle_lens_vs_fresnel():
+    """M = -2 imaging with f = 5 mm and 0.1 mm defocus (z1, z2 from the thin
+    lens equation, tests/transfer_matrices.py:263-271)."""
+    M, f, defocus, px, n, wl, w0 = -2.0, 5e-3, 1e-4, 5e-6, 2048, 1e-5, 5e-4
+    z1, z2 = f * (1 / M - 1), f * (1 - M)
+    model = [{"kind": "source", "z": 0.0},
+             {"kind": "lens", "z": abs(z1) + defocus, "focal_length": f},
+             {"kind": "detector", "z": abs(z1) + z2, "pixel_size": (px, px), "shape": (n, n)}]
+    amp, ph = _fresnel_case(model, wl, w0,
+                            lambda g, X, Y: OF.fresnel_thin_lens(g, X, Y, px, wl, defocus + abs(z1), f, z2))
+    assert amp <= 5e-1 and ph <= 2.0, (amp, ph)
