@@ -324,3 +324,56 @@ def test_oracle_lens_vs_fresnel():
     amp, ph = _fresnel_case(model, wl, w0,
                             lambda g, X, Y: OF.fresnel_thin_lens(g, X, Y, px, wl, defocus + abs(z1), f, z2))
     assert amp <= 5e-1 and ph <= 2.0, (amp, ph)
+
+
+def test_oracle_two_beam_interference_vs_fresnel():
+    """Two beams tilted 0.1 rad (in y and in x) through a 5 mm lens to 2 mm
+    past focus, against the Fresnel FFT of the summed tilted Gaussians
+    (tests/test_gaussians.py:520-681).  Normalised to unit peak and zero
+    centre phase; amplitudes compared inside 0.8 of the half-width (the
+    reference's 0.5), phases at pixels above a quarter of the peak."""
+    from oracle.grid import grid_coords
+    px, n, f, defocus, wl, w0 = 5e-6, 1024, 5e-3, 2e-3, 1e-4, 0.5e-3
+    z2 = f + defocus
+    det = {"kind": "detector", "z": z2, "pixel_size": (px, px), "shape": (n, n)}
+    model = [{"kind": "lens", "z": 0.0, "focal_length": f}, det]
+    tilts = [(0.0, 0.1), (0.1, 0.0)]  # (dx, dy)
+    rays = {"x": np.zeros(2), "y": np.zeros(2), "dx": np.array([t[0] for t in tilts]),
+            "dy": np.array([t[1] for t in tilts]), "z": 0.0, "pathlength": np.zeros(2),
+            "amplitude": np.ones(2), "waist_xy": np.full((2, 2), w0), "radii_of_curv": np.full((2, 2), np.inf),
+            "wavelength": wl, "theta": np.zeros(2)}
+    a = OF.make_gaussian_image(rays, model, chunk=1)
+    xy = grid_coords(det)
+    X, Y = xy[:, 0].reshape(n, n), xy[:, 1].reshape(n, n)
+    k = 2 * np.pi / wl
+    g = sum(OF.gaussian_beam(X, Y, OF.q_inv_z(0.0, w0, wl), k) * np.exp(1j * k * (X * tx + Y * ty))
+            for tx, ty in tilts)
+    b = OF.fresnel_thin_lens(g, X, Y, px, wl, 0.0, f, z2)
+    out = []
+    for u in (a, b):
+        u = u * np.exp(-1j * np.angle(u[n // 2, n // 2]))
+        out.append(u / np.max(np.abs(u)))
+    mask = (X ** 2 + Y ** 2) < (0.8 * np.max(np.abs(X))) ** 2
+    amp = np.max(np.abs(np.abs(out[0][mask]) - np.abs(out[1][mask])))
+    bright = mask & (np.abs(out[1]) > 0.25)
+    ph = np.max(np.abs(np.angle(out[0][bright] * np.conj(out[1][bright]))))
+    assert amp <= 5e-1 and ph <= 2.0, (amp, ph)
+
+
+def test_oracle_input_slope_and_angle_vs_fresnel():
+    """A beam with a random offset and tilt: the peak of its detector field at
+    1 m is where the Fresnel FFT of its input-plane field peaks, within 3
+    pixels of flat index (tests/test_gaussians.py:788-817; seeded here)."""
+    rng = np.random.default_rng(7)
+    n, px, z, wl = 1024, 1e-5, 1.0, 500e-9
+    det = {"kind": "detector", "z": z, "pixel_size": (px, px), "shape": (n, n)}
+    for _ in range(3):
+        r1m = rng.uniform(-1e-3, 1e-3, 2)
+        t1m = rng.uniform(-1e-4, 1e-4, 2)
+        rays = {"x": r1m[0], "y": r1m[1], "dx": t1m[0], "dy": t1m[1], "z": 0.0, "pathlength": 0.0,
+                "amplitude": 1.0, "waist_xy": [[1e-4, 1e-4]], "radii_of_curv": [[np.inf, np.inf]],
+                "wavelength": wl, "theta": 0.0}
+        inp = OF.evaluate_gaussian_input_image(rays, dict(det, z=0.0), chunk=1)
+        out = OF.make_gaussian_image(rays, [det], chunk=1)
+        fr = OF.fresnel_tf(inp, n * px, wl, z)
+        assert abs(int(np.argmax(np.abs(fr))) - int(np.argmax(np.abs(out)))) <= 3
