@@ -36,11 +36,15 @@ def custom_jacobian_matrix(ray_jac) -> np.ndarray:
 
 def make_aperture(X, Y, aperture_ratio: float = 0.1):
     """utils.py:285-294: boolean disc of radius aperture_ratio * max|X| on the
-    coordinate grids X, Y (an image-plane mask)."""
-    Xt = X if isinstance(X, torch.Tensor) else torch.as_tensor(np.asarray(X))
-    Yt = Y if isinstance(Y, torch.Tensor) else torch.as_tensor(np.asarray(Y))
-    radius = aperture_ratio * Xt.abs().max()
-    return (Xt ** 2 + Yt ** 2) < radius ** 2
+    coordinate grids X, Y (an image-plane mask); NumPy in, NumPy out, and
+    torch tensors stay torch tensors on their device."""
+    if isinstance(X, torch.Tensor) or isinstance(Y, torch.Tensor):
+        Xt, Yt = torch.as_tensor(X), torch.as_tensor(Y)
+        radius = aperture_ratio * Xt.abs().max()
+        return (Xt ** 2 + Yt ** 2) < radius ** 2
+    X, Y = np.asarray(X), np.asarray(Y)
+    radius = np.max(np.abs(X)) * aperture_ratio
+    return X ** 2 + Y ** 2 < radius ** 2
 
 
 _DTYPES = {torch.int32: 0, torch.int64: 1, torch.float32: 2, torch.float64: 3}

@@ -196,3 +196,15 @@ def test_ray_to_vector_and_scan_grid_rotation():
         mx1, my1 = g.pixels_to_metres((5, 6))
         th = np.deg2rad(rot)
         np.testing.assert_allclose([mx1 - mx0, my1 - my0], [np.cos(th) * 0.1, -np.sin(th) * 0.1], atol=1e-12)
+
+
+def test_make_aperture_types():
+    """utils.py:285-294: NumPy grids give a NumPy mask; torch grids a torch mask."""
+    import torch
+    from temgymcore_gb300.utils import make_aperture
+    Y, X = np.meshgrid(np.linspace(-1, 1, 11), np.linspace(-1, 1, 11), indexing="ij")
+    m = make_aperture(X, Y, aperture_ratio=0.4)
+    assert isinstance(m, np.ndarray) and m.dtype == bool and m[5, 5] and not m[0, 0]
+    assert np.array_equal(m, X ** 2 + Y ** 2 < (0.4 * np.max(np.abs(X))) ** 2)
+    mt = make_aperture(torch.as_tensor(X), torch.as_tensor(Y), aperture_ratio=0.4)
+    assert isinstance(mt, torch.Tensor) and np.array_equal(mt.numpy(), m)
