@@ -454,3 +454,34 @@ def evaluate_misaligned_input_gaussian_jax_scan(amp, phase_offset, Q1_inv, r1m, 
             _per_beam(k, n, (), torch.float64, dev)]
     r, npts = _points(r1, dev)
     return _run_points("tg_evaluate_misaligned_input_gaussian", n, npts, dev, args, r)
+
+
+def _einsum(spec, *ops):
+    if any(isinstance(o, torch.Tensor) for o in ops):
+        return torch.einsum(spec, *(torch.as_tensor(o) for o in ops))
+    return np.einsum(spec, *ops)
+
+
+def matrix_vector_mul(M, v):
+    """gaussian.py:180-187: M @ v for one 2x2 block and one 2-vector."""
+    return _einsum("ij,j->i", M, v)
+
+
+def matrix_matrix_mul(M1, M2):
+    """gaussian.py:190-197: M1 @ M2 for 2x2 blocks."""
+    return _einsum("ij,jk->ik", M1, M2)
+
+
+def matrix_quadratic_mul(v, M):
+    """gaussian.py:200-207: v^T M v."""
+    return _einsum("i,ij,j->", v, M, v)
+
+
+def matrix_linear_mul(v, M, w):
+    """gaussian.py:210-218: v^T M w_n for every row w_n of w (np, 2)."""
+    return _einsum("i,ij,nj->n", v, M, w)
+
+
+def matrix_matrix_matrix_mul(M1, M2, M3):
+    """gaussian.py:221-222: M1 M2 M3^T per batch entry (n, 2, 2)."""
+    return _einsum("nij,njk,npk->nip", M1, M2, M3)

@@ -74,3 +74,8 @@ class HasParamsMixin:
 
     def new_with(self, **kwargs):
         return dataclasses.replace(self, **kwargs)
+
+
+def isnamedtuple(obj) -> bool:
+    """tree_utils.py:14-19."""
+    return isinstance(obj, tuple) and hasattr(obj, "_asdict") and hasattr(obj, "_fields")

@@ -122,3 +122,58 @@ def zero_phase(u, idx_x, idx_y):
         return u
     u *= np.exp(1j * (0 - np.angle(c)))
     return u
+
+
+def multi_cumsum_inplace(values, partitions, start):
+    """utils.py:47-80: running sums over ``values`` (1-D, modified in place)
+    that restart at ``start`` once a partition's length has been counted.
+    The count starts after the first element of each partition, so each
+    restart lands one index after the partition boundary - the layout the
+    reference's concentric_rings relies on, reproduced here as is.  Host
+    helper; the ray sources run the same recurrence on the GPU."""
+    parts = [int(p) for p in np.asarray(partitions).reshape(-1)]
+    if values.size == 0:
+        return None
+    part, length, count = 0, parts[0], 0
+    values[0] = start
+    for i in range(1, values.size):
+        if count == length:
+            count = 0
+            part += 1
+            length = parts[part]
+            values[i] = start
+        else:
+            values[i] += values[i - 1]
+            count += 1
+    return None
+
+
+def FresnelPropagator(u1, L, wavelength, z, xp=np):  # noqa: N802 - the reference's name
+    """utils.py:245-262: Fresnel propagation of the square field u1 (side L)
+    over z by the transfer-function method, U2 = IFFT(H FFT(u1)) with
+    H = exp(-i pi wavelength z (fx^2 + fy^2)).  torch tensors (or
+    xp=torch) run with torch.fft on their device; anything else with NumPy."""
+    if isinstance(u1, torch.Tensor) or xp is torch:
+        t = torch.as_tensor(u1)
+        m, n = t.shape
+        d = L / m
+        fx = torch.fft.fftfreq(n, d=d, device=t.device, dtype=torch.float64)
+        fy = torch.fft.fftfreq(m, d=d, device=t.device, dtype=torch.float64)
+        FY, FX = torch.meshgrid(fy, fx, indexing="ij")
+        H = torch.exp(-1j * torch.pi * wavelength * z * (FX ** 2 + FY ** 2))
+        return torch.fft.ifft2(H * torch.fft.fft2(t))
+    m, n = u1.shape
+    d = L / m
+    FX, FY = np.meshgrid(np.fft.fftfreq(n, d=d), np.fft.fftfreq(m, d=d))
+    return np.fft.ifft2(np.exp(-1j * np.pi * wavelength * z * (FX ** 2 + FY ** 2)) * np.fft.fft2(u1))
+
+
+def fresnel_lens_imaging_solution(E0, Y, X, ps, lambda0, z1, f, z2):  # noqa: N803
+    """utils.py:265-272: E0 propagated z1, through a thin lens of focal length
+    f (phase exp(-i k (X^2 + Y^2) / 2f)), then z2; square grid of pixel ps."""
+    k = 2 * np.pi / lambda0
+    side = E0.shape[0] * ps
+    E = FresnelPropagator(E0, side, lambda0, z1)
+    lib = torch if isinstance(E, torch.Tensor) else np
+    E = E * lib.exp((-1j * k) / (2 * f) * (X ** 2 + Y ** 2))
+    return FresnelPropagator(E, side, lambda0, z2)

@@ -208,3 +208,37 @@ def test_make_aperture_types():
     assert np.array_equal(m, X ** 2 + Y ** 2 < (0.4 * np.max(np.abs(X))) ** 2)
     mt = make_aperture(torch.as_tensor(X), torch.as_tensor(Y), aperture_ratio=0.4)
     assert isinstance(mt, torch.Tensor) and np.array_equal(mt.numpy(), m)
+
+
+def test_small_reference_helpers():
+    """multi_cumsum_inplace (utils.py:47-80), FresnelPropagator
+    (utils.py:245-262, NumPy and torch agree with the oracle's restatement),
+    the 2x2 matrix helpers (gaussian.py:180-222), isnamedtuple."""
+    import torch
+    import temgymcore_gb300 as t
+    from oracle import field as OF
+    from temgymcore_gb300 import gaussian as G
+    from temgymcore_gb300.tree_utils import isnamedtuple
+    from temgymcore_gb300.utils import FresnelPropagator, fresnel_lens_imaging_solution, multi_cumsum_inplace
+    v = np.ones(10)
+    multi_cumsum_inplace(v, np.array([3, 2, 3]), 0.0)
+    # restart one index after each boundary: [0,1,2,3] [0,1,2] [0,1,...]
+    np.testing.assert_array_equal(v, [0, 1, 2, 3, 0, 1, 2, 0, 1, 2])
+    rng = np.random.default_rng(0)
+    u = rng.normal(size=(16, 16)) + 1j * rng.normal(size=(16, 16))
+    ref = OF.fresnel_tf(u, 1e-3, 5e-7, 0.01)
+    np.testing.assert_allclose(FresnelPropagator(u, 1e-3, 5e-7, 0.01), ref, rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(FresnelPropagator(torch.as_tensor(u), 1e-3, 5e-7, 0.01).numpy(), ref,
+                               rtol=1e-12, atol=1e-12)
+    Y, X = np.meshgrid(np.arange(16) * 1e-5, np.arange(16) * 1e-5, indexing="ij")
+    np.testing.assert_allclose(fresnel_lens_imaging_solution(u, Y, X, 1e-5, 5e-7, 0.01, 0.02, 0.03),
+                               OF.fresnel_thin_lens(u, X, Y, 1e-5, 5e-7, 0.01, 0.02, 0.03), rtol=1e-12, atol=1e-12)
+    M, N2, v2 = rng.normal(size=(2, 2)), rng.normal(size=(2, 2)), rng.normal(size=2)
+    np.testing.assert_allclose(G.matrix_vector_mul(M, v2), M @ v2)
+    np.testing.assert_allclose(G.matrix_matrix_mul(M, N2), M @ N2)
+    np.testing.assert_allclose(G.matrix_quadratic_mul(v2, M), v2 @ M @ v2)
+    w = rng.normal(size=(5, 2))
+    np.testing.assert_allclose(G.matrix_linear_mul(v2, M, w), w @ (M.T @ v2))
+    B = rng.normal(size=(3, 2, 2))
+    np.testing.assert_allclose(G.matrix_matrix_matrix_mul(B, B, B), B @ B @ np.swapaxes(B, 1, 2))
+    assert isnamedtuple(t.DescanError()) and not isnamedtuple((1, 2))
