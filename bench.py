@@ -1,19 +1,22 @@
 """Benchmark of the GB300 TemGymCore hot path.
 
-Headline workload (one step): the 4D-STEM shadow-image batch - a 64 x 64 scan
-(step 1e-9 m, random rotation), one 1,024-ray point-source bundle per probe
-(4,194,304 ray traces), descan matrix I + N(0, 1e-3), camera length 0.1 m,
-per-probe dense 256 x 256 int32 detector images (1.07 GB written per step).
-Metric: ray-component steps per second (rays x components, forward trace +
-binning), whole job.  The working set (1.07 GB of images) exceeds the 129 MB
-L2, so no flush is needed between steps.
+Headline workload (one step): the batched sweep - 512 independent optical
+models with U{2..12} components drawn from lens / deflector / biprism /
+aperture (log-uniform f in [0.01, 1] m), log-uniform ray counts in
+[1e3, 2.6e5] (23,544,821 rays), forward trace + adjoint of the
+squared-residual detector loss (the batched form of jax.value_and_grad over
+run_to_end), one persistent launch replayed as a CUDA graph.  Metric:
+ray-component steps per second (sum over models of rays x components),
+whole job.  The working set (565 MB of inputs and targets, 1.15 GB moved per
+step) exceeds the 129 MB L2, so no flush is needed between steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
-Under torchrun (N > 1) every rank runs its own scan (weak scaling: probes
+Under torchrun (N > 1) every rank runs its own sweep (weak scaling: models
 are independent, there is no data-path collective); rank 0 prints the line.
-``--impl reference`` times the CPU restatement of the reference's per-probe
-loop (run_to_end + into_image) on all host cores, same metric and config.
+``--impl reference`` times the CPU arm: the reference's JAX path when it
+imports (jax + temgym_core), else the NumPy float64 restatement of its
+per-model value-and-gradient, over the whole sweep on all host cores.
 """
 from __future__ import annotations
 
@@ -30,8 +33,13 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "fwd+grad ray·component steps/s; field beam·px/s at stated err vs the float64 kernel"
-UNIT = "ray·component steps/s"
+METRIC = "fwd+grad ray\u00b7component steps/s; field beam\u00b7px/s at stated err vs FP64 oracle"
+UNIT = "ray\u00b7component steps/s"
+SWEEP_SEED = 0
+SWEEP_MODELS = 512
+# bytes per ray of the fused forward + adjoint launch: x, y, dx, dy and the
+# two targets read (24), x, y, dx, dy written (16), pathlength (8), alive (1)
+SWEEP_BYTES_PER_RAY = 49
 SCAN = (64, 64)
 RAYS = 1024
 N_COMPONENTS = 5  # PointSource, ScanGrid, Scanner, Descanner, Detector
@@ -150,49 +158,97 @@ def _workload():
     return stem_4d(seed=0, scan=SCAN, rays_per_probe=RAYS)
 
 
-# ------------------------------------------------------------ CPU baseline
-
-def _cpu_probe_chunk(args):
-    """Reference loop restated (oracle): run_to_end + metres_to_pixels +
-    into_image per probe.  Returns elapsed seconds for ``probes``."""
-    sys.path.insert(0, ROOT)
-    import oracle
-    from oracle.rays import ORay
-    from temgymcore_gb300.workloads import stem_4d, stem_probe_model
-    probes, = args
-    w = stem_4d(seed=0, scan=SCAN, rays_per_probe=RAYS)
-    g = {k: w["detector"][k] for k in ("pixel_size", "shape")}
-    sg = {k: w["scangrid"][k] for k in ("pixel_size", "shape", "rotation")}
-    t0 = time.perf_counter()
-    for p in probes:
-        r, c = divmod(int(p), SCAN[1])
-        spx, spy = oracle.pixels_to_metres(sg, r, c)
-        spec = stem_probe_model(w, float(spx), float(spy))
-        out = oracle.run_to_end(ORay(w["x"].astype(np.float64), w["y"].astype(np.float64),
-                                     w["dx"].astype(np.float64), w["dy"].astype(np.float64),
-                                     0.0, 0.0), spec)
-        py, px = oracle.metres_to_pixels(g, out.x, out.y)
-        oracle.into_image(g, py, px)
-    return time.perf_counter() - t0
+_SWEEP = {}
 
 
-def cpu_baseline(sample_probes=SCAN[0] * SCAN[1]):
-    """Single-core oracle timing on a bounded sample (rank 0, N=1 only)."""
-    el = _cpu_probe_chunk((list(range(sample_probes)),))
-    v = sample_probes * RAYS * N_COMPONENTS / el
-    return {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"{sample_probes} of {SCAN[0] * SCAN[1]} probes x {RAYS} rays, NumPy float64 "
-                      "restatement of run_to_end + metres_to_pixels + into_image per probe, 1 thread"}
+def _sweep():
+    """The headline workload's seeded inputs (cached per process)."""
+    if not _SWEEP:
+        from temgymcore_gb300.workloads import batched_sweep
+        w = batched_sweep(seed=SWEEP_SEED, n_models=SWEEP_MODELS)
+        w["offsets"] = np.concatenate([[0], np.cumsum(w["counts"])])
+        w["work"] = np.array([int(c) * len(sp) for c, sp in zip(w["counts"], w["specs"])], dtype=np.int64)
+        _SWEEP.update(w)
+    return _SWEEP
 
 
 def headline_config(world: int) -> dict:
     """The headline workload (both arms print this config)."""
-    return {"workload": "4D-STEM shadow images: 64x64 scan (step 1e-9 m, rotation "
-                        "U(0,2pi)), 1024-ray point-source bundle per probe, descan I+N(0,1e-3), "
-                        "camera length 0.1 m, 256x256 int32 images at 5.5e-5 m",
-            "rays_per_step": SCAN[0] * SCAN[1] * RAYS, "components": N_COMPONENTS,
-            "l2": "no flush: 1.07 GB of images written per step > 129 MB L2",
-            "parallelism": f"dp{world} (independent scans per rank)"}
+    w = _sweep()
+    return {"workload": "batched sweep: 512 models, U{2..12} components from lens/deflector/biprism/"
+                        "aperture (log-uniform f in [0.01, 1] m), log-uniform rays per model in "
+                        "[1e3, 2.6e5], forward + adjoint of the squared-residual detector loss "
+                        "(per-model loss and per-step gradient sums), seed 0",
+            "models": len(w["specs"]), "rays_per_step": int(w["offsets"][-1]),
+            "ray_component_steps_per_step": int(w["work"].sum()),
+            "l2": "no flush: 565 MB of inputs and targets read, 590 MB written per step > 129 MB L2",
+            "parallelism": f"dp{world} (independent sweeps per rank)"}
+
+
+# ------------------------------------------------------------ CPU baselines
+
+def _cpu_sweep_chunk(models):
+    """The oracle's float64 value-and-gradient (forward with its tape, loss,
+    reverse walk: what jax.value_and_grad over run_to_end does) for the given
+    sweep models.  Returns (seconds, ray-component steps)."""
+    if ROOT not in sys.path:
+        sys.path.insert(0, ROOT)
+    from oracle.adjoint import value_and_raw
+    w = _sweep()
+    off = w["offsets"]
+    t0 = time.perf_counter()
+    steps = 0
+    for m in models:
+        a, b = int(off[m]), int(off[m + 1])
+        value_and_raw(w["specs"][m], *(w[k][a:b].astype(np.float64) for k in ("x", "y", "dx", "dy", "tx", "ty")))
+        steps += int(w["work"][m])
+    return time.perf_counter() - t0, steps
+
+
+def cpu_baseline():
+    """Single-thread oracle value-and-gradient over the whole sweep (rank 0, N=1)."""
+    el, steps = _cpu_sweep_chunk(list(range(len(_sweep()["specs"]))))
+    return {"value": steps / el, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": "the whole 512-model sweep once (all 23,544,821 rays): NumPy float64 restatement "
+                      "of run_to_end + squared-residual loss + reverse-mode gradient per model, 1 thread",
+            "seconds": el}
+
+
+def _jax_probe():
+    """Whether the reference's own JAX path imports here (the driver's
+    baseline/_ref install first on the path)."""
+    ref = os.path.join(ROOT, "baseline", "_ref")
+    if os.path.isdir(ref) and ref not in sys.path:
+        sys.path.insert(0, ref)
+    try:
+        import jax  # noqa: F401
+        import temgym_core  # noqa: F401
+    except Exception as e:  # the normal case: jax is not installed on this image
+        return f"unavailable: {type(e).__name__}: {e}"
+    return ("jax and temgym_core import, but the reference has no Aperture component, so it "
+            "cannot express this workload; the timed arm is the NumPy restatement")
+
+
+def _windows(work, target, n_workers, n_windows):
+    """Per step: a window of models (cycling through a fixed shuffled order)
+    holding about ``target`` ray-component steps, dealt to the workers
+    heaviest first onto the least-loaded worker."""
+    order = np.random.default_rng(0).permutation(len(work))
+    pos, out = 0, []
+    for _ in range(n_windows):
+        take, acc = [], 0
+        while acc < target and len(take) < len(work):
+            m = int(order[pos % len(order)])
+            take.append(m)
+            acc += int(work[m])
+            pos += 1
+        chunks, load = [[] for _ in range(n_workers)], [0] * n_workers
+        for m in sorted(take, key=lambda m: -int(work[m])):
+            i = load.index(min(load))
+            chunks[i].append(m)
+            load[i] += int(work[m])
+        out.append([c for c in chunks if c])
+    return out
 
 
 def run_reference(args, world, rank):
@@ -200,30 +256,36 @@ def run_reference(args, world, rank):
         return
     import multiprocessing as mp
     cores = os.cpu_count() or 1
-    # size each step so the whole --steps/--warmup run stays near a minute
-    t_probe = _cpu_probe_chunk((list(range(8)),)) / 8
-    per_worker = int(min(SCAN[0] * SCAN[1] // cores, max(1, 60.0 / (args.steps + args.warmup)
-                                                          / max(t_probe, 1e-6))))
-    per_step = per_worker * cores  # a bounded sample of the 4096-probe scan
+    jax_state = _jax_probe()
+    w = _sweep()
+    total = int(w["work"].sum())
+    # size each step so the whole --steps/--warmup run stays near 90 s
+    t, n = _cpu_sweep_chunk(list(range(8)))
+    rate = n / max(t, 1e-9) * cores
+    target = int(min(total, max(1, 90.0 / (args.steps + args.warmup) * rate)))
+    wins = _windows(w["work"], target, cores, args.steps + args.warmup)
     ctx = mp.get_context("spawn")
-    with ctx.Pool(cores) as pool:
-        def step():
-            chunks = [(list(range(i * per_worker, (i + 1) * per_worker)),) for i in range(cores)]
+    with ctx.Pool(cores, initializer=_sweep) as pool:
+        def step(chunks):
             t0 = time.perf_counter()
-            pool.map(_cpu_probe_chunk, chunks)
-            return time.perf_counter() - t0
-        for _ in range(args.warmup):
-            step()
-        times = [step() for _ in range(args.steps)]
-    t = sum(times)
-    v = args.steps * per_step * RAYS * N_COMPONENTS / t
+            r = pool.map(_cpu_sweep_chunk, chunks)
+            return time.perf_counter() - t0, sum(x[1] for x in r)
+        for i in range(args.warmup):
+            step(wins[i])
+        res = [step(wins[args.warmup + i]) for i in range(args.steps)]
+    secs = sum(r[0] for r in res)
+    steps = sum(r[1] for r in res)
+    v = steps / secs
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded), no dataset",
             "config": headline_config(1),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"{per_step} of 4096 probes per step, {cores} spawn workers"},
+                             "sample": f"per step a window of sweep models holding ~{target} of the "
+                                       f"{total} ray-component steps (windows cycle through all 512 "
+                                       f"models), {cores} spawn workers, NumPy float64 value-and-gradient",
+                             "jax_reference": jax_state},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -251,7 +313,24 @@ def secondary_plain(torch, dev):
     g = plan.capture()
     ms_graph = _time(torch, g.replay, 500)
     n = 65536
+    # CPU baseline (1 thread): the oracle's run_to_end + metres_to_pixels +
+    # into_image + the model's ABCD, repeated for about 3 s
+    import oracle
+    from oracle.rays import ORay
+    g = {"pixel_size": (1e-5, 1e-5), "shape": (256, 256)}
+    reps, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < 3.0:
+        o = oracle.run_to_end(ORay.from_f32(w["x"], w["y"], w["dx"], w["dy"], 0.0, 0.0), w["model"])
+        py, px = oracle.metres_to_pixels(g, o.x, o.y)
+        oracle.into_image(g, py, px)
+        oracle.model_abcd(ORay(np.zeros(1), np.zeros(1), np.zeros(1), np.zeros(1), 0.0, 0.0), w["model"])
+        reps += 1
+    el = (time.perf_counter() - t0) / reps
+    cpu = {"value": 2 * n / el, "unit": UNIT, "cores": 1, "kind": "port", "ms_per_call": 1e3 * el,
+           "sample": f"the whole 65,536-ray workload, {reps} repetitions: NumPy float64 run_to_end + "
+                     "metres_to_pixels + into_image + ABCD, 1 thread"}
     return {"workload": "plain trace 65,536 rays, Lens+Detector 256x256, fused trace+pixels+hist",
+            "cpu_baseline": cpu,
             "ms_api_call": ms_api, "ms_trace_plan": ms_plan, "ms_graph_replay": ms_graph,
             "rays_per_s_graph": n / (ms_graph * 1e-3),
             "ray_component_steps_per_s_graph": 2 * n / (ms_graph * 1e-3),
@@ -283,6 +362,38 @@ def _field_errors(plan, ref, methods, into):
                            "phase_err_rad_bright": ph})
 
 
+def _pixel_sample(shape, n_random=4096):
+    """Flat pixel indices: the central 32 x 32 block (where the diffraction
+    pattern is bright) and n_random seeded random pixels."""
+    h, w = shape
+    yy, xx = np.meshgrid(np.arange(h // 2 - 16, h // 2 + 16), np.arange(w // 2 - 16, w // 2 + 16), indexing="ij")
+    rnd = np.random.default_rng(7).choice(h * w, n_random, replace=False)
+    return np.unique(np.concatenate([(yy * w + xx).ravel(), rnd]))
+
+
+def _oracle_field_leg(images, oracle_fn, n_beams, idx):
+    """CPU baseline of a beamlet-field workload and the error of each GPU
+    image against the float64 oracle (exact k*pathlength reduction) at the
+    pixel sample idx: the oracle's chunked sum over every beam at those
+    pixels, 1 thread, timed."""
+    t0 = time.perf_counter()
+    ref = oracle_fn(idx)
+    el = time.perf_counter() - t0
+    scale = np.max(np.abs(ref))
+    bright = np.abs(ref) > 0.25 * scale
+    errs = {}
+    for name, img in images.items():
+        g = img.reshape(-1)[idx].astype(np.complex128)
+        errs[name] = {"field_rel_err_vs_fp64_oracle": float(np.max(np.abs(g - ref)) / scale),
+                      "phase_err_rad_bright_vs_fp64_oracle":
+                          float(np.max(np.abs(np.angle(g[bright] * np.conj(ref[bright]))))) if bright.any() else None}
+    cpu = {"value": n_beams * idx.size / el, "unit": "beam\u00b7px/s", "cores": 1, "kind": "port",
+           "sample": f"all {n_beams} beams x {idx.size} pixels (the central 32x32 block and seeded random "
+                     "pixels): NumPy complex128 make_gaussian_image restatement, chunks of 64 beams, 1 thread",
+           "seconds": el}
+    return cpu, errs
+
+
 def secondary_input_field(torch, dev, bf16):
     """Input-plane beamlet field (evaluate_gaussian_input_image): 16,384
     overlapping beams on 512 x 512 pixels; separable split-BF16 GEMM and the
@@ -309,6 +420,14 @@ def secondary_input_field(torch, dev, bf16):
     pa = t.FieldPlan(gaussian_rays(wa["rays"]), None, grid=grid)
     ms_a = _time(torch, lambda: pa.evaluate("direct"), 3)
     res["astigmatic_direct"] = {"ms": ms_a, "beam_px_per_s": pairs / (ms_a * 1e-3), "separable": pa.separable}
+    import oracle.field as of
+    idx = _pixel_sample((512, 512), 2048)
+    cpu, errs = _oracle_field_leg({n: plan.evaluate(n).cpu().numpy() for n in ("separable", "direct")},
+                                  lambda i: of.evaluate_gaussian_input_image(w["rays"], w["grid"], pixel_index=i),
+                                  16384, idx)
+    res["cpu_baseline"] = cpu
+    res["separable_gemm"].update(errs["separable"])
+    res["direct_fast"].update(errs["direct"])
     return res
 
 
@@ -340,8 +459,7 @@ def secondary_field(torch, dev, hbm, bf16):
     res["direct_fp64"] = {"ms": ms_f64, "beam_px_per_s": pairs / (ms_f64 * 1e-3)}
     res["speedup_separable_vs_fp64"] = ms_f64 / ms_sep
     res["prep_plan_ms"] = ms_prep
-    # errors against the all-float64 kernel's image (that kernel is held to
-    # 5e-7 of the float64 oracle by the tests; the bench itself runs no oracle)
+    # errors against the all-float64 kernel's image
     ref = plan.evaluate("fp64").clone().cpu().numpy().astype(np.complex128)
     _field_errors(plan, ref, ("separable", "direct"),
                   {"separable": res["separable_gemm"], "direct": res["direct_fast"]})
@@ -350,6 +468,18 @@ def secondary_field(torch, dev, hbm, bf16):
     pa = t.FieldPlan(gaussian_rays(wa["rays"]), build_model(wa["model"]))
     ms_a = _time(torch, lambda: pa.evaluate("direct"), 3)
     res["astigmatic_direct"] = {"ms": ms_a, "beam_px_per_s": pairs / (ms_a * 1e-3), "separable": pa.separable}
+    # CPU baseline and the errors against the float64 oracle at a pixel sample
+    import oracle.field as of
+    idx = _pixel_sample((512, 512))
+    imgs = {n: plan.evaluate(n).cpu().numpy() for n in ("separable", "direct", "fp64")}
+    cpu, errs = _oracle_field_leg(imgs, lambda i: of.make_gaussian_image(w["rays"], w["model"], pixel_index=i),
+                                  16384, idx)
+    res["cpu_baseline"] = cpu
+    for n, e in errs.items():
+        res.setdefault({"separable": "separable_gemm", "direct": "direct_fast", "fp64": "direct_fp64"}[n], {}).update(e)
+    _, ea = _oracle_field_leg({"direct": pa.evaluate("direct").cpu().numpy()},
+                              lambda i: of.make_gaussian_image(wa["rays"], wa["model"], pixel_index=i), 16384, idx)
+    res["astigmatic_direct"].update(ea["direct"])
     return res
 
 
@@ -413,15 +543,53 @@ def secondary_fit(torch, dev):
             lib.tg_trace_vjp(C.byref(m), C.byref(rin), C.byref(gout), None, raw.data_ptr(), ws.data_ptr(),
                              ws.numel(), N.stream_ptr())
     ms_plain = _time(torch, plain, 3) * n_probes / sample
+    cpu = _cpu_fit_step(w)
     return {"workload": "adjoint fit: 32x32 scan x 1,024 rays (1,048,576 rays), 21 parameters, "
                         "loss = sum of squared detector residuals",
+            "cpu_baseline": cpu,
             "loss_grad_ms": ms_lg, "adam_step_graph_ms": ms_step,
             "grad_evals_per_s": 1e3 / ms_step,
-            "ray_component_steps_per_s": n_probes * n * 5 / (ms_step * 1e-3),
+            "ray_component_steps_per_s": n_probes * n * 6 / (ms_step * 1e-3),
             "achieved_gbs": n_probes * n * 8 / (ms_step * 1e-3) / 1e9,
             "loss_before_after_200": [l0, l1], "rel_err_f_defocus_cl": rel.tolist(),
             "plain_per_probe_path_ms_per_grad_eval": ms_plain,
             "speedup_vs_plain_per_probe": ms_plain / ms_step}
+
+
+def _cpu_fit_step(w):
+    """CPU baseline of one fit step (1 thread): per probe, the oracle's
+    float64 value-and-gradient of the squared detector residual (targets from
+    the oracle at the perturbed parameters, formed before the clock starts);
+    the chain rule from per-step sums to the 21 parameters is O(1) per probe
+    and left out."""
+    import oracle
+    from oracle.adjoint import value_and_raw
+    from oracle.rays import ORay
+    from temgymcore_gb300.workloads import stem_fit_probe_spec
+
+    def specs(theta):
+        sg, spec = stem_fit_probe_spec(w, theta, 0)
+        yy, xx = np.meshgrid(np.arange(w["rows"]), np.arange(w["cols"]), indexing="ij")
+        spx, spy = oracle.pixels_to_metres(sg, yy.ravel(), xx.ravel())
+        out = []
+        for p in range(w["rows"] * w["cols"]):
+            sp = [dict(c) for c in spec]
+            for c in sp:
+                if c["kind"] in ("scanner", "descanner"):
+                    c["scan_pos_x"], c["scan_pos_y"] = float(spx[p]), float(spy[p])
+            out.append(sp)
+        return out
+    v = [w[k].astype(np.float64) for k in ("x", "y", "dx", "dy")]
+    tgt = [oracle.run_to_end(ORay(*v, 0.0, 0.0), sp) for sp in specs(w["theta_true"])]
+    s0 = specs(w["theta0"])
+    t0 = time.perf_counter()
+    for sp, tr in zip(s0, tgt):
+        value_and_raw(sp, *v, tr.x, tr.y)
+    el = time.perf_counter() - t0
+    n = len(s0) * v[0].size
+    return {"value": n * 6 / el, "unit": UNIT, "cores": 1, "kind": "port", "ms_per_grad_eval": 1e3 * el,
+            "sample": f"one whole loss + gradient evaluation ({len(s0)} probes x {v[0].size} rays, 6 "
+                      "components): NumPy float64 value-and-gradient per probe, 1 thread"}
 
 
 def run_only(args):
@@ -459,8 +627,8 @@ def run_only(args):
         bt = BatchedTrace([build_model(s) for s in w["specs"]], w["counts"], tile_rays=16384)
         bt.block, bt.rpt = 256, 2
         x, y, dx, dy, tx, ty = (torch.tensor(w[k], device=dev) for k in ("x", "y", "dx", "dy", "tx", "ty"))
-        out, raw = bt.alloc_outputs(), bt.alloc_raw()
-        fn = lambda: bt.run(x, y, dx, dy, out, (tx, ty), raw)  # noqa: E731
+        out, raw, alive, loss = bt.alloc_outputs(), bt.alloc_raw(), bt.alloc_alive(), bt.alloc_loss()
+        fn = lambda: bt.run(x, y, dx, dy, out, (tx, ty), raw, alive=alive, loss=loss)  # noqa: E731
     elif args.only == "plain":
         from temgymcore_gb300.workloads import build_model, plain_trace
         w = plain_trace(seed=0, n=args.rays or 65536)
@@ -490,29 +658,33 @@ def run_only(args):
                       "error_word": t._native.error_word()}))
 
 
-def secondary_batched(torch, dev, hbm):
-    """Batched sweep: 512 models (U{2..12} components), ~2.4e7 rays, forward +
-    adjoint in one persistent launch replayed as a CUDA graph (autotuned launch
-    shape), versus per-model plain launches on the same GPU."""
+def headline_setup(torch, dev):
+    """The batched sweep on the device: plan, autotuned launch shape, and the
+    forward + adjoint launch captured as a CUDA graph."""
+    from temgymcore_gb300.batched import BatchedTrace
+    from temgymcore_gb300.workloads import build_model
+    w = _sweep()
+    models = [build_model(s) for s in w["specs"]]
+    bt = BatchedTrace(models, w["counts"], tile_rays=16384)
+    x, y, dx, dy, tx, ty = (torch.tensor(w[k], device=dev) for k in ("x", "y", "dx", "dy", "tx", "ty"))
+    out, raw, alive, loss = bt.alloc_outputs(), bt.alloc_raw(), bt.alloc_alive(), bt.alloc_loss()
+    best, results = bt.autotune(x, y, dx, dy, out, (tx, ty), raw, alive=alive, loss=loss)
+    g = bt.capture(x, y, dx, dy, out, (tx, ty), raw, alive=alive, loss=loss)
+    return {"w": w, "models": models, "bt": bt, "io": (x, y, dx, dy, tx, ty), "out": out, "raw": raw,
+            "alive": alive, "loss": loss, "graph": g, "best": best, "results": results}
+
+
+def batched_vs_per_model(torch, dev, H, ms):
+    """The plain per-model kernel path on the same GPU (per model: fused
+    forward launch, the residual in torch, the generic adjoint launch) against
+    the batched launch (ms per step)."""
     import ctypes as C
 
     from temgymcore_gb300 import _native as N
-    from temgymcore_gb300.batched import BatchedTrace
     from temgymcore_gb300.run import _rays_struct
-    from temgymcore_gb300.workloads import batched_sweep, build_model
-    w = batched_sweep(seed=0)
-    models = [build_model(s) for s in w["specs"]]
-    bt = BatchedTrace(models, w["counts"])
-    x, y, dx, dy, tx, ty = (torch.tensor(w[k], device=dev) for k in ("x", "y", "dx", "dy", "tx", "ty"))
-    out = bt.alloc_outputs()
-    raw = bt.alloc_raw()
-    best, results = bt.autotune(x, y, dx, dy, out, (tx, ty), raw)
-    g = bt.capture(x, y, dx, dy, out, (tx, ty), raw)
-    ms = _time(torch, g.replay, 10)
-    steps = int(sum(c * len(m) for c, m in zip(w["counts"], models)))
-    total = int(w["counts"].sum())
-    alg = total * (16 + 24 + 8)
-    # per-model plain launches: forward, residual, generic adjoint per model
+    bt, models = H["bt"], H["models"]
+    x, y, dx, dy, tx, ty = H["io"]
+    total = bt.total
     packed = bt._packed
     outs = bt.alloc_outputs()
     gxy = [torch.empty(total, dtype=torch.float32, device=dev) for _ in range(2)]
@@ -540,19 +712,10 @@ def secondary_batched(torch, dev, hbm):
             lib.tg_trace_vjp(C.byref(mm), C.byref(rin), C.byref(gout), None, raws[m].data_ptr(),
                              ws.data_ptr(), ws.numel(), N.stream_ptr())
     ms_plain = _time(torch, plain, 2)
-    return {"workload": f"batched sweep: {len(models)} models, U{{2..12}} components, {total} rays, "
-                        "forward + adjoint (squared-residual loss)",
-            "ms": ms, "ray_component_steps_per_s": steps / (ms * 1e-3), "rays_per_s": total / (ms * 1e-3),
-            "algorithmic_bytes": alg, "achieved_gbs": alg / (ms * 1e-3) / 1e9,
-            "frac_of_hbm": alg / (ms * 1e-3) / 1e9 / hbm,
-            # separate forward and adjoint passes would move 64 B/ray (forward
-            # 16 in + 24 out, adjoint 16 in + 8 targets); the fused launch reads
-            # the inputs once, 48 B/ray
-            "bytes_separate_passes": total * 64,
-            "frac_of_hbm_separate_passes": total * 64 / (ms * 1e-3) / 1e9 / hbm,
-            "autotuned": {"tile_rays": best[0], "block": best[1], "rays_per_thread": best[2]},
-            "autotune_ms": None if results is None else [[r[1], r[2], r[3], r[0]] for r in results],
-            "plain_per_model_ms": ms_plain, "speedup_vs_plain_per_model": ms_plain / ms}
+    return {"workload": "the headline sweep through per-model plain launches (forward, residual, generic "
+                        "adjoint per model; apertures not applied)",
+            "plain_per_model_ms": ms_plain, "batched_ms": ms,
+            "speedup_batched_vs_plain_per_model": ms_plain / ms}
 
 
 def _trace_large_calls(torch, dev, n):
@@ -667,12 +830,12 @@ def secondary_aberrated_scan(torch, dev, hbm):
             "hits": int(out.sum().item())}
 
 
-def run_gpu(args, world, rank, local):
-    import torch
-
+def secondary_stem(torch, dev, hbm, world):
+    """4D-STEM shadow images (64 x 64 scan x 1,024 rays, per-probe dense
+    256 x 256 int32 images): the fused scan kernel, its roofline, the call
+    through the public API with host buffers, and a 1-thread CPU baseline."""
     import temgymcore_gb300 as t
     from temgymcore_gb300.workloads import stem_model
-    dev = torch.device("cuda", torch.cuda.current_device())
     w = _workload()
     model = stem_model(w)
     ray = t.Ray(x=torch.tensor(w["x"], device=dev), y=torch.tensor(w["y"], device=dev),
@@ -680,8 +843,68 @@ def run_gpu(args, world, rank, local):
                 z=0.0, pathlength=0.0)
     n_probes = SCAN[0] * SCAN[1]
     out = torch.empty((n_probes, 256, 256), dtype=torch.int32, device=dev)
+    ms = _time(torch, lambda: t.scan_images(ray, model, out=out), 200)
+    units = n_probes * RAYS * N_COMPONENTS
+    alg = n_probes * 256 * 256 * 4 + RAYS * 16
+    res = {"workload": "4D-STEM shadow images: 64x64 scan (step 1e-9 m, rotation U(0,2pi)), 1024-ray "
+                       "point-source bundle per probe, descan I+N(0,1e-3), camera length 0.1 m, 256x256 "
+                       "int32 images at 5.5e-5 m",
+           "ms": ms, "ray_component_steps_per_s": units / (ms * 1e-3),
+           "roofline": {"kernel": "k_scan_hist", "bound": "hbm", "achieved": alg / (ms * 1e-3) / 1e9,
+                        "peak": hbm, "unit": "GB/s", "frac": alg / (ms * 1e-3) / 1e9 / hbm,
+                        "algorithmic_bytes_per_launch": alg, "traffic": _traffic("k_scan_hist")}}
+    # through the public API with host buffers: the ray bundle host -> device,
+    # the images written by the kernel straight into pinned host memory
+    pin_in = torch.empty((4, RAYS), dtype=torch.float32).pin_memory()
+    for i, k in enumerate(("x", "y", "dx", "dy")):
+        pin_in[i] = torch.from_numpy(w[k])
+    pin_out = torch.empty((n_probes, 256, 256), dtype=torch.int32).pin_memory()
+    dev_in = torch.empty((4, RAYS), dtype=torch.float32, device=dev)
+
+    def e2e_step():
+        dev_in.copy_(pin_in, non_blocking=True)
+        r = t.Ray(x=dev_in[0], y=dev_in[1], dx=dev_in[2], dy=dev_in[3], z=0.0, pathlength=0.0)
+        t.scan_images(r, model, out=pin_out)
+    e2e_ms = _time(torch, e2e_step, 10)
+    res["e2e"] = {"value": units / (e2e_ms * 1e-3), "unit": UNIT, "ms_per_step": e2e_ms,
+                  "h2d_bytes_per_step": int(pin_in.numel() * 4), "d2h_bytes_per_step": int(pin_out.numel() * 4)}
+    del pin_out
+    # CPU baseline (1 thread): the per-probe loop of run_to_end + into_image
+    import oracle
+    from oracle.rays import ORay
+    from temgymcore_gb300.workloads import stem_probe_model
+    g = {k: w["detector"][k] for k in ("pixel_size", "shape")}
+    sg = {k: w["scangrid"][k] for k in ("pixel_size", "shape", "rotation")}
+    probes = 1024
+    t0 = time.perf_counter()
+    for p in range(probes):
+        r, c = divmod(p, SCAN[1])
+        spx, spy = oracle.pixels_to_metres(sg, r, c)
+        o = oracle.run_to_end(ORay(w["x"].astype(np.float64), w["y"].astype(np.float64),
+                                   w["dx"].astype(np.float64), w["dy"].astype(np.float64), 0.0, 0.0),
+                              stem_probe_model(w, float(spx), float(spy)))
+        py, px = oracle.metres_to_pixels(g, o.x, o.y)
+        oracle.into_image(g, py, px)
+    el = time.perf_counter() - t0
+    res["cpu_baseline"] = {"value": probes * RAYS * N_COMPONENTS / el, "unit": UNIT, "cores": 1,
+                           "kind": "port",
+                           "sample": f"{probes} of {n_probes} probes x {RAYS} rays: NumPy float64 run_to_end + "
+                                     "metres_to_pixels + into_image per probe, 1 thread"}
+    return res
+
+
+def run_gpu(args, world, rank, local):
+    import torch
+
+    import temgymcore_gb300 as t
+    dev = torch.device("cuda", torch.cuda.current_device())
+    hbm, bf16, peak_src = _peaks()
+    H = headline_setup(torch, dev)
+    bt, g = H["bt"], H["graph"]
+    w = H["w"]
+    units = int(w["work"].sum())
     for _ in range(args.warmup):
-        t.scan_images(ray, model, out=out)
+        g.replay()
     torch.cuda.synchronize()
     a, b = _events(torch)
     _barrier(world)
@@ -689,100 +912,73 @@ def run_gpu(args, world, rank, local):
     with Clocks(local) as clk:
         a.record()
         for _ in range(args.steps):
-            t.scan_images(ray, model, out=out)
+            g.replay()
         b.record()
         torch.cuda.synchronize()
     _barrier(world)
     ms = a.elapsed_time(b) / args.steps
     ms = _max_over_ranks(ms, world)
-    units = n_probes * RAYS * N_COMPONENTS
     value = world * units / (ms * 1e-3)
     err = t._native.error_word()
-
-    hbm, bf16, peak_src = _peaks()
-    alg_bytes = n_probes * 256 * 256 * 4 + RAYS * 16
+    alg_bytes = bt.total * SWEEP_BYTES_PER_RAY
     achieved = alg_bytes / (ms * 1e-3) / 1e9
-    roof = {"kernel": "k_scan_hist", "bound": "hbm", "achieved": achieved, "peak": hbm,
-            "unit": "GB/s", "frac": achieved / hbm, "peak_source": peak_src,
-            "algorithmic_bytes_per_launch": alg_bytes, "traffic": _traffic("k_scan_hist")}
+    tr = _traffic("k_batch")
+    roof = {"kernel": "k_batch", "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+            "frac": achieved / hbm, "peak_source": peak_src, "algorithmic_bytes_per_launch": alg_bytes,
+            "bytes_per_ray": SWEEP_BYTES_PER_RAY, "traffic": tr,
+            "timing": "graph replay of one step (the work-counter memset + k_batch) with CUDA events"}
     if args.headline_only:
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
                               "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
-                              "scan": list(SCAN), "roofline": roof, "clocks": clk.summary(),
-                              "error_word": err}))
+                              "roofline": roof, "clocks": clk.summary(), "error_word": err}))
         return
 
-    # end to end through the public API with host buffers
-    pin_in = torch.empty((4, RAYS), dtype=torch.float32).pin_memory()
-    for i, k in enumerate(("x", "y", "dx", "dy")):
-        pin_in[i] = torch.from_numpy(w[k])
-    pin_out = torch.empty((n_probes, 256, 256), dtype=torch.int32).pin_memory()
-    dev_in = torch.empty((4, RAYS), dtype=torch.float32, device=dev)
-    e2e_steps = max(3, min(args.steps, 20))
-
-    def e2e_step():
-        # ray bundle host -> device; the images go device -> host inside the
-        # kernel: scan_images writes them straight into the pinned host
-        # buffer across the host link (the link, ~193 GB/s, bounds this)
-        dev_in.copy_(pin_in, non_blocking=True)
-        r = t.Ray(x=dev_in[0], y=dev_in[1], dx=dev_in[2], dy=dev_in[3], z=0.0, pathlength=0.0)
-        t.scan_images(r, model, out=pin_out)
+    # end to end through the public API with host buffers: value_and_grad
+    # copies the six input arrays in from pinned host memory and the loss and
+    # per-step gradient sums back, every step
+    host = [torch.from_numpy(w[k]).pin_memory() for k in ("x", "y", "dx", "dy", "tx", "ty")]
     for _ in range(2):
-        e2e_step()
+        bt.value_and_grad(*host)
     torch.cuda.synchronize()
     _barrier(world)
+    e2e_steps = max(3, min(args.steps, 20))
     a2, b2 = _events(torch)
     a2.record()
     for _ in range(e2e_steps):
-        e2e_step()
+        bt.value_and_grad(*host, sync=False)
     b2.record()
     torch.cuda.synchronize()
     e2e_ms = _max_over_ranks(a2.elapsed_time(b2) / e2e_steps, world)
     e2e = {"value": world * units / (e2e_ms * 1e-3), "unit": UNIT,
-           "h2d_bytes_per_step": int(pin_in.numel() * 4), "d2h_bytes_per_step": int(pin_out.numel() * 4),
-           "ms_per_step": e2e_ms, "steps": e2e_steps}
-    del pin_out
+           "h2d_bytes_per_step": int(sum(h.numel() * 4 for h in host)),
+           "d2h_bytes_per_step": int(len(H["models"]) * 8 + int(bt.info.total_steps) * 4 * 8),
+           "ms_per_step": e2e_ms, "steps": e2e_steps, "call": "BatchedTrace.value_and_grad(host tensors)"}
 
     secondary = {}
     if rank == 0:
-        try:
-            secondary["plain_trace"] = secondary_plain(torch, dev)
-        except Exception as e:  # report, never hide
-            secondary["plain_trace"] = {"error": repr(e)}
-        try:
-            secondary["beamlet_field"] = secondary_field(torch, dev, hbm, bf16)
-        except Exception as e:
-            secondary["beamlet_field"] = {"error": repr(e)}
-        try:
-            secondary["input_field"] = secondary_input_field(torch, dev, bf16)
-        except Exception as e:
-            secondary["input_field"] = {"error": repr(e)}
-        try:
-            secondary["trace_large"] = secondary_trace_large(torch, dev, hbm)
-        except Exception as e:
-            secondary["trace_large"] = {"error": repr(e)}
-        try:
-            secondary["transfer_rays"] = secondary_transfer(torch, dev, hbm)
-        except Exception as e:
-            secondary["transfer_rays"] = {"error": repr(e)}
-        try:
-            secondary["aberrated_scan"] = secondary_aberrated_scan(torch, dev, hbm)
-        except Exception as e:
-            secondary["aberrated_scan"] = {"error": repr(e)}
-        try:
-            secondary["adjoint_fit"] = secondary_fit(torch, dev)
-        except Exception as e:
-            secondary["adjoint_fit"] = {"error": repr(e)}
-        try:
-            secondary["batched_sweep"] = secondary_batched(torch, dev, hbm)
-        except Exception as e:
-            secondary["batched_sweep"] = {"error": repr(e)}
+        secondary["batched_autotune"] = {
+            "chosen": {"tile_rays": H["best"][0], "block": H["best"][1], "rays_per_thread": H["best"][2]},
+            "candidates_ms": None if H["results"] is None else [[r[1], r[2], r[3], r[0]] for r in H["results"]]}
+        for name, fn in (("batched_vs_per_model", lambda: batched_vs_per_model(torch, dev, H, ms)),
+                         ("stem_4d", lambda: secondary_stem(torch, dev, hbm, world)),
+                         ("plain_trace", lambda: secondary_plain(torch, dev)),
+                         ("beamlet_field", lambda: secondary_field(torch, dev, hbm, bf16)),
+                         ("input_field", lambda: secondary_input_field(torch, dev, bf16)),
+                         ("trace_large", lambda: secondary_trace_large(torch, dev, hbm)),
+                         ("transfer_rays", lambda: secondary_transfer(torch, dev, hbm)),
+                         ("aberrated_scan", lambda: secondary_aberrated_scan(torch, dev, hbm)),
+                         ("adjoint_fit", lambda: secondary_fit(torch, dev))):
+            try:
+                secondary[name] = fn()
+            except Exception as e:  # report, never hide
+                secondary[name] = {"error": repr(e)}
+    del H
     cpu = cpu_baseline() if (rank == 0 and world == 1) else None
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32 rays / f64 binning ties", "data": "synthetic (seeded)",
-            "config": headline_config(world),
+            "vs_baseline": None, "dtype": "f32 rays / f64 composition, moments and pathlength",
+            "data": "synthetic (seeded)", "config": headline_config(world),
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps,
             "clocks": clk.summary(), "error_word": err, "secondary": secondary}
     if rank == 0:
@@ -792,7 +988,7 @@ def run_gpu(args, world, rank, local):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--scan", type=int, nargs=2, default=None, metavar=("ROWS", "COLS"),

@@ -427,22 +427,33 @@ typedef struct tg_batch_info {
   int32_t n_models;
   int64_t partial_doubles; /* workspace layout: per-tile moment partials    */
   int64_t moment_doubles;  /* per-model moments                             */
+  int32_t max_record_floats; /* largest per-model forward record (shared memory) */
 } tg_batch_info;
 
-/* Rays of all models concatenated in model order (device float32).  With
- * target_x/target_y (device float32, may be NULL = forward only) the adjoint
- * of loss = sum |(x, y)_out - target|^2 runs too and raw (device float64
- * [total_steps][4], OVERWRITTEN) receives each model's per-step sums (the
- * quantities of tg_trace_vjp), model m's steps starting at
- * 2 * (components of models 0..m-1).  The adjoint is evaluated from per-model
- * moments of the rays (the loss reaches every step through the chain's
- * ray-independent linear part), so it costs a few multiply-adds per ray. */
+/* Rays of all models concatenated in model order (device float32).  The
+ * output coordinates are each model's chain composed in float64 on the host
+ * (one affine map plus one offset per biprism sign) and applied to the input
+ * ray in float32; the per-ray pathlength terms, biprism signs and aperture
+ * tests come from the step-by-step float32 chain.  out_alive (device uint8,
+ * may be NULL) receives 1 for a ray that every aperture passes, else 0; a
+ * blocked ray keeps its traced coordinates.  With target_x/target_y (device
+ * float32, may be NULL = forward only) the adjoint of
+ *   loss = sum over alive rays of |(x, y)_out - target|^2
+ * runs too: raw (device float64 [total_steps][4], OVERWRITTEN) receives each
+ * model's per-step sums (the quantities of tg_trace_vjp), model m's steps
+ * starting at 2 * (components of models 0..m-1), and loss (device float64
+ * [n_models], may be NULL; needs targets) each model's loss.  The adjoint is
+ * evaluated from per-model moments of the rays (the loss reaches every step
+ * through the chain's ray-independent linear part), so it costs a few
+ * multiply-adds per ray. */
 typedef struct tg_batch_io {
   const float *x, *y, *dx, *dy;
   float *out_x, *out_y, *out_dx, *out_dy;
   double *out_pathlength;
   const float *target_x, *target_y;
   double *raw;
+  uint8_t *out_alive; /* may be NULL */
+  double *loss;       /* may be NULL */
 } tg_batch_io;
 
 /*
@@ -451,6 +462,13 @@ typedef struct tg_batch_io {
  * only: with plan == NULL fills *info (sizes); otherwise writes the plan into
  * the host buffer plan (info->plan_bytes) for the caller to copy to the
  * device.  Replaces a Python loop of run_to_end (run.py:85-116) per model.
+ * Each model is composed on the host in float64 into closed forms over its
+ * input ray and biprism signs (output map, pathlength form, the rows of each
+ * biprism / aperture decision).  Statuses: TG_ERR_UNSUPPORTED for an
+ * aberrated lens, per-probe scan positions or direction-cosine propagation;
+ * TG_ERR_TOO_LARGE for a model with more than 16 biprisms or a record of
+ * more than 8192 floats (about 60 components of which 16 biprisms and the
+ * rest apertures).
  */
 int tg_batch_plan(int32_t n_models, const tg_model *models, const int64_t *n_rays,
                   const double *z_in, int32_t tile_rays, void *plan, size_t plan_bytes,
@@ -463,8 +481,7 @@ int tg_batch_plan(int32_t n_models, const tg_model *models, const int64_t *n_ray
  * and writes its per-step sums, so nothing else is launched besides one
  * memset of the work counters.  block in {128, 256, 512}; rays_per_thread in
  * {1, 2, 4}.  workspace: device, info->workspace_bytes, 256-byte aligned.
- * An aperture does not change the traced state here (the outputs carry no
- * mask) and the loss covers every ray.
+ * Statuses: TG_ERR_INVALID for a loss pointer without targets.
  */
 int tg_batch_run(const void *plan_dev, const tg_batch_info *info, const tg_batch_io *io,
                  int32_t block, int32_t rays_per_thread, void *workspace, size_t ws_bytes,

@@ -55,6 +55,48 @@ static void descan_delta(const tg_component& c, double d[4]) {
   }
 }
 
+int component_affine_f64(const tg_component& c, double cm[25]) {
+  std::memset(cm, 0, 25 * sizeof(double));
+  for (int i = 0; i < 5; ++i) cm[6 * i] = 1.0;
+  const double* p = c.p;
+  switch (c.kind) {
+    case TG_PLANE:
+    case TG_APERTURE:
+    case TG_BIPRISM:  // its offset def_x * sign(x) depends on the ray: callers add it
+      return TG_OK;
+    case TG_LENS:
+    case TG_THICKLENS:
+      if (!(p[0] != 0.0)) return TG_ERR_INVALID;
+      cm[10] = -1.0 / p[0];  // [2,0]
+      cm[16] = -1.0 / p[0];  // [3,1]
+      return TG_OK;
+    case TG_SCANNER:
+    case TG_DESCANNER: {
+      if (c.flags & TG_FLAG_PER_PROBE) return TG_ERR_UNSUPPORTED;
+      double d[4];
+      if (c.kind == TG_SCANNER) {
+        d[0] = p[0]; d[1] = p[1]; d[2] = p[2]; d[3] = p[3];
+      } else {
+        descan_delta(c, d);
+      }
+      for (int r = 0; r < 4; ++r) cm[5 * r + 4] = d[r];
+      return TG_OK;
+    }
+    case TG_DEFLECTOR:
+      cm[14] = p[0];  // [2,4]
+      cm[19] = p[1];  // [3,4]
+      return TG_OK;
+    case TG_ROTATOR: {
+      const double a = p[0] * (M_PI / 180.0), ca = std::cos(a), sa = std::sin(a);
+      cm[0] = ca; cm[1] = -sa; cm[5] = sa; cm[6] = ca;
+      cm[12] = ca; cm[13] = -sa; cm[17] = sa; cm[18] = ca;
+      return TG_OK;
+    }
+    default:
+      return TG_ERR_UNSUPPORTED;
+  }
+}
+
 int compile_program(const tg_model* model, bool per_ray_z, double z_scalar,
                     Program* prog) {
   if (!model || !prog || model->n_components < 0 ||

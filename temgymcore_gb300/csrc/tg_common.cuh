@@ -67,6 +67,11 @@ struct Program {
 int compile_program(const tg_model* model, bool per_ray_z, double z_scalar,
                     Program* prog);
 
+// Float64 5x5 affine matrix of one linear component over (x, y, dx, dy, 1)
+// (host).  A biprism gives the identity: its offset def_x * sign(x) depends
+// on the ray.  TG_ERR_UNSUPPORTED for a nonlinear or per-probe component.
+int component_affine_f64(const tg_component& c, double cm[25]);
+
 // Device error word: one per translation unit; tg_get_error_word ORs them.
 #define TG_DEFINE_ERROR_WORD(tu)                                             \
   static __device__ uint32_t g_tg_err;                                       \
