@@ -217,6 +217,17 @@ int tg_abcd_compose(const tg_model *model, const double central[5],
                     double out[25], double *steps);
 
 /*
+ * tg_aber_monomials - the Krivanek wave aberration as a polynomial (host
+ * code, no GPU needed): kc holds the 25 KrivanekCoeffs values in field order
+ * (aberrations.py:5-31); w[28] receives the coefficient of ax^p ay^q of
+ * W (aberrations.py:51-61) at index p * 7 - p * (p - 1) / 2 + q (p + q <= 6),
+ * gx[21] / gy[21] (either may be NULL) those of dW/dax and dW/day
+ * (aberrations.py:64-108) at p * 6 - p * (p - 1) / 2 + q (p + q <= 5).
+ * The kernels evaluate the aberrated lens from these coefficients.
+ */
+int tg_aber_monomials(const double kc[25], double w[28], double *gx, double *gy);
+
+/*
  * tg_trace_vjp - adjoint of tg_trace_fwd (reverse mode, forward state
  * recomputed per ray, nothing stored between the passes).
  * Replaces jax.grad / jax.vjp of run_to_end (README.md:113-160,

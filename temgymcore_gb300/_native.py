@@ -74,6 +74,8 @@ _SIGS = {
                                  C.c_void_p, C.c_int32, C.c_void_p, C.c_size_t, C.c_void_p]),
     "tg_bin": (C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(TgGrid),
                          C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
+    "tg_aber_monomials": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                     C.POINTER(C.c_double)]),
     "tg_abcd_compose": (C.c_int, [C.POINTER(TgModel), C.POINTER(C.c_double),
                                   C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "tg_trace_vjp_workspace": (C.c_size_t, [C.c_int64, C.POINTER(TgModel)]),

@@ -1,14 +1,17 @@
 """Krivanek wave aberrations (drop-in for temgym_core.aberrations,
 aberrations.py:5-108).
 
-``W_krivanek`` and ``grad_W_krivanek`` evaluate the series on NumPy arrays or
-torch tensors (host / torch-device helpers for plotting and set-up).  The GPU
-ray chain evaluates the same series inside the fused kernels from monomial
-coefficients compiled once per component (``AberratedLensKrivanek``).
+``W_krivanek``, ``grad_W_krivanek`` and ``krivanek_coeff_brackets`` evaluate
+the series on NumPy arrays or torch tensors (host / torch-device helpers for
+plotting and set-up) from its expansion into monomials of the slopes
+(``aberration_monomials``), the same coefficients the fused GPU kernels use
+for ``AberratedLensKrivanek``.
 """
 from __future__ import annotations
 
+import ctypes as C
 from dataclasses import astuple, dataclass, fields
+from functools import lru_cache
 
 import numpy as np
 import torch
@@ -63,60 +66,72 @@ def _lib(v):
     return torch if isinstance(v, torch.Tensor) else np
 
 
-def _cos(m, ph, ph0):
-    return _lib(ph).cos(m * (ph - ph0))
+def _off(D: int, p: int) -> int:
+    """Index of the coefficient of x^p y^0 in a degree-D triangle."""
+    return p * (D + 1) - p * (p - 1) // 2
 
 
-def _sin(m, ph, ph0):
-    return _lib(ph).sin(m * (ph - ph0))
+@lru_cache(maxsize=64)
+def _monomials_cached(kc: tuple):
+    from . import _native as N
+    a = (C.c_double * 25)(*kc)
+    w, gx, gy = (C.c_double * 28)(), (C.c_double * 21)(), (C.c_double * 21)()
+    N.check(N.lib().tg_aber_monomials(a, w, gx, gy), "tg_aber_monomials")
+    return tuple(w), tuple(gx), tuple(gy)
+
+
+def aberration_monomials(p):
+    """W as a polynomial in the slopes: coefficients of ax^p ay^q of W
+    (degree <= 6, triangle order p * 7 - p (p - 1) / 2 + q) and of dW/dax,
+    dW/day (degree <= 5).  Every Krivanek term alpha^n cos(m (phi - phi0))
+    is |u|^(n-m) Re(u^m e^(-i m phi0)) with u = ax + i ay and n - m even, a
+    polynomial; the library expands the series once (tg_aber_monomials), and
+    the GPU kernels evaluate the aberrated lens from the same coefficients."""
+    w, gx, gy = _monomials_cached(tuple(as_coeffs(p).as_list()))
+    return np.array(w), np.array(gx), np.array(gy)
+
+
+def _tri_eval(c, D: int, x, y):
+    """Horner evaluation of a degree-D triangle polynomial (NumPy or torch)."""
+    acc = None
+    for pp in range(D, -1, -1):
+        inner = 0.0 * y
+        o = _off(D, pp)
+        for qq in range(D - pp, -1, -1):
+            inner = inner * y + float(c[o + qq])
+        acc = inner if acc is None else acc * x + inner
+    return acc
 
 
 def krivanek_coeff_brackets(phi, p: KrivanekCoeffs):
-    """aberrations.py:42-48: the angular brackets B2..B6."""
-    B2 = p.C10 + p.C12 * _cos(2, phi, p.phi12)
-    B3 = p.C21 * _cos(1, phi, p.phi21) + p.C23 * _cos(3, phi, p.phi23)
-    B4 = p.C30 + p.C32 * _cos(2, phi, p.phi32) + p.C34 * _cos(4, phi, p.phi34)
-    B5 = p.C41 * _cos(1, phi, p.phi41) + p.C43 * _cos(3, phi, p.phi43) + p.C45 * _cos(5, phi, p.phi45)
-    B6 = (p.C50 + p.C52 * _cos(2, phi, p.phi52) + p.C54 * _cos(4, phi, p.phi54)
-          + p.C56 * _cos(6, phi, p.phi56))
-    return B2, B3, B4, B5, B6
+    """aberrations.py:42-48: the angular brackets B2..B6.  W's degree-n
+    homogeneous part is alpha^n B_n / n, so B_n(phi) is n times that part
+    evaluated on the unit circle (cos phi, sin phi)."""
+    w, _, _ = aberration_monomials(p)
+    L = _lib(phi)
+    c, s = L.cos(phi), L.sin(phi)
+    out = []
+    for n in range(2, 7):
+        b = 0.0 * c
+        for pp in range(n + 1):
+            coef = float(w[_off(6, pp) + n - pp])
+            if coef != 0.0:
+                b = b + coef * c ** pp * s ** (n - pp)
+        out.append(n * b)
+    return tuple(out)
 
 
 def W_krivanek(alpha, phi, p):
-    """aberrations.py:51-61: W(alpha, phi)."""
-    p = as_coeffs(p)
-    B2, B3, B4, B5, B6 = krivanek_coeff_brackets(phi, p)
-    a2 = alpha * alpha
-    a3 = a2 * alpha
-    a4 = a2 * a2
-    a6 = a3 * a3
-    return 0.5 * a2 * B2 + (a3 / 3.0) * B3 + 0.25 * a4 * B4 + 0.2 * a4 * alpha * B5 + (a6 / 6.0) * B6
+    """aberrations.py:51-61: W(alpha, phi), as the monomial polynomial at the
+    slopes (alpha cos phi, alpha sin phi)."""
+    w, _, _ = aberration_monomials(p)
+    L = _lib(alpha)
+    return _tri_eval(w, 6, alpha * L.cos(phi), alpha * L.sin(phi))
 
 
 def grad_W_krivanek(alpha_x, alpha_y, p):
-    """aberrations.py:64-108: (dW/d alpha_x, dW/d alpha_y) through the polar
-    chain rule, with alpha = 0 guarded as in the reference."""
-    p = as_coeffs(p)
-    L = _lib(alpha_x)
-    a = L.hypot(alpha_x, alpha_y) if L is np else torch.hypot(alpha_x, alpha_y)
-    phi = L.arctan2(alpha_y, alpha_x)
-    B2, B3, B4, B5, B6 = krivanek_coeff_brackets(phi, p)
-    a2 = a * a
-    a3 = a2 * a
-    a4 = a2 * a2
-    a5 = a4 * a
-    a6 = a3 * a3
-    dW_da = a * B2 + a2 * B3 + a3 * B4 + a4 * B5 + a5 * B6
-    dW_dphi = (0.5 * a2) * (-2.0 * p.C12 * _sin(2, phi, p.phi12))
-    dW_dphi = dW_dphi + (a3 / 3.0) * (-1.0 * p.C21 * _sin(1, phi, p.phi21) - 3.0 * p.C23 * _sin(3, phi, p.phi23))
-    dW_dphi = dW_dphi + (0.25 * a4) * (-2.0 * p.C32 * _sin(2, phi, p.phi32) - 4.0 * p.C34 * _sin(4, phi, p.phi34))
-    dW_dphi = dW_dphi + (0.2 * a5) * (-1.0 * p.C41 * _sin(1, phi, p.phi41) - 3.0 * p.C43 * _sin(3, phi, p.phi43)
-                                      - 5.0 * p.C45 * _sin(5, phi, p.phi45))
-    dW_dphi = dW_dphi + (a6 / 6.0) * (-2.0 * p.C52 * _sin(2, phi, p.phi52) - 4.0 * p.C54 * _sin(4, phi, p.phi54)
-                                      - 6.0 * p.C56 * _sin(6, phi, p.phi56))
-    a_safe = L.where(a == 0, 1e-30, a) if L is np else torch.where(a == 0, torch.full_like(a, 1e-30), a)
-    inv_a = 1.0 / a_safe
-    inv_a2 = inv_a * inv_a
-    dWx = dW_da * (alpha_x * inv_a) + dW_dphi * (-alpha_y * inv_a2)
-    dWy = dW_da * (alpha_y * inv_a) + dW_dphi * (alpha_x * inv_a2)
-    return dWx, dWy
+    """aberrations.py:64-108: (dW/d alpha_x, dW/d alpha_y), the derivative
+    polynomials at the slopes (no polar chain rule, so alpha = 0 needs no
+    guard: the gradient there is the polynomials' constant terms, 0)."""
+    _, gx, gy = aberration_monomials(p)
+    return _tri_eval(gx, 5, alpha_x, alpha_y), _tri_eval(gy, 5, alpha_x, alpha_y)

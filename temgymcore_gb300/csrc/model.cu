@@ -355,6 +355,16 @@ extern "C" int tg_abcd_compose(const tg_model* model, const double central[5],
 }
 
 // ------------------------------------------------------------ library info
+extern "C" int tg_aber_monomials(const double* kc, double* w, double* gx, double* gy) {
+  if (!kc || !w) return TG_ERR_INVALID;
+  aber_monomials(kc, w);
+  double g[2][kAberG];
+  aber_gradient(w, g[0], g[1]);
+  if (gx) std::memcpy(gx, g[0], sizeof(g[0]));
+  if (gy) std::memcpy(gy, g[1], sizeof(g[1]));
+  return TG_OK;
+}
+
 extern "C" const char* tg_version(void) { return "temgym_gb300 0.1.0 (sm_103a)"; }
 
 extern "C" const char* tg_status_string(int s) {

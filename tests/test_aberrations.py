@@ -77,6 +77,20 @@ def test_package_series_matches_oracle():
         np.testing.assert_allclose(got.numpy(), ref, rtol=1e-12, atol=1e-30)
 
 
+def test_brackets_and_zero_slope_match_oracle():
+    from oracle.rays import _brackets, _kc
+    from temgymcore_gb300.aberrations import KrivanekCoeffs, grad_W_krivanek, krivanek_coeff_brackets
+    rng = np.random.default_rng(4)
+    c = _random_coeffs(rng)
+    ph = rng.uniform(-np.pi, np.pi, 32)
+    ref = _brackets(ph, _kc(c))
+    got = krivanek_coeff_brackets(ph, KrivanekCoeffs(**c))
+    for g, r in zip(got, ref):
+        np.testing.assert_allclose(g, r, rtol=1e-12, atol=1e-12 * np.max(np.abs(r)))
+    gx, gy = grad_W_krivanek(np.zeros(3), np.zeros(3), KrivanekCoeffs(**c))
+    assert np.all(gx == 0) and np.all(gy == 0)  # the reference's alpha = 0 guard gives 0 too
+
+
 def test_host_abcd_through_aberrated_lens():
     import oracle
     import temgymcore_gb300 as T
