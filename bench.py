@@ -459,6 +459,14 @@ def secondary_field(torch, dev, hbm, bf16):
     res["direct_fp64"] = {"ms": ms_f64, "beam_px_per_s": pairs / (ms_f64 * 1e-3)}
     res["speedup_separable_vs_fp64"] = ms_f64 / ms_sep
     res["prep_plan_ms"] = ms_prep
+    # the adjoint (tg_field_vjp): gradients of sum |F - T|^2 with respect to
+    # every beam's amplitude, pathlength, x, y, dx, dy and the model's steps
+    T = torch.zeros(plan.shape, dtype=torch.complex64, device=dev)
+    G = 2 * (plan.evaluate("separable").clone() - T)
+    ms_vjp = _time(torch, lambda: plan.vjp(G), 5)
+    res["adjoint"] = {"ms": ms_vjp, "beam_px_per_s": pairs / (ms_vjp * 1e-3),
+                      "note": "one pass over beams x pixels (six complex moments per beam) + float64 "
+                              "forward-mode chain rule per beam"}
     # errors against the all-float64 kernel's image
     ref = plan.evaluate("fp64").clone().cpu().numpy().astype(np.complex128)
     _field_errors(plan, ref, ("separable", "direct"),
@@ -516,6 +524,8 @@ def secondary_fit(torch, dev):
     l1 = float(fit.loss_grad()[0])
     th = fit.theta.cpu().numpy()
     rel = np.abs(th[:3] - w["theta_true"][:3]) / np.abs(w["theta_true"][:3])
+    idf, idt = fit.identifiable(), fit.identifiable(w["theta_true"])
+    rel_id = np.abs(idf - idt) / np.abs(idt)
     # plain per-model path on a sample of probes: tg_trace_fwd + residual + tg_trace_vjp
     sample = 64
     sp = t.scan_positions(fit.model_at(w["theta0"])[1])
@@ -551,7 +561,12 @@ def secondary_fit(torch, dev):
             "grad_evals_per_s": 1e3 / ms_step,
             "ray_component_steps_per_s": n_probes * n * 6 / (ms_step * 1e-3),
             "achieved_gbs": n_probes * n * 8 / (ms_step * 1e-3) / 1e9,
-            "loss_before_after_200": [l0, l1], "rel_err_f_defocus_cl": rel.tolist(),
+            "loss_before_after_200": [l0, l1],
+            "identifiable_rel_err": dict(zip(("A", "b", "K00", "K01", "K10", "K11"), rel_id.tolist())),
+            "rel_err_f_defocus_cl": rel.tolist(),
+            "note_identifiability": "the detector positions fix 6 combinations of the 21 parameters "
+                                    "(position gain A, slope gain b = A defocus + B, 2x2 scan response K); "
+                                    "f, defocus and camera length individually are not identifiable",
             "plain_per_probe_path_ms_per_grad_eval": ms_plain,
             "speedup_vs_plain_per_probe": ms_plain / ms_step}
 
@@ -604,6 +619,12 @@ def run_only(args):
         plan = t.FieldPlan(gaussian_rays(w["rays"]), None, grid=build_model([w["grid"]])[0])
         meth = "direct" if args.only == "field-input-astig" else "separable"
         fn = lambda: plan.evaluate(meth)  # noqa: E731
+    elif args.only == "field-vjp":
+        from temgymcore_gb300.workloads import beamlet_field, build_model, gaussian_rays
+        w = beamlet_field(seed=0, n_beams=args.beams or 16384)
+        plan = t.FieldPlan(gaussian_rays(w["rays"]), build_model(w["model"]))
+        G = 2 * plan.evaluate().clone()
+        fn = lambda: plan.vjp(G)  # noqa: E731
     elif args.only.startswith("field"):
         from temgymcore_gb300.workloads import beamlet_field, build_model, gaussian_rays
         beams = args.beams or 16384
@@ -996,7 +1017,7 @@ def main():
     ap.add_argument("--headline-only", action="store_true",
                     help="skip the secondary workloads, e2e and CPU baseline")
     ap.add_argument("--only", default=None,
-                    help="profile one workload alone: field-separable, field-direct, field-astig, "
+                    help="profile one workload alone: field-separable, field-direct, field-astig, field-vjp, "
                          "field-fp64, field-input, field-input-astig, fit, fit-step, batched, plain, "
                          "trace-forward, trace-image, trace-image-global, trace-adjoint, transfer (--rays N)")
     ap.add_argument("--beams", type=int, default=None)

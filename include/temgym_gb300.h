@@ -636,6 +636,45 @@ int tg_field_direct(const tg_model *model, const tg_beams *beams, const tg_pixel
 int tg_field_separable(const tg_model *model, const tg_beams *beams, const tg_pixel_map *pm,
                        float *out, void *workspace, size_t ws_bytes, void *stream);
 
+/* ---- beamlet field adjoint --------------------------------------------- */
+/* Gradients of a real loss L of the detector field F (complex64 [h][w]) with
+ * respect to the beams and the model.  Every pointer may be NULL (not
+ * computed); all device memory, OVERWRITTEN. */
+typedef struct tg_field_grads {
+  float *amplitude;   /* complex64 pairs [n]: dL/dRe a + i dL/dIm a          */
+  double *pathlength; /* [n]                                                  */
+  double *x, *y, *dx, *dy; /* [n]: the central rays                           */
+  double *raw;        /* [2 * n_components][4]: per-step sums, the layout of
+                         tg_trace_vjp (propagator distance; lens focal length;
+                         deflector def_x, def_y; biprism def_x; scanner /
+                         descanner shifts x, y, dx, dy; rotator angle in rad) */
+} tg_field_grads;
+
+/*
+ * tg_field_vjp - adjoint of tg_field_prep + tg_field_eval (make_gaussian_image,
+ * gaussian.py:225-316, under jax.grad / jax.vjp).  grad: device complex64
+ * [h][w], dL/dRe F + i dL/dIm F (PyTorch's gradient of a complex tensor).
+ * Per beam the field is amp * exp(log pref + i k pl + i Phi(row, col)) with
+ * Phi a complex quadratic in the pixel indices; the call reduces conj(grad) *
+ * field against the six monomials of Phi per beam (one pass over beams x
+ * pixels) and applies the chain rule from Phi's coefficients to the beam and
+ * model parameters in float64 forward mode.  An aberrated lens in the model
+ * returns TG_ERR_UNSUPPORTED.  workspace: device, tg_field_vjp_workspace(n,
+ * h, w) bytes, 256-byte aligned.  Deterministic (fixed-order reductions).
+ */
+size_t tg_field_vjp_workspace(int64_t n_beams, int32_t h, int32_t w);
+int tg_field_vjp(const tg_model *model, const tg_beams *beams, const tg_pixel_map *pm,
+                 const float *grad, const tg_field_grads *out, void *workspace, size_t ws_bytes,
+                 void *stream);
+
+/*
+ * tg_field_vjp_input - the same for the field of the beams in their own
+ * plane (evaluate_gaussian_input_image, gaussian.py:372-409); out->raw must
+ * be NULL (there is no model).
+ */
+int tg_field_vjp_input(const tg_beams *beams, const tg_pixel_map *pm, const float *grad,
+                       const tg_field_grads *out, void *workspace, size_t ws_bytes, void *stream);
+
 /*
  * tg_field_direct_noalloc - tg_field_prep + tg_field_eval(TG_FIELD_DIRECT)
  * in one call that allocates nothing.  No counterpart in the reference: it
@@ -643,14 +682,21 @@ int tg_field_separable(const tg_model *model, const tg_beams *beams, const tg_pi
  * another framework, a pre-sized memory pool, a host that forbids device
  * allocation after start-up).  Its scratch (beam records + partial images) is
  * a fixed 32 MiB array inside the library, held by every GPU that loads the
- * library until the process exits.  Limits: at most 32768 beams, and the
- * records plus one h*w complex64 partial image must fit the 32 MiB (about
- * 3.2 million pixels at 32768 beams, 4.1 million with few beams); larger
- * requests return
- * TG_ERR_TOO_LARGE.  The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress); make that first call before any stream
- * capture.  All calls share the array: calls that overlap on the GPU (other
- * streams, other threads) race and must be serialised by the caller.
+ * library until the process exits.  Limits: at most 32768 beams, and
+ *   part(n) + 8 * h * w <= 33554432 bytes, with
+ *   part(n) = R(R(R(96 n) + 128 n) + 256), R(v) = v rounded up to 256
+ * (the float32 and float64 beam records, a status word, and one complex64
+ * partial image; about 3.2 million pixels at 32768 beams and 4.2 million
+ * with a handful of beams); larger requests return TG_ERR_TOO_LARGE before
+ * any work.  When tg_field_direct's beam chunks would not all fit, the
+ * beams are summed in fewer chunks, so results agree with it to float32
+ * rounding, not bit for bit.  Per-beam preparation flags (tg_field_prep's flags) are not reported
+ * here.  The array's device address is looked up (cudaGetSymbolAddress) on
+ * every call made outside stream capture; a call while its stream is being
+ * captured uses the address of the last uncaptured call on that device, so
+ * make at least one call on each device before capturing one.  All calls
+ * share the array: calls that overlap on the GPU (other streams, other
+ * threads) race and must be serialised by the caller.
  * out: device complex64 [h][w], overwritten.
  */
 int tg_field_direct_noalloc(const tg_model *model, const tg_beams *beams,

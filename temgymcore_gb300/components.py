@@ -273,8 +273,9 @@ class AberratedLensKrivanek(Lens):
     thin-lens slopes u, then slopes u - grad W(u)/f and pathlength
     - (x^2 + y^2)/(2f) + W(u)/f.  ``coeffs``: KrivanekCoeffs (or a dict of
     its fields).  Runs in the forward chain kernels (run_to_end, 4D-STEM
-    scans) and the beamlet-field preparation; the adjoint and batched paths
-    reject it."""
+    scans), the beamlet-field preparation and the trace adjoint (gradients
+    with respect to the rays and the focal length); the batched sweep and the
+    beamlet-field adjoint reject it."""
     coeffs: Any = None
     _kind = N.ABERLENS
     _pfields = ("focal_length",)

@@ -42,6 +42,28 @@ __host__ __device__ __forceinline__ T tri_eval(const T* c, T x, T y) {
   return acc;
 }
 
+// Value and both first partial derivatives of a triangle polynomial of
+// degree D (Horner in x over Horner in y, derivatives carried along).
+template <int D, typename T>
+__host__ __device__ __forceinline__ void tri_eval_d(const T* c, T x, T y, T* v, T* vx, T* vy) {
+  T a = T(0), ax = T(0), ay = T(0);
+#pragma unroll
+  for (int p = D; p >= 0; --p) {
+    T q = T(0), qy = T(0);
+#pragma unroll
+    for (int r = D - p; r >= 0; --r) {
+      qy = qy * y + q;
+      q = q * y + c[tri_off(D, p) + r];
+    }
+    ax = ax * x + a;
+    a = a * x + q;
+    ay = ay * x + qy;
+  }
+  *v = a;
+  *vx = ax;
+  *vy = ay;
+}
+
 // ---- host: Krivanek coefficients -> monomials of W (float64)
 // kc: C10, C12, phi12, C21, phi21, C23, phi23, C30, C32, phi32, C34, phi34,
 //     C41, phi41, C43, phi43, C45, phi45, C50, C52, phi52, C54, phi54, C56, phi56

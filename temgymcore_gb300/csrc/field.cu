@@ -30,22 +30,6 @@ TG_DEFINE_ERROR_WORD(field)
 
 namespace tg {
 
-enum DKind : int32_t { D_NOP = 0, D_FREE = 1, D_LENS = 2, D_SHIFT = 3, D_BIPRISM = 4, D_ROTATE = 5,
-                       D_ABER = 6 };
-
-struct DStep {
-  int32_t kind;
-  int32_t pad;
-  double a[4];
-};
-
-struct DModel {
-  int32_t n;
-  int32_t n_aber;
-  DStep s[kMaxSteps];
-  double aber[kMaxAber][kAberW];  // D_ABER (pad = slot): W monomials, float64
-};
-
 struct cd {
   double re, im;
 };
@@ -131,6 +115,7 @@ struct PrepArgs {
   BeamF64* f64;
   int32_t* flags;  // [0]: non-separable beams seen
   int32_t input_plane;  // 1: field of the beams in their own plane (no model)
+  int32_t unit_amp;     // 1: every amplitude taken as 1 (the field adjoint's records)
 };
 
 __global__ void __launch_bounds__(128)
@@ -229,7 +214,7 @@ k_field_prep(const __grid_constant__ DModel M, const __grid_constant__ PrepArgs 
   // R D R^T with R = [[c, -s], [s, c]]
   cm2 Q1i{cth * cth * qx + sth * sth * qy, cth * sth * qx - sth * cth * qy,
           sth * cth * qx - cth * sth * qy, sth * sth * qx + cth * cth * qy};
-  const cd amp = C((double)A.amp[2 * b], (double)A.amp[2 * b + 1]);
+  const cd amp = A.unit_amp ? C(1.0) : C((double)A.amp[2 * b], (double)A.amp[2 * b + 1]);
   const double k = 2.0 * PI / wl;
   const double hk = 0.5 * k;
   // Phase polynomial (k/2) (s^T S s + L.s + c0) of the pixel position r,
@@ -598,7 +583,7 @@ static int sm_count_field() {
   return cached;
 }
 
-static int build_dmodel(const tg_model* model, double z_in, DModel* dm) {
+int build_dmodel(const tg_model* model, double z_in, DModel* dm) {
   if (!model || model->n_components < 0 || model->n_components > TG_MAX_COMPONENTS)
     return TG_ERR_INVALID;
   if (model->n_components > 0 && !model->components) return TG_ERR_INVALID;
@@ -744,7 +729,7 @@ extern "C" size_t tg_field_workspace(int64_t n_beams, int32_t h, int32_t w, int3
 namespace tg {
 static int field_prep_launch(const DModel& dm, const tg_beams* beams, const tg_pixel_map* pm,
                              void* workspace, size_t ws_bytes, int32_t* flags, void* stream,
-                             int input_plane) {
+                             int input_plane, int unit_amp = 0) {
   if (!beams || !pm || pm->h <= 0 || pm->w <= 0 || beams->n < 0) return TG_ERR_INVALID;
   if (beams->n > 0 && (!beams->x || !beams->y || !beams->dx || !beams->dy || !beams->pathlength ||
                        !beams->amplitude || !beams->waist_xy || !beams->radii))
@@ -775,11 +760,24 @@ static int field_prep_launch(const DModel& dm, const tg_beams* beams, const tg_p
   A.f64 = reinterpret_cast<BeamF64*>(ws + L.f64);
   A.flags = fl;
   A.input_plane = input_plane;
+  A.unit_amp = unit_amp;
   // 64-thread blocks: one thread per beam is all the parallelism there is, so
   // spread the (float64-bound) beams over every SM
   int blocks = (int)((beams->n + 63) / 64);
   k_field_prep<<<blocks, 64, 0, s>>>(dm, A);
   return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
+}
+}  // namespace tg
+
+namespace tg {
+// For the field adjoint (field_adjoint.cu): the bytes of the per-beam records
+// (BeamFast at offset 0, then BeamF64 and a status word), and the records of
+// unit-amplitude beams written there.
+size_t field_records_bytes(int64_t n) { return field_layout(n, 1, 1, TG_FIELD_DIRECT).part; }
+
+int field_prep_unit_amp(const DModel& dm, const tg_beams* beams, const tg_pixel_map* pm, void* records,
+                        size_t bytes, void* stream, int input_plane) {
+  return field_prep_launch(dm, beams, pm, records, bytes, nullptr, stream, input_plane, 1);
 }
 }  // namespace tg
 
@@ -878,19 +876,27 @@ constexpr size_t kNoAllocBytes = (size_t)32 << 20;  // 32 MiB per device
 constexpr int64_t kNoAllocMaxBeams = 32768;
 static __device__ __align__(256) unsigned char g_field_noalloc[kNoAllocBytes];
 static std::mutex g_noalloc_mu;
-static void* g_noalloc_addr[256];  // device address of g_field_noalloc, per device ordinal
+static void* g_noalloc_addr[256];  // last looked-up device address, per device ordinal
+static_assert(sizeof(BeamFast) == 96 && sizeof(BeamF64) == 128, "record sizes stated in the header");
 
 // Device address of the scratch array on the current device.  Host code may
 // not use the symbol itself as a pointer (it is a host-side stand-in), so the
-// address is fetched once per device with that device current.
-static int noalloc_scratch(void** out) {
+// address is looked up with the device current: on every call that is not
+// being captured into a CUDA graph (after a device reset or on a new context
+// the address can change), and taken from the last such call while the
+// stream is being captured.
+static int noalloc_scratch(cudaStream_t s, void** out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) return TG_ERR_CUDA;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) return TG_ERR_CUDA;
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
-  if (!g_noalloc_addr[dev]) {
+  if (cs == cudaStreamCaptureStatusNone) {
     void* p = nullptr;
     if (cudaGetSymbolAddress(&p, g_field_noalloc) != cudaSuccess || !p) return TG_ERR_CUDA;
     g_noalloc_addr[dev] = p;
+  } else if (!g_noalloc_addr[dev]) {
+    return TG_ERR_CUDA;  // no uncaptured call on this device yet
   }
   *out = g_noalloc_addr[dev];
   return TG_OK;
@@ -908,7 +914,7 @@ extern "C" int tg_field_direct_noalloc(const tg_model* model, const tg_beams* be
   if (L.part > kNoAllocBytes || kNoAllocBytes - L.part < per_chunk) return TG_ERR_TOO_LARGE;
   if (!out) return TG_ERR_INVALID;
   void* scratch = nullptr;
-  int st = noalloc_scratch(&scratch);
+  int st = noalloc_scratch(reinterpret_cast<cudaStream_t>(stream), &scratch);
   if (st != TG_OK) return st;
   st = tg_field_prep(model, beams, pm, scratch, L.part, nullptr, stream);
   if (st != TG_OK) return st;

@@ -1,0 +1,729 @@
+// field_adjoint.cu - adjoint of the Gaussian-beamlet detector field
+// (make_gaussian_image, gaussian.py:225-316, and the input-plane field,
+// gaussian.py:372-409, under jax.grad / jax.vjp).
+//
+// Every beam's field is F_b(row, col) = amp_b E_b with
+//   E_b = exp(log pref_b + i k pl_b + i Phi_b(row, col)),
+//   Phi_b = kap_cc col^2 + kap_rr row^2 + kap_rc row col + kap_c col + kap_r row + kap_0
+// (complex coefficients: the real part is the phase, the imaginary part the
+// Gaussian envelope; field_common.cuh).  For a real loss L with upstream
+// gradient G = dL/dRe F + i dL/dIm F (PyTorch's convention for complex
+// tensors) and any real parameter p of beam b,
+//   dL/dp = Re( amp_b [ i sum_j (d kap_j / dp) mu_j + (d log pref / dp) mu_1 ] ),
+//   mu_j  = sum_pixels conj(G) E_b m_j,   m_j in {col^2, row^2, row col, col, row, 1},
+// dL/d pl_b = -k Im(amp_b mu_1) and the amplitude's gradient is conj(mu_1).
+// So the adjoint is
+//   1. k_field_moments: the six complex moments of every beam, a reduction
+//      over (beam, pixel) that evaluates E_b with the direct kernel's exact
+//      fixed-point phase and float32 recurrence (unit-amplitude records),
+//      about the beam's envelope centre for conditioning;
+//   2. k_field_moment_sum: the per-block partials summed in a fixed order;
+//   3. k_field_beam_grad<8>: per beam, the preparation arithmetic again in
+//      float64 forward mode (dual numbers carrying 8 directions: the central
+//      ray's x, y, dx, dy and the model's step parameters) for d kap / dp and
+//      d log pref / dp, contracted with the moments;
+//   4. k_field_model_sum: the model parameters' per-block sums in a fixed
+//      order, written as per-step sums in the layout of tg_trace_vjp.
+// Every reduction runs in a fixed order, so the gradients are deterministic.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "field_common.cuh"
+#include "tg_common.cuh"
+
+namespace tg {
+
+// ------------------------------------------------------------ moments
+constexpr int kML = 16;               // columns per lane (one strip)
+constexpr int kMRows = 8;             // rows per staged band
+constexpr int kMBeams = 64;           // beams per block
+constexpr int kMThreads = 256;
+constexpr int kMCols = 32 * kML;      // columns per block (one warp's strips)
+constexpr float kMSkipLog = -60.f;    // strip below e^-60 of unit amplitude: no contribution
+constexpr float kMRecurMax = 80.f;    // geometric recurrence while |log| stays below
+
+struct MomArgs {
+  const BeamFast* beams;  // unit-amplitude records
+  const float2* g;        // [h][w] upstream gradient
+  int64_t n;
+  int32_t h, w, col_chunks, rows_per_split;
+  float* part;            // [gridDim.x][n][12]
+};
+
+__device__ __forceinline__ float2 exp_turn(float logamp, uint64_t turns) {
+  const int32_t hi = (int32_t)(turns >> 32);  // [-1/2, 1/2) turn
+  const float ang = (float)hi * 1.4629180792671596e-09f;  // 2 pi / 2^32
+  float s, c;
+  __sincosf(ang, &s, &c);
+  const float a = __expf(logamp);
+  return make_float2(a * c, a * s);
+}
+
+__global__ void __launch_bounds__(kMThreads, 3) k_field_moments(const __grid_constant__ MomArgs A) {
+  // the band of the gradient image, transposed so that lane l's column j of
+  // its strip sits at [row][j][l] (conflict-free reads)
+  __shared__ float2 sg[kMRows][kML][32];
+  __shared__ double acc[kMBeams][12];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int cx = blockIdx.x % A.col_chunks, rs = blockIdx.x / A.col_chunks;
+  const int cbase = cx * kMCols;
+  const int col0 = cbase + lane * kML;
+  const int r_begin = rs * A.rows_per_split;
+  const int r_end = min(A.h, r_begin + A.rows_per_split);
+  const int64_t b0 = (int64_t)blockIdx.y * kMBeams;
+  const int nb = (int)min((int64_t)kMBeams, A.n - b0);
+  for (int i = threadIdx.x; i < kMBeams * 12; i += blockDim.x) (&acc[0][0])[i] = 0.0;
+  const uint64_t ucol = (uint64_t)col0, ucol2 = ucol * ucol, ustep = 2 * ucol + 1;
+  for (int band = r_begin; band < r_end; band += kMRows) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < kMRows * kMCols; i += blockDim.x) {
+      const int rr = i / kMCols, cc = i % kMCols;
+      const int row = band + rr, col = cbase + cc;
+      sg[rr][cc % kML][cc / kML] =
+          (row < r_end && col < A.w) ? A.g[(size_t)row * A.w + col] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    for (int k = warp; k < nb; k += kMThreads / 32) {
+      float s[12];
+#pragma unroll
+      for (int i = 0; i < 12; ++i) s[i] = 0.f;
+      if (col0 < A.w) {
+        const BeamFast B = A.beams[b0 + k];
+        for (int rr = 0; rr < kMRows; ++rr) {
+          const int row = band + rr;
+          if (row >= r_end) break;
+          const uint64_t urow = (uint64_t)row;
+          uint64_t th = B.p_cc * ucol2 + B.p_rr * (urow * urow) + B.p_rc * (urow * ucol) + B.p_c * ucol +
+                        B.p_r * urow + B.p_0;
+          uint64_t dth = B.p_cc * ustep + B.p_rc * urow + B.p_c;
+          const float dr = (float)row - B.r0, dc = (float)col0 - B.c0;
+          const float la = B.e0 - (B.b_cc * dc * dc + B.b_rr * dr * dr + B.b_rc * dr * dc + B.l_c * dc + B.l_r * dr);
+          const float dla = -(B.b_cc * (2.f * dc + 1.f) + B.b_rc * dr + B.l_c);
+          const float jl = (float)(kML - 1);
+          const float la_end = la + jl * dla - B.b_cc * jl * (jl - 1.f);
+          const float dla_end = dla - 2.f * B.b_cc * (jl - 1.f);
+          float jv = B.b_cc > 0.f ? 0.5f + dla / (2.f * B.b_cc) : (dla > 0.f ? jl : 0.f);
+          jv = fminf(fmaxf(jv, 0.f), jl);
+          const float la_max = fmaxf(fmaxf(la, la_end), la + jv * dla - B.b_cc * jv * (jv - 1.f));
+          if (!(la_max > kMSkipLog)) continue;
+          float s0r = 0.f, s0i = 0.f, s1r = 0.f, s1i = 0.f, s2r = 0.f, s2i = 0.f;
+          auto add = [&](int j, float2 z) {  // conj(G) E at column col0 + j
+            if (col0 + j < A.w) {
+              const float2 g = sg[rr][j][lane];
+              const float pr = g.x * z.x + g.y * z.y, pi = g.x * z.y - g.y * z.x;
+              const float c = dc + (float)j;
+              s0r += pr; s0i += pi;
+              s1r = fmaf(c, pr, s1r); s1i = fmaf(c, pi, s1i);
+              s2r = fmaf(c * c, pr, s2r); s2i = fmaf(c * c, pi, s2i);
+            }
+          };
+          if (la > -kMRecurMax && fabsf(dla) < kMRecurMax && fabsf(dla_end) < kMRecurMax) {
+            float2 z = exp_turn(la, th), wv = exp_turn(dla, dth);
+            const float rr_ = B.rho_re, ri = B.rho_im;
+#pragma unroll
+            for (int j = 0; j < kML; ++j) {
+              add(j, z);
+              z = make_float2(z.x * wv.x - z.y * wv.y, z.x * wv.y + z.y * wv.x);
+              wv = make_float2(wv.x * rr_ - wv.y * ri, wv.x * ri + wv.y * rr_);
+            }
+          } else {
+            const uint64_t ddth = 2 * B.p_cc;
+#pragma unroll
+            for (int j = 0; j < kML; ++j) {
+              const float fj = (float)j;
+              add(j, exp_turn(la + fj * dla - B.b_cc * fj * (fj - 1.f), th));
+              th += dth;
+              dth += ddth;
+            }
+          }
+          // moments about the centre: 1, dc, dr, dc^2, dr dc, dr^2
+          s[0] += s0r; s[1] += s0i;
+          s[2] += s1r; s[3] += s1i;
+          s[4] = fmaf(dr, s0r, s[4]); s[5] = fmaf(dr, s0i, s[5]);
+          s[6] += s2r; s[7] += s2i;
+          s[8] = fmaf(dr, s1r, s[8]); s[9] = fmaf(dr, s1i, s[9]);
+          s[10] = fmaf(dr * dr, s0r, s[10]); s[11] = fmaf(dr * dr, s0i, s[11]);
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < 12; ++i) {
+        float v = s[i];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) acc[k][i] += (double)v;
+      }
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nb * 12; i += blockDim.x)
+    A.part[((size_t)blockIdx.x * A.n + b0) * 12 + i] = (float)acc[i / 12][i % 12];
+}
+
+// moments[b][i] = sum over the blocks' partials in block order (float64)
+__global__ void k_field_moment_sum(const float* __restrict__ part, int nparts, int64_t n,
+                                   double* __restrict__ mom) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n * 12) return;
+  double a = 0.0;
+  for (int p = 0; p < nparts; ++p) a += (double)part[(size_t)p * n * 12 + i];
+  mom[i] = a;
+}
+
+// ------------------------------------------------------------ dual numbers
+// value + derivatives along N directions (forward mode, float64)
+template <int N>
+struct Du {
+  double v, d[N];
+};
+template <int N>
+__device__ __forceinline__ Du<N> dc_(double v) {
+  Du<N> r;
+  r.v = v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = 0.0;
+  return r;
+}
+template <int N>
+__device__ __forceinline__ Du<N> operator+(const Du<N>& a, const Du<N>& b) {
+  Du<N> r;
+  r.v = a.v + b.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] + b.d[i];
+  return r;
+}
+template <int N>
+__device__ __forceinline__ Du<N> operator-(const Du<N>& a, const Du<N>& b) {
+  Du<N> r;
+  r.v = a.v - b.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] - b.d[i];
+  return r;
+}
+template <int N>
+__device__ __forceinline__ Du<N> operator*(const Du<N>& a, const Du<N>& b) {
+  Du<N> r;
+  r.v = a.v * b.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * b.v + a.v * b.d[i];
+  return r;
+}
+template <int N>
+__device__ __forceinline__ Du<N> operator*(double s, const Du<N>& a) {
+  Du<N> r;
+  r.v = s * a.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = s * a.d[i];
+  return r;
+}
+template <int N>
+__device__ __forceinline__ Du<N> operator/(const Du<N>& a, const Du<N>& b) {
+  Du<N> r;
+  r.v = a.v / b.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = (a.d[i] - r.v * b.d[i]) / b.v;
+  return r;
+}
+
+// complex dual and 2x2 complex dual matrices
+template <int N>
+struct Cx {
+  Du<N> re, im;
+};
+template <int N>
+__device__ __forceinline__ Cx<N> cx_(const Du<N>& re) { return Cx<N>{re, dc_<N>(0.0)}; }
+template <int N>
+__device__ __forceinline__ Cx<N> cx_(double re, double im) { return Cx<N>{dc_<N>(re), dc_<N>(im)}; }
+template <int N>
+__device__ __forceinline__ Cx<N> operator+(const Cx<N>& a, const Cx<N>& b) { return Cx<N>{a.re + b.re, a.im + b.im}; }
+template <int N>
+__device__ __forceinline__ Cx<N> operator-(const Cx<N>& a, const Cx<N>& b) { return Cx<N>{a.re - b.re, a.im - b.im}; }
+template <int N>
+__device__ __forceinline__ Cx<N> operator*(const Cx<N>& a, const Cx<N>& b) {
+  return Cx<N>{a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+template <int N>
+__device__ __forceinline__ Cx<N> operator*(double s, const Cx<N>& a) { return Cx<N>{s * a.re, s * a.im}; }
+template <int N>
+__device__ __forceinline__ Cx<N> operator*(const Du<N>& s, const Cx<N>& a) { return Cx<N>{s * a.re, s * a.im}; }
+template <int N>
+__device__ __forceinline__ Cx<N> operator/(const Cx<N>& a, const Cx<N>& b) {
+  const Du<N> den = b.re * b.re + b.im * b.im;
+  return Cx<N>{(a.re * b.re + a.im * b.im) / den, (a.im * b.re - a.re * b.im) / den};
+}
+
+template <int N>
+struct M2 {
+  Cx<N> a, b, c, d;  // [[a, b], [c, d]]
+};
+template <int N>
+__device__ __forceinline__ M2<N> operator*(const M2<N>& x, const M2<N>& y) {
+  return M2<N>{x.a * y.a + x.b * y.c, x.a * y.b + x.b * y.d, x.c * y.a + x.d * y.c, x.c * y.b + x.d * y.d};
+}
+template <int N>
+__device__ __forceinline__ M2<N> operator+(const M2<N>& x, const M2<N>& y) {
+  return M2<N>{x.a + y.a, x.b + y.b, x.c + y.c, x.d + y.d};
+}
+template <int N>
+__device__ __forceinline__ M2<N> inv2(const M2<N>& m) {  // explicit inverse (inf / nan when singular)
+  const Cx<N> det = m.a * m.d - m.b * m.c;
+  const Cx<N> one = cx_<N>(1.0, 0.0);
+  const Cx<N> r = one / det;
+  const Cx<N> z = cx_<N>(0.0, 0.0);
+  return M2<N>{m.d * r, (z - m.b) * r, (z - m.c) * r, m.a * r};
+}
+// nan_to_num of the reference (gaussian.py:283-287): a non-finite entry
+// becomes 0 (and so does its derivative)
+template <int N>
+__device__ __forceinline__ Du<N> fin0(const Du<N>& a) { return isfinite(a.v) ? a : dc_<N>(0.0); }
+template <int N>
+__device__ __forceinline__ M2<N> nan0(const M2<N>& m) {
+  auto f = [](const Cx<N>& c) { return Cx<N>{fin0(c.re), fin0(c.im)}; };
+  return M2<N>{f(m.a), f(m.b), f(m.c), f(m.d)};
+}
+
+// ------------------------------------------------------------ beam gradient
+constexpr int kND = 8;               // directions per launch
+constexpr int kBGThreads = 64;
+enum DirKind : int32_t { DIR_X = 0, DIR_Y = 1, DIR_DX = 2, DIR_DY = 3, DIR_STEP = 4 };
+
+struct BGArgs {
+  int64_t n;
+  const double *x, *y, *dx, *dy;
+  const double* pl;
+  const float* amp;  // complex64 pairs
+  const double *waist, *radii;
+  const double* wl;
+  double wl_scalar;
+  const double* theta;
+  PixMap pm;
+  const BeamFast* rec;  // unit-amplitude records: the envelope centres
+  const double* mom;    // [n][12] moments about the centres
+  int32_t input_plane;
+  int32_t n_dir;
+  int32_t dir_kind[kND], dir_step[kND], dir_a[kND];  // dir_a: the step's a[] entry, -1 = rotation angle
+  double dir_seed[kND];                              // d a[dir_a] / d parameter
+  double *gx, *gy, *gdx, *gdy;  // per beam, for DIR_X .. DIR_DY directions (may be NULL)
+  double* gpl;                  // per beam d L / d pathlength (may be NULL)
+  float* gamp;                  // per beam complex64 gradient of the amplitude (may be NULL)
+  double* model_part;           // [gridDim.x][kND] sums over the block's beams (DIR_STEP)
+};
+
+__global__ void __launch_bounds__(kBGThreads)
+k_field_beam_grad(const __grid_constant__ DModel M, const __grid_constant__ BGArgs A) {
+  using D = Du<kND>;
+  using X = Cx<kND>;
+  __shared__ double red[kBGThreads][kND];
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double contrib[kND];
+#pragma unroll
+  for (int d = 0; d < kND; ++d) contrib[d] = 0.0;
+  if (b < A.n) {
+    D x = dc_<kND>(A.x[b]), y = dc_<kND>(A.y[b]), dx = dc_<kND>(A.dx[b]), dy = dc_<kND>(A.dy[b]);
+#pragma unroll
+    for (int d = 0; d < kND; ++d) {
+      if (d >= A.n_dir) break;
+      if (A.dir_kind[d] == DIR_X) x.d[d] = 1.0;
+      if (A.dir_kind[d] == DIR_Y) y.d[d] = 1.0;
+      if (A.dir_kind[d] == DIR_DX) dx.d[d] = 1.0;
+      if (A.dir_kind[d] == DIR_DY) dy.d[d] = 1.0;
+    }
+    const D x0 = x, y0 = y, dx0 = dx, dy0 = dy;
+    const double PI = 3.141592653589793;
+    const double wl = A.wl ? A.wl[b] : A.wl_scalar;
+    const double k = 2.0 * PI / wl, hk = 0.5 * k;
+    // Q1^-1 = R diag(1/qx, 1/qy) R^T (gaussian.py:138-177): no directions
+    const double wx = A.waist[2 * b], wy = A.waist[2 * b + 1];
+    const double Rx = A.radii[2 * b], Ry = A.radii[2 * b + 1];
+    const double qxr = isinf(Rx) ? 0.0 : -1.0 / Rx, qxi = wl / (PI * wx * wx);
+    const double qyr = isinf(Ry) ? 0.0 : -1.0 / Ry, qyi = wl / (PI * wy * wy);
+    const double th = A.theta ? A.theta[b] : 0.0;
+    double sth, cth;
+    sincos(th, &sth, &cth);
+    const M2<kND> Q1i{cx_<kND>(cth * cth * qxr + sth * sth * qyr, cth * cth * qxi + sth * sth * qyi),
+                      cx_<kND>(cth * sth * (qxr - qyr), cth * sth * (qxi - qyi)),
+                      cx_<kND>(cth * sth * (qxr - qyr), cth * sth * (qxi - qyi)),
+                      cx_<kND>(sth * sth * qxr + cth * cth * qyr, sth * sth * qxi + cth * cth * qyi)};
+    X Sxx, Syy, Sxy, Lx, Ly, c0;
+    D ox, oy;
+    X dlp[1];  // d log pref as a complex dual (its derivative parts are used)
+    dlp[0] = cx_<kND>(0.0, 0.0);
+    if (A.input_plane) {  // gaussian.py:402-409: s = r1 - r1m, S = Q1^-1, L = 2 theta1m
+      Sxx = Q1i.a;
+      Syy = Q1i.d;
+      Sxy = 0.5 * (Q1i.b + Q1i.c);
+      Lx = cx_<kND>(2.0 * dx0);
+      Ly = cx_<kND>(2.0 * dy0);
+      c0 = cx_<kND>(0.0, 0.0);
+      ox = x0;
+      oy = y0;
+    } else {
+      // central ray and 5x5 ABCD (rows x, y, dx, dy, 1) with the model's
+      // step parameters as directions
+      D m[5][5];
+#pragma unroll
+      for (int i = 0; i < 5; ++i)
+#pragma unroll
+        for (int j = 0; j < 5; ++j) m[i][j] = dc_<kND>(i == j ? 1.0 : 0.0);
+      for (int s = 0; s < M.n; ++s) {
+        const DStep& st = M.s[s];
+        D a[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) a[j] = dc_<kND>(st.a[j]);
+#pragma unroll
+        for (int d = 0; d < kND; ++d) {
+          if (d >= A.n_dir || A.dir_kind[d] != DIR_STEP || A.dir_step[d] != s) continue;
+          if (A.dir_a[d] >= 0) {
+            a[A.dir_a[d] & 3].d[d] = A.dir_seed[d];
+          } else {  // rotation angle (radians): d(cos, sin) = (-sin, cos)
+            a[0].d[d] = -st.a[1];
+            a[1].d[d] = st.a[0];
+          }
+        }
+        switch (st.kind) {
+          case D_FREE:
+            for (int j = 0; j < 5; ++j) {
+              m[0][j] = m[0][j] + a[0] * m[2][j];
+              m[1][j] = m[1][j] + a[0] * m[3][j];
+            }
+            x = x + dx * a[0];
+            y = y + dy * a[0];
+            break;
+          case D_LENS:  // a[1] = 1/f
+            for (int j = 0; j < 5; ++j) {
+              m[2][j] = m[2][j] - m[0][j] * a[1];
+              m[3][j] = m[3][j] - m[1][j] * a[1];
+            }
+            dx = dx - x * a[1];
+            dy = dy - y * a[1];
+            break;
+          case D_SHIFT:
+            m[0][4] = m[0][4] + a[0]; m[1][4] = m[1][4] + a[1];
+            m[2][4] = m[2][4] + a[2]; m[3][4] = m[3][4] + a[3];
+            x = x + a[0]; y = y + a[1]; dx = dx + a[2]; dy = dy + a[3];
+            break;
+          case D_BIPRISM: {
+            const double sg = x.v > 0.0 ? 1.0 : (x.v < 0.0 ? -1.0 : 0.0);
+            m[2][4] = m[2][4] + sg * a[0];
+            dx = dx + sg * a[0];
+          } break;
+          case D_ROTATE:
+            for (int j = 0; j < 5; ++j) {
+              const D r0 = m[0][j], r1 = m[1][j], r2 = m[2][j], r3 = m[3][j];
+              m[0][j] = a[0] * r0 - a[1] * r1;
+              m[1][j] = a[1] * r0 + a[0] * r1;
+              m[2][j] = a[0] * r2 - a[1] * r3;
+              m[3][j] = a[1] * r2 + a[0] * r3;
+            }
+            {
+              const D nx = a[0] * x - a[1] * y, ny = a[1] * x + a[0] * y;
+              const D ndx = a[0] * dx - a[1] * dy, ndy = a[1] * dx + a[0] * dy;
+              x = nx; y = ny; dx = ndx; dy = ndy;
+            }
+            break;
+          default:  // D_NOP (an aberrated lens is rejected on the host)
+            break;
+        }
+      }
+      const M2<kND> Am{cx_<kND>(m[0][0]), cx_<kND>(m[0][1]), cx_<kND>(m[1][0]), cx_<kND>(m[1][1])};
+      const M2<kND> Bm{cx_<kND>(m[0][2]), cx_<kND>(m[0][3]), cx_<kND>(m[1][2]), cx_<kND>(m[1][3])};
+      const M2<kND> Cm{cx_<kND>(m[2][0]), cx_<kND>(m[2][1]), cx_<kND>(m[3][0]), cx_<kND>(m[3][1])};
+      const M2<kND> Dm{cx_<kND>(m[2][2]), cx_<kND>(m[2][3]), cx_<kND>(m[3][2]), cx_<kND>(m[3][3])};
+      // Q2^-1 = (A + B Q1^-1)^-1 (C + D Q1^-1)   (gaussian.py:92-96)
+      const M2<kND> denom = Am + Bm * Q1i;
+      const M2<kND> Q2 = inv2(denom) * (Cm + Dm * Q1i);
+      const M2<kND> Binv = nan0(inv2(Bm));
+      const M2<kND> Q1 = nan0(inv2(Q1i));
+      const D r2mx = m[0][0] * x0 + m[0][1] * y0 + m[0][2] * dx0 + m[0][3] * dy0;
+      const D r2my = m[1][0] * x0 + m[1][1] * y0 + m[1][2] * dx0 + m[1][3] * dy0;
+      // pref = amp / sqrt(det): d log pref = -d det / (2 det)
+      const X det = denom.a * denom.d - denom.b * denom.c;
+      {
+        X dd;
+        dd.re = det.re;
+        dd.im = det.im;
+        dd.re.v = 0.0;  // the quotient below uses only the derivative parts
+        dd.im.v = 0.0;
+        const X q = (-0.5) * (dd / cx_<kND>(det.re.v, det.im.v));
+        dlp[0] = q;
+      }
+      const M2<kND> ABinv = Am * Binv;
+      const M2<kND> P = Q1 * inv2(Bm * (Am * Q1 + Bm));
+      Sxx = Q2.a;
+      Syy = Q2.d;
+      Sxy = 0.5 * (Q2.b + Q2.c);
+      const X bx = Binv.a * cx_<kND>(x0) + Binv.c * cx_<kND>(y0), by = Binv.b * cx_<kND>(x0) + Binv.d * cx_<kND>(y0);
+      const X px = P.a * cx_<kND>(r2mx) + P.c * cx_<kND>(r2my), py = P.b * cx_<kND>(r2mx) + P.d * cx_<kND>(r2my);
+      Lx = 2.0 * (cx_<kND>(m[2][4]) - bx + px);
+      Ly = 2.0 * (cx_<kND>(m[3][4]) - by + py);
+      const X q1 = cx_<kND>(x0) * (ABinv.a * cx_<kND>(x0) + ABinv.b * cx_<kND>(y0)) +
+                   cx_<kND>(y0) * (ABinv.c * cx_<kND>(x0) + ABinv.d * cx_<kND>(y0));
+      const X q2 = cx_<kND>(r2mx) * (P.a * cx_<kND>(r2mx) + P.b * cx_<kND>(r2my)) +
+                   cx_<kND>(r2my) * (P.c * cx_<kND>(r2mx) + P.d * cx_<kND>(r2my));
+      c0 = q1 - q2;
+      ox = m[0][4];
+      oy = m[1][4];
+    }
+    // the polynomial in (row, col): s = s0 + row u + col v
+    const D s0x = dc_<kND>(A.pm.t[5]) - ox, s0y = dc_<kND>(A.pm.t[2]) - oy;
+    const double ux = A.pm.t[3], uy = A.pm.t[0], vx = A.pm.t[4], vy = A.pm.t[1];
+    auto quad = [&](const D& ax, const D& ay, const D& bx2, const D& by2) -> X {  // a^T S b
+      return (ax * bx2) * Sxx + (ay * by2) * Syy + (ax * by2 + ay * bx2) * Sxy;
+    };
+    const D U0 = dc_<kND>(ux), U1 = dc_<kND>(uy), V0 = dc_<kND>(vx), V1 = dc_<kND>(vy);
+    X kap[6];  // cc, rr, rc, c, r, 0
+    kap[0] = hk * quad(V0, V1, V0, V1);
+    kap[1] = hk * quad(U0, U1, U0, U1);
+    kap[2] = hk * (2.0 * quad(U0, U1, V0, V1));
+    kap[3] = hk * (2.0 * quad(s0x, s0y, V0, V1) + V0 * Lx + V1 * Ly);
+    kap[4] = hk * (2.0 * quad(s0x, s0y, U0, U1) + U0 * Lx + U1 * Ly);
+    kap[5] = hk * (quad(s0x, s0y, s0x, s0y) + s0x * Lx + s0y * Ly + c0);
+    // moments about the envelope centre -> moments of the monomials
+    const double* mo = A.mom + b * 12;
+    const double r0 = (double)A.rec[b].r0, cc0 = (double)A.rec[b].c0;
+    double mr[6], mi[6];  // centred: 1, dc, dr, dc^2, dr dc, dr^2
+    for (int i = 0; i < 6; ++i) { mr[i] = mo[2 * i]; mi[i] = mo[2 * i + 1]; }
+    double ur[6], ui[6];  // by kap order: col^2, row^2, row col, col, row, 1
+    ur[5] = mr[0]; ui[5] = mi[0];
+    ur[3] = mr[1] + cc0 * mr[0]; ui[3] = mi[1] + cc0 * mi[0];
+    ur[4] = mr[2] + r0 * mr[0]; ui[4] = mi[2] + r0 * mi[0];
+    ur[0] = mr[3] + 2.0 * cc0 * mr[1] + cc0 * cc0 * mr[0];
+    ui[0] = mi[3] + 2.0 * cc0 * mi[1] + cc0 * cc0 * mi[0];
+    ur[1] = mr[5] + 2.0 * r0 * mr[2] + r0 * r0 * mr[0];
+    ui[1] = mi[5] + 2.0 * r0 * mi[2] + r0 * r0 * mi[0];
+    ur[2] = mr[4] + cc0 * mr[2] + r0 * mr[1] + r0 * cc0 * mr[0];
+    ui[2] = mi[4] + cc0 * mi[2] + r0 * mi[1] + r0 * cc0 * mi[0];
+    // times the amplitude: F = amp E
+    const double ar = (double)A.amp[2 * b], ai = (double)A.amp[2 * b + 1];
+    double wr[6], wi[6];
+    for (int j = 0; j < 6; ++j) {
+      wr[j] = ar * ur[j] - ai * ui[j];
+      wi[j] = ar * ui[j] + ai * ur[j];
+    }
+    // dL/dp = Re(i sum_j dkap_j w_j + dlogpref w_1) = -sum_j Im(dkap_j w_j) + Re(dlogpref w_1)
+#pragma unroll
+    for (int d = 0; d < kND; ++d) {
+      if (d >= A.n_dir) break;
+      double g = 0.0;
+      for (int j = 0; j < 6; ++j) g -= kap[j].re.d[d] * wi[j] + kap[j].im.d[d] * wr[j];
+      g += dlp[0].re.d[d] * wr[5] - dlp[0].im.d[d] * wi[5];
+      contrib[d] = g;
+      const int kd = A.dir_kind[d];
+      if (kd == DIR_X && A.gx) A.gx[b] = g;
+      if (kd == DIR_Y && A.gy) A.gy[b] = g;
+      if (kd == DIR_DX && A.gdx) A.gdx[b] = g;
+      if (kd == DIR_DY && A.gdy) A.gdy[b] = g;
+    }
+    if (A.gpl) A.gpl[b] = -k * wi[5];
+    if (A.gamp) {
+      A.gamp[2 * b] = (float)ur[5];
+      A.gamp[2 * b + 1] = (float)(-ui[5]);
+    }
+  }
+  // the block's sums of the model directions, in a fixed order
+#pragma unroll
+  for (int d = 0; d < kND; ++d) red[threadIdx.x][d] = (d < A.n_dir && A.dir_kind[d] == DIR_STEP) ? contrib[d] : 0.0;
+  __syncthreads();
+  for (int s = kBGThreads / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s)
+#pragma unroll
+      for (int d = 0; d < kND; ++d) red[threadIdx.x][d] += red[threadIdx.x + s][d];
+    __syncthreads();
+  }
+  if (threadIdx.x < kND && A.model_part) A.model_part[(size_t)blockIdx.x * kND + threadIdx.x] = red[0][threadIdx.x];
+}
+
+// raw[target[d]] = sum over blocks (in order) of the group's per-block sums
+struct ModelSumArgs {
+  int32_t n_dir, blocks;
+  int32_t target[kND];  // index into raw (step * 4 + slot), -1 = none
+};
+
+__global__ void k_field_model_sum(const double* __restrict__ part, const __grid_constant__ ModelSumArgs A,
+                                  double* __restrict__ raw) {
+  const int d = threadIdx.x;
+  if (d >= A.n_dir || A.target[d] < 0) return;
+  double a = 0.0;
+  for (int bk = 0; bk < A.blocks; ++bk) a += part[(size_t)bk * kND + d];
+  raw[A.target[d]] = a;
+}
+
+// ------------------------------------------------------------ host
+struct AdjLayout {
+  size_t rec, part, mom, model, total;
+  int col_chunks, row_splits, rows_per_split, beam_chunks, bg_blocks;
+};
+
+static inline size_t al256a(size_t v) { return (v + 255) & ~(size_t)255; }
+
+static AdjLayout adj_layout(int64_t n, int h, int w) {
+  AdjLayout L;
+  std::memset(&L, 0, sizeof(L));
+  L.col_chunks = (w + kMCols - 1) / kMCols;
+  L.beam_chunks = (int)((n + kMBeams - 1) / kMBeams);
+  if (L.beam_chunks < 1) L.beam_chunks = 1;
+  // enough blocks to fill the GPU: split the rows when there are few beams
+  const int want = 2048;
+  int splits = (want + L.col_chunks * L.beam_chunks - 1) / (L.col_chunks * L.beam_chunks);
+  const int max_splits = (h + kMRows - 1) / kMRows;
+  if (splits > max_splits) splits = max_splits;
+  if (splits < 1) splits = 1;
+  L.rows_per_split = ((h + splits - 1) / splits + kMRows - 1) / kMRows * kMRows;
+  L.row_splits = (h + L.rows_per_split - 1) / L.rows_per_split;
+  L.bg_blocks = (int)((n + kBGThreads - 1) / kBGThreads);
+  if (L.bg_blocks < 1) L.bg_blocks = 1;
+  size_t off = 0;
+  L.rec = off; off = al256a(off + field_records_bytes(n));
+  L.part = off; off = al256a(off + (size_t)L.col_chunks * L.row_splits * n * 12 * sizeof(float));
+  L.mom = off; off = al256a(off + (size_t)n * 12 * sizeof(double));
+  L.model = off; off = al256a(off + (size_t)L.bg_blocks * kND * sizeof(double));
+  L.total = off;
+  return L;
+}
+
+struct Dir {
+  int32_t kind, step, a;
+  double seed;
+  int32_t target;  // raw index, -1 for a ray direction
+};
+
+}  // namespace tg
+
+using namespace tg;
+
+extern "C" size_t tg_field_vjp_workspace(int64_t n_beams, int32_t h, int32_t w) {
+  if (n_beams < 0 || h <= 0 || w <= 0) return 0;
+  return adj_layout(n_beams, h, w).total;
+}
+
+static int field_vjp_impl(const tg_model* model, const tg_beams* beams, const tg_pixel_map* pm,
+                          const float* grad, const tg_field_grads* out, void* workspace, size_t ws_bytes,
+                          void* stream) {
+  if (!beams || !pm || !grad || !out || pm->h <= 0 || pm->w <= 0 || beams->n < 0) return TG_ERR_INVALID;
+  const bool input_plane = model == nullptr;
+  if (input_plane && out->raw) return TG_ERR_INVALID;  // no model, no per-step sums
+  const int64_t n = beams->n;
+  if (n > 0 && (!beams->x || !beams->y || !beams->dx || !beams->dy || !beams->pathlength ||
+                !beams->amplitude || !beams->waist_xy || !beams->radii))
+    return TG_ERR_INVALID;
+  DModel dm;
+  std::memset(&dm, 0, sizeof(dm));
+  if (!input_plane) {
+    int st = build_dmodel(model, beams->z, &dm);
+    if (st != TG_OK) return st;
+    if (dm.n_aber) return TG_ERR_UNSUPPORTED;  // the aberrated lens has no field adjoint here
+  }
+  const AdjLayout L = adj_layout(n, pm->h, pm->w);
+  if (!workspace || ws_bytes < L.total) return TG_ERR_WORKSPACE;
+  if (((uintptr_t)workspace & 255) != 0) return TG_ERR_ALIGN;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  char* ws = reinterpret_cast<char*>(workspace);
+  const int nsteps = input_plane ? 0 : dm.n;
+  if (out->raw && cudaMemsetAsync(out->raw, 0, sizeof(double) * 4 * (size_t)nsteps, s) != cudaSuccess)
+    return TG_ERR_CUDA;
+  if (n == 0) return TG_OK;
+  // 1. unit-amplitude records
+  int st = field_prep_unit_amp(dm, beams, pm, ws + L.rec, field_records_bytes(n), stream, input_plane ? 1 : 0);
+  if (st != TG_OK) return st;
+  // 2. moments
+  MomArgs MA;
+  MA.beams = reinterpret_cast<const BeamFast*>(ws + L.rec);
+  MA.g = reinterpret_cast<const float2*>(grad);
+  MA.n = n;
+  MA.h = pm->h;
+  MA.w = pm->w;
+  MA.col_chunks = L.col_chunks;
+  MA.rows_per_split = L.rows_per_split;
+  MA.part = reinterpret_cast<float*>(ws + L.part);
+  k_field_moments<<<dim3(L.col_chunks * L.row_splits, L.beam_chunks), kMThreads, 0, s>>>(MA);
+  double* mom = reinterpret_cast<double*>(ws + L.mom);
+  k_field_moment_sum<<<(int)((n * 12 + 255) / 256), 256, 0, s>>>(MA.part, L.col_chunks * L.row_splits, n, mom);
+  // 3. directions: the central ray's x, y, dx, dy, then the model's step parameters
+  std::vector<Dir> dirs;
+  const bool ray = out->x || out->y || out->dx || out->dy;
+  if (ray) {
+    for (int j = 0; j < 4; ++j) dirs.push_back(Dir{j, 0, 0, 1.0, -1});
+  }
+  if (out->raw) {
+    for (int s2 = 0; s2 < dm.n; ++s2) {
+      const DStep& stp = dm.s[s2];
+      const int kind = model->components[s2 / 2].kind;
+      switch (stp.kind) {
+        case D_FREE: dirs.push_back(Dir{DIR_STEP, s2, 0, 1.0, 4 * s2}); break;
+        case D_LENS: dirs.push_back(Dir{DIR_STEP, s2, 1, -1.0 / (stp.a[0] * stp.a[0]), 4 * s2}); break;
+        case D_BIPRISM: dirs.push_back(Dir{DIR_STEP, s2, 0, 1.0, 4 * s2}); break;
+        case D_ROTATE: dirs.push_back(Dir{DIR_STEP, s2, -1, 1.0, 4 * s2}); break;
+        case D_SHIFT:
+          if (kind == TG_DEFLECTOR) {  // def_x, def_y in slots 0, 1 (as tg_trace_vjp)
+            dirs.push_back(Dir{DIR_STEP, s2, 2, 1.0, 4 * s2});
+            dirs.push_back(Dir{DIR_STEP, s2, 3, 1.0, 4 * s2 + 1});
+          } else {
+            for (int j = 0; j < 4; ++j) dirs.push_back(Dir{DIR_STEP, s2, j, 1.0, 4 * s2 + j});
+          }
+          break;
+        default: break;
+      }
+    }
+  }
+  double* mpart = reinterpret_cast<double*>(ws + L.model);
+  const int groups = dirs.empty() ? 1 : (int)((dirs.size() + kND - 1) / kND);
+  for (int gidx = 0; gidx < groups; ++gidx) {
+    BGArgs B;
+    std::memset(&B, 0, sizeof(B));
+    B.n = n;
+    B.x = beams->x; B.y = beams->y; B.dx = beams->dx; B.dy = beams->dy;
+    B.pl = beams->pathlength;
+    B.amp = beams->amplitude;
+    B.waist = beams->waist_xy;
+    B.radii = beams->radii;
+    B.wl = beams->wavelength;
+    B.wl_scalar = beams->wavelength_scalar;
+    B.theta = beams->theta;
+    B.pm.h = pm->h;
+    B.pm.w = pm->w;
+    for (int i = 0; i < 6; ++i) B.pm.t[i] = pm->t[i];
+    B.rec = MA.beams;
+    B.mom = mom;
+    B.input_plane = input_plane ? 1 : 0;
+    ModelSumArgs S;
+    std::memset(&S, 0, sizeof(S));
+    bool any_model = false;
+    for (int d = 0; d < kND; ++d) {
+      const size_t i = (size_t)gidx * kND + d;
+      S.target[d] = -1;
+      if (i >= dirs.size()) continue;
+      B.n_dir = d + 1;
+      B.dir_kind[d] = dirs[i].kind;
+      B.dir_step[d] = dirs[i].step;
+      B.dir_a[d] = dirs[i].a;
+      B.dir_seed[d] = dirs[i].seed;
+      S.target[d] = dirs[i].target;
+      if (dirs[i].kind == DIR_STEP) any_model = true;
+    }
+    if (gidx == 0) {
+      B.gx = out->x; B.gy = out->y; B.gdx = out->dx; B.gdy = out->dy;
+      B.gpl = out->pathlength;
+      B.gamp = out->amplitude;
+    }
+    B.model_part = mpart;
+    k_field_beam_grad<<<L.bg_blocks, kBGThreads, 0, s>>>(dm, B);
+    if (any_model && out->raw) {
+      S.n_dir = B.n_dir;
+      S.blocks = L.bg_blocks;
+      k_field_model_sum<<<1, kND, 0, s>>>(mpart, S, out->raw);
+    }
+  }
+  return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
+}
+
+extern "C" int tg_field_vjp(const tg_model* model, const tg_beams* beams, const tg_pixel_map* pm,
+                            const float* grad, const tg_field_grads* out, void* workspace, size_t ws_bytes,
+                            void* stream) {
+  if (!model) return TG_ERR_INVALID;
+  return field_vjp_impl(model, beams, pm, grad, out, workspace, ws_bytes, stream);
+}
+
+extern "C" int tg_field_vjp_input(const tg_beams* beams, const tg_pixel_map* pm, const float* grad,
+                                  const tg_field_grads* out, void* workspace, size_t ws_bytes, void* stream) {
+  return field_vjp_impl(nullptr, beams, pm, grad, out, workspace, ws_bytes, stream);
+}

@@ -19,6 +19,8 @@
 
 #include <stdint.h>
 
+#include "tg_common.cuh"
+
 namespace tg {
 
 // Fast record (fixed-point phase, float32 envelope), 96 bytes.
@@ -38,6 +40,33 @@ struct alignas(16) BeamF64 {
   double lnamp;   // ln |pref|
   double pad[2];
 };
+
+// Float64 model of the per-beam preparation: two steps per component (the
+// free-space distance, then the component), as run.py:75-82 inserts them.
+enum DKind : int32_t { D_NOP = 0, D_FREE = 1, D_LENS = 2, D_SHIFT = 3, D_BIPRISM = 4, D_ROTATE = 5,
+                       D_ABER = 6 };
+
+struct DStep {
+  int32_t kind;
+  int32_t pad;
+  double a[4];  // FREE: d; LENS: f, 1/f; SHIFT: x, y, dx, dy; BIPRISM: def_x; ROTATE: cos, sin; ABER: f
+};
+
+struct DModel {
+  int32_t n;
+  int32_t n_aber;
+  DStep s[kMaxSteps];
+  double aber[kMaxAber][kAberW];  // D_ABER (pad = slot): W monomials, float64
+};
+
+// Host: a tg_model (paraxial) -> DModel with the beams starting at z_in.
+int build_dmodel(const tg_model* model, double z_in, DModel* dm);
+
+// Host (field.cu): bytes of the per-beam records of n beams (BeamFast array at
+// offset 0), and the records of the beams with every amplitude taken as 1.
+size_t field_records_bytes(int64_t n);
+int field_prep_unit_amp(const DModel& dm, const tg_beams* beams, const tg_pixel_map* pm, void* records,
+                        size_t bytes, void* stream, int input_plane);
 
 // Pixel map of the detector: pixels -> metres (grid.py:155-182).
 struct PixMap {

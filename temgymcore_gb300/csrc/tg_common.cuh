@@ -384,6 +384,35 @@ struct Adj {
   float lx, ly, ldx, ldy, lpl;
 };
 
+// Reverse of the aberrated lens (aber_forward): q is the state entering the
+// lens (the caller recomputes it: the slope map u -> u - grad W(u) / f has no
+// closed-form inverse), a the adjoint after the lens, turned into the adjoint
+// before it; c0 receives d L / d f.  With u = d - r / f:
+//   d(d')/du = I - H / f (H the Hessian of W at u), d pl' / du = grad W / f,
+//   d(d')/d(1/f) = -r - grad W + (H r) / f, d pl'/d(1/f) = W - (grad W . r) / f,
+//   d pl' / d(1/(2f)) = -(x^2 + y^2).
+__device__ __forceinline__ void aber_reverse(const float* aw, float k1, float h, const RayS& q, Adj& ad,
+                                             float& c0) {
+  const float x = q.x, y = q.y;
+  const float ux = fmaf(-x, k1, q.dx), uy = fmaf(-y, k1, q.dy);
+  const float W = tri_eval<6>(aw, ux, uy);
+  float Wx, Hxx, Hxy1, Wy, Hxy2, Hyy;
+  tri_eval_d<5>(aw + kAberW, ux, uy, &Wx, &Hxx, &Hxy1);
+  tri_eval_d<5>(aw + kAberW + kAberG, ux, uy, &Wy, &Hxy2, &Hyy);
+  const float Hxy = 0.5f * (Hxy1 + Hxy2);
+  const float ldx = ad.ldx, ldy = ad.ldy, lpl = ad.lpl;
+  const float lux = ldx * (1.f - k1 * Hxx) - ldy * (k1 * Hxy) + lpl * k1 * Wx;
+  const float luy = -ldx * (k1 * Hxy) + ldy * (1.f - k1 * Hyy) + lpl * k1 * Wy;
+  const float dk1 = ldx * (-x - Wx + k1 * (Hxx * x + Hxy * y)) + ldy * (-y - Wy + k1 * (Hxy * x + Hyy * y)) +
+                    lpl * (W - k1 * (Wx * x + Wy * y));
+  const float dh = -lpl * (x * x + y * y);
+  c0 = -k1 * k1 * (dk1 + 0.5f * dh);
+  ad.ldx = lux;
+  ad.ldy = luy;
+  ad.lx = ad.lx - k1 * lux - 2.f * h * x * lpl;
+  ad.ly = ad.ly - k1 * luy - 2.f * h * y * lpl;
+}
+
 // Reverse one step: on entry r is the state after the step and a the adjoint
 // after it; on exit both describe the state before it.  c receives the step's
 // parameter sensitivities for this ray.  gz receives dL/dz_in (OP_FREE_VARZ).

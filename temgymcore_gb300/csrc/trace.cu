@@ -656,7 +656,7 @@ __device__ __forceinline__ float warp_sum(float v) {
 
 __device__ __forceinline__ int op_nsums(int kind) {
   switch (kind) {
-    case OP_FREE: case OP_FREE_VARZ: case OP_LENS: case OP_BIPRISM: case OP_ROTATE: return 1;
+    case OP_FREE: case OP_FREE_VARZ: case OP_LENS: case OP_BIPRISM: case OP_ROTATE: case OP_ABER: return 1;
     case OP_DEFLECT: return 2;
     case OP_SHIFT: case OP_PROBE_SHIFT: return 4;
     default: return 0;
@@ -672,9 +672,14 @@ constexpr int kVjpRays = 8;  // rays per thread on the aligned path
 // warps per SM.  Measured at 16.8 M rays: 0.197 ms with 4 rays (79
 // registers, 3 blocks), 0.251 ms with 2, 0.375 ms with 1, 0.215 ms with 8
 // unbounded (144 registers, 1 block), 0.172 ms with 8 bounded.
-template <int R>
+// ABER: the model holds aberrated lenses.  Their slope map has no
+// closed-form inverse, so at each one the reverse walk recomputes the state
+// entering it from the ray's input (forward steps up to the lens) and applies
+// the lens's adjoint (aber_reverse); the other steps invert as usual.
+template <int R, bool ABER>
 __global__ void __launch_bounds__(kVjpThreads, 2)
 k_trace_vjp(const __grid_constant__ Program P, const __grid_constant__ VjpArgs A) {
+  const float* aw = ABER ? &P.aber[0][0] : nullptr;
   // per-warp float32 step sums (each warp owns a row: no atomics, no float64
   // in the ray loop); combined in float64 in warp order at the end
   __shared__ float wacc[kVjpThreads / 32][kMaxSteps * 4];
@@ -724,7 +729,7 @@ k_trace_vjp(const __grid_constant__ Program P, const __grid_constant__ VjpArgs A
       const Op op = P.op[s];
 #pragma unroll
       for (int k = 0; k < R; ++k)
-        op_forward(op, nullptr, r[k], dvf[k], sb[k], alive[k]);
+        op_forward(op, nullptr, r[k], dvf[k], sb[k], alive[k], aw);
     }
     for (int s = P.n_steps - 1; s >= 0; --s) {
       const Op op = P.op[s];
@@ -732,7 +737,16 @@ k_trace_vjp(const __grid_constant__ Program P, const __grid_constant__ VjpArgs A
 #pragma unroll
       for (int k = 0; k < R; ++k) {
         float ck[4] = {0.f, 0.f, 0.f, 0.f};
-        op_reverse(op, nullptr, r[k], ad[k], sb[k], dvf[k], ck, gz[k]);
+        if (ABER && op.kind == OP_ABER) {
+          RayS q{x[k], y[k], dx[k], dy[k], 0.f};  // recompute the state entering the lens
+          uint64_t sq = 0;
+          bool aq = true;
+          for (int t = 0; t < s; ++t) op_forward(P.op[t], nullptr, q, dvf[k], sq, aq, aw);
+          aber_reverse(aw + op.aux * kAberFloats, op.c[0], op.c[1], q, ad[k], ck[0]);
+          r[k] = q;
+        } else {
+          op_reverse(op, nullptr, r[k], ad[k], sb[k], dvf[k], ck, gz[k]);
+        }
         c[0] += ck[0]; c[1] += ck[1]; c[2] += ck[2]; c[3] += ck[3];
       }
       if (sums) {
@@ -793,7 +807,7 @@ static int vjp_grid(int64_t n) {
   static int per_sm = 0;
   if (!per_sm) {
     int v = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_trace_vjp<kVjpRays>, kVjpThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_trace_vjp<kVjpRays, false>, kVjpThreads, 0);
     per_sm = v > 0 ? v : 1;
   }
   const int64_t per_block = (int64_t)kVjpThreads * kVjpRays;
@@ -821,7 +835,6 @@ extern "C" int tg_trace_vjp(const tg_model* model, const tg_rays* in, const tg_r
   Program P;
   int st = compile_program(model, in->z != nullptr, in->z_scalar, &P);
   if (st != TG_OK) return st;
-  if (P.n_aber > 0) return TG_ERR_UNSUPPORTED;  // nonlinear lens: forward paths only
   if (P.n_probe_ops) return TG_ERR_UNSUPPORTED;
   if (in->n == 0) return TG_OK;
   const int grid = vjp_grid(in->n);
@@ -844,8 +857,13 @@ extern "C" int tg_trace_vjp(const tg_model* model, const tg_rays* in, const tg_r
              al16(A.gy) && al16(A.gdx) && al16(A.gdy) && (!A.ix || al16(A.ix)) &&
              (!A.iy || al16(A.iy)) && (!A.idx || al16(A.idx)) && (!A.idy || al16(A.idy));
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-  if (vec) k_trace_vjp<kVjpRays><<<grid, kVjpThreads, 0, s>>>(P, A);
-  else k_trace_vjp<1><<<grid, kVjpThreads, 0, s>>>(P, A);
+  if (P.n_aber > 0) {
+    if (vec) k_trace_vjp<4, true><<<grid, kVjpThreads, 0, s>>>(P, A);
+    else k_trace_vjp<1, true><<<grid, kVjpThreads, 0, s>>>(P, A);
+  } else {
+    if (vec) k_trace_vjp<kVjpRays, false><<<grid, kVjpThreads, 0, s>>>(P, A);
+    else k_trace_vjp<1, false><<<grid, kVjpThreads, 0, s>>>(P, A);
+  }
   if (A.partial) {
     int width = P.n_steps * 4;
     k_reduce_partials<<<(width + 127) / 128, 128, 0, s>>>(A.partial, grid, width, raw);

@@ -151,6 +151,13 @@ class StemFit:
                 hist[i] = self.out[0]
         return hist
 
+    def identifiable(self, theta=None) -> np.ndarray:
+        """``identifiable_combinations`` of theta (default: the current
+        parameters) for this scan and lens gap."""
+        th = self.theta if theta is None else theta
+        th = th.detach().cpu().numpy() if isinstance(th, torch.Tensor) else th
+        return identifiable_combinations(th, self.gap, self.rows, self.cols)
+
     def model_at(self, theta, spx=0.0, spy=0.0):
         """The equivalent component model at one scan position (reference form)."""
         th = np.asarray(theta.detach().cpu() if isinstance(theta, torch.Tensor) else theta, np.float64)
@@ -162,3 +169,29 @@ class StemFit:
                 Descanner(z=dfc, scan_pos_x=spx, scan_pos_y=spy, descan_error=err),
                 Lens(z=dfc + self.gap, focal_length=f),
                 Detector(z=dfc + cl, pixel_size=(1e-5, 1e-5), shape=(256, 256))]
+
+
+def identifiable_combinations(theta, lens_gap: float, rows: int, cols: int) -> np.ndarray:
+    """The six combinations of the 21 parameters that the detector positions
+    determine (parameter vectors with equal combinations give the same loss).
+    From the scan plane the lens section maps (x, dx) to x_det = A x + B dx,
+    A = 1 - (cl - gap) / f, B = gap + (cl - gap)(1 - gap / f); a bundle ray
+    (x0, dx0) reaches the scan plane at x0 + defocus dx0; the scan adds the
+    descan matrix's position rows to x and its slope rows to dx, times the
+    scan position S (row, col) (S: the ScanGrid's pixel -> metre map, which
+    holds the rotation and the step).  So the detector sees only
+      a = A, b = A defocus + B   (the bundle's position and slope gains),
+      K = (A M[0:2, 0:2] + B M[2:4, 0:2]) S   (2 x 2: scan pixel -> detector),
+    returned as [a, b, K00, K01, K10, K11]; the descan tilt columns
+    M[:, 2:4] do not enter at all (the scan tilt is 0)."""
+    th = np.asarray(theta, np.float64)
+    f, dfc, cl, rot, step = th[:5]
+    M = th[5:].reshape(4, 4)
+    g = float(lens_gap)
+    A = 1.0 - (cl - g) / f
+    B = g + (cl - g) * (1.0 - g / f)
+    t = ScanGrid(z=dfc, pixel_size=(step, step), shape=(int(rows), int(cols)),
+                 rotation=rot).pixels_to_metres_mat
+    S = np.array([[t[1, 0], t[1, 1]], [t[0, 0], t[0, 1]]])  # (x, y) per (row, col)
+    K = (A * M[0:2, 0:2] + B * M[2:4, 0:2]) @ S
+    return np.concatenate([[A, A * dfc + B], K.reshape(4)])

@@ -60,6 +60,18 @@ N.register("tg_field_eval", C.c_int, [C.c_int32, C.c_int64, C.POINTER(TgPixelMap
                                       C.c_void_p, C.c_size_t, C.c_void_p])
 
 
+class TgFieldGrads(C.Structure):
+    _fields_ = [("amplitude", C.c_void_p), ("pathlength", C.c_void_p), ("x", C.c_void_p),
+                ("y", C.c_void_p), ("dx", C.c_void_p), ("dy", C.c_void_p), ("raw", C.c_void_p)]
+
+
+N.register("tg_field_vjp_workspace", C.c_size_t, [C.c_int64, C.c_int32, C.c_int32])
+N.register("tg_field_vjp", C.c_int, [C.POINTER(N.TgModel), C.POINTER(TgBeams), C.POINTER(TgPixelMap),
+                                     C.c_void_p, C.POINTER(TgFieldGrads), C.c_void_p, C.c_size_t, C.c_void_p])
+N.register("tg_field_vjp_input", C.c_int, [C.POINTER(TgBeams), C.POINTER(TgPixelMap), C.c_void_p,
+                                           C.POINTER(TgFieldGrads), C.c_void_p, C.c_size_t, C.c_void_p])
+
+
 def _f64(v, n, dev, width=None):
     if isinstance(v, torch.Tensor):
         t = v.detach().to(device=dev, dtype=torch.float64)
@@ -200,6 +212,8 @@ class FieldPlan:
             raise ValueError(f"unknown method {method!r}")
         self.method = method
         self.out = torch.empty(self.shape, dtype=torch.complex64, device=self.dev)
+        self.comps = comps
+        self._vjp_ws = None
 
     def evaluate(self, method: str | None = None, out: torch.Tensor | None = None) -> torch.Tensor:
         method = method or self.method
@@ -214,11 +228,109 @@ class FieldPlan:
     def separable(self) -> bool:
         return int(self.flags.item()) == 0
 
+    def vjp(self, grad: torch.Tensor, beams: bool = True, model: bool = True) -> dict:
+        """Gradients of a real loss L from its gradient with respect to the
+        field, ``grad`` = dL/dRe F + i dL/dIm F (complex (H, W), PyTorch's
+        convention): per beam ``amplitude`` (complex64), ``pathlength``,
+        ``x``, ``y``, ``dx``, ``dy`` (float64) when ``beams``, and the model's
+        per-step sums ``raw`` (float64 [2 * components, 4], the layout of the
+        trace adjoint) when ``model`` (tg_field_vjp / tg_field_vjp_input)."""
+        n, dev = self.beams.n, self.dev
+        g = torch.view_as_real(grad.to(device=dev, dtype=torch.complex64).reshape(self.shape).contiguous())
+        if self._vjp_ws is None:
+            nb = N.lib().tg_field_vjp_workspace(n, self.pm.h, self.pm.w)
+            self._vjp_ws = torch.empty(nb + 256, dtype=torch.uint8, device=dev)
+        ws = self._vjp_ws
+        off = (-ws.data_ptr()) % 256
+        res = {}
+        out = TgFieldGrads()
+        if beams:
+            res["amplitude"] = torch.empty(n, dtype=torch.complex64, device=dev)
+            out.amplitude = torch.view_as_real(res["amplitude"]).data_ptr()
+            for k in ("pathlength", "x", "y", "dx", "dy"):
+                res[k] = torch.empty(n, dtype=torch.float64, device=dev)
+                setattr(out, k, res[k].data_ptr())
+        if model and self.comps is not None:
+            res["raw"] = torch.empty((2 * len(self.comps), 4), dtype=torch.float64, device=dev)
+            out.raw = res["raw"].data_ptr()
+        if self.comps is None:
+            st = N.lib().tg_field_vjp_input(C.byref(self.beams.struct()), C.byref(self.pm), g.data_ptr(),
+                                            C.byref(out), ws.data_ptr() + off, ws.numel() - off,
+                                            N.stream_ptr())
+            N.check(st, "tg_field_vjp_input")
+        else:
+            m, keep = pack_model(self.comps)
+            st = N.lib().tg_field_vjp(C.byref(m), C.byref(self.beams.struct()), C.byref(self.pm),
+                                      g.data_ptr(), C.byref(out), ws.data_ptr() + off, ws.numel() - off,
+                                      N.stream_ptr())
+            del keep
+            N.check(st, "tg_field_vjp")
+        return res
+
+
+_BEAM_FIELDS = ("amplitude", "pathlength", "x", "y", "dx", "dy")
+
+
+class _FieldFn(torch.autograd.Function):
+    """The detector (or input-plane) field with its hand-written adjoint:
+    forward through FieldPlan.evaluate, backward through FieldPlan.vjp."""
+
+    @staticmethod
+    def forward(ctx, spec, *inputs):
+        plan = spec["plan"]
+        ctx.spec = spec
+        return plan.evaluate(spec["method"]).clone()
+
+    @staticmethod
+    def backward(ctx, grad):
+        spec = ctx.spec
+        plan = spec["plan"]
+        r = plan.vjp(grad, beams=bool(spec["beam_inputs"]), model=bool(spec["params"]))
+        out = []
+        for name, t in spec["beam_inputs"]:
+            if t is None:
+                out.append(None)
+                continue
+            g = r[name]
+            if t.numel() == 1 and g.numel() != 1:
+                g = g.sum()
+            out.append(g.to(t.dtype).reshape(t.shape))
+        if spec["params"]:
+            from .run import param_gradient
+            for (i, path, t) in spec["params"]:
+                out.append(param_gradient(plan.comps, i, path, r["raw"]).to(t.dtype).reshape(t.shape))
+        return (None, *out)
+
+
+def _field_autograd(gaussian_rays: GaussianRay, model, method: str, grid=None):
+    """The field through _FieldFn when a beam field (amplitude, pathlength,
+    x, y, dx, dy) or a model parameter tensor requires grad, else None."""
+    if not torch.is_grad_enabled():
+        return None
+    from .run import _grad_params
+    beam_inputs = []
+    for name in _BEAM_FIELDS:
+        v = getattr(gaussian_rays, name)
+        beam_inputs.append((name, v if isinstance(v, torch.Tensor) and v.requires_grad else None))
+    params = _grad_params(_check_model(model)) if model is not None else []
+    if not params and all(t is None for _, t in beam_inputs):
+        return None
+    plan = FieldPlan(gaussian_rays, model, method, grid=grid)
+    spec = {"plan": plan, "method": plan.method, "beam_inputs": beam_inputs, "params": params}
+    tensors = [t for _, t in beam_inputs if t is not None] + [t for (_, _, t) in params]
+    spec["beam_inputs"] = [(n_, t) for n_, t in beam_inputs if t is not None]
+    return _FieldFn.apply(spec, *tensors)
+
 
 def make_gaussian_image(gaussian_rays: GaussianRay, model, batch_size: int = 128,
                         method: str = "auto") -> torch.Tensor:
     """Complex64 detector field (H, W) of the Gaussian beamlets after ``model``
-    (gaussian.py:225-273)."""
+    (gaussian.py:225-273).  Differentiable (hand-written adjoint,
+    tg_field_vjp) with respect to the beams' amplitude, pathlength, x, y, dx,
+    dy and the model's parameter tensors that require grad."""
+    out = _field_autograd(gaussian_rays, model, method)
+    if out is not None:
+        return out
     plan = FieldPlan(gaussian_rays, model, method)
     return plan.evaluate().clone()
 
@@ -226,7 +338,12 @@ def make_gaussian_image(gaussian_rays: GaussianRay, model, batch_size: int = 128
 def evaluate_gaussian_input_image(gaussian_rays: GaussianRay, grid, batch_size: int = 128,
                                   method: str = "auto") -> torch.Tensor:
     """Complex64 field (H, W) of the Gaussian beamlets in their own plane,
-    sampled at the pixel centres of ``grid`` (gaussian.py:372-400)."""
+    sampled at the pixel centres of ``grid`` (gaussian.py:372-400).
+    Differentiable with respect to the beams' amplitude, pathlength, x, y,
+    dx, dy (tg_field_vjp_input)."""
+    out = _field_autograd(gaussian_rays, None, method, grid=grid)
+    if out is not None:
+        return out
     plan = FieldPlan(gaussian_rays, None, method, grid=grid)
     return plan.evaluate().clone()
 

@@ -90,3 +90,35 @@ def test_invalid_arguments_rejected_without_gpu():
     m.n_components = 1
     m.components = ctypes.cast(comp, ctypes.POINTER(N.TgComponent))
     assert lib.tg_abcd_compose(ctypes.byref(m), cen, out, None) == -2
+
+
+def test_noalloc_size_limit_matches_its_stated_formula():
+    """tg_field_direct_noalloc's size check follows the header's formula
+    part(n) + 8 h w <= 32 MiB: at the largest image it passes the size check
+    (the call then stops on the missing beam arrays, or without a GPU on the
+    device lookup) and one row more is rejected with TG_ERR_TOO_LARGE; the
+    stated capacities (about 3.2 million pixels at 32768 beams, 4.2 million
+    with a few) are no larger than the formula gives."""
+    import ctypes as C
+
+    from temgymcore_gb300 import _native as N
+    from temgymcore_gb300 import gaussian as G
+    lib = N.lib()
+    lib.tg_field_direct_noalloc.restype = C.c_int
+    lib.tg_field_direct_noalloc.argtypes = [C.POINTER(N.TgModel), C.POINTER(G.TgBeams),
+                                            C.POINTER(G.TgPixelMap), C.c_void_p, C.c_void_p]
+    r = lambda v: (v + 255) // 256 * 256  # noqa: E731
+    part = lambda n: r(r(r(96 * n) + 128 * n) + 256)  # noqa: E731
+    cap = lambda n: ((32 << 20) - part(n)) // 8  # noqa: E731
+    assert cap(32768) >= 3.2e6 and cap(1) >= 4.19e6
+    m = N.TgModel()
+    m.n_components = 0
+    for n, wd in ((32768, 1000), (1, 2048), (7, 1800)):
+        b = G.TgBeams()
+        b.n = n  # beam arrays left NULL: nothing runs past the size check
+        pm = G.TgPixelMap()
+        pm.w = wd
+        pm.h = cap(n) // wd
+        assert lib.tg_field_direct_noalloc(C.byref(m), C.byref(b), C.byref(pm), 8, None) != -5
+        pm.h += 1
+        assert lib.tg_field_direct_noalloc(C.byref(m), C.byref(b), C.byref(pm), 8, None) == -5

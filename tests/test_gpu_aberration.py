@@ -5,7 +5,8 @@ kernel, and the beamlet field prepared through the lens (its Jacobian enters
 each beam's ABCD).  Coordinates <= 2e-6 normwise (float32 ray state with the
 aberration polynomial evaluated in float32); pixels and histograms bit-exact
 given the same float32 coordinates; field tolerances as for the other
-beamlet-field tests.  The adjoint and batched paths reject the component."""
+beamlet-field tests; the reverse mode through the lens against central
+differences of the oracle.  The batched path rejects the component."""
 import ctypes as C
 
 import numpy as np
@@ -123,17 +124,64 @@ def test_field_through_aberrated_lens(cuda):
     assert t._native.error_word() == 0
 
 
-def test_adjoint_and_batched_reject_aberrated_lens(cuda):
+def test_adjoint_through_aberrated_lens(cuda):
+    """Reverse mode through the aberrated lens (the state entering it is
+    recomputed, its slope map has no closed-form inverse): per-ray input
+    gradients and the lens focal length's gradient of a weighted sum of the
+    outputs, against central differences of the oracle's polar-form series
+    (<= 1e-4 normwise)."""
+    import temgymcore_gb300 as t
+    rng = np.random.default_rng(5)
+    n = 4096
+    x0, y0 = rng.uniform(-1e-3, 1e-3, n), rng.uniform(-1e-3, 1e-3, n)
+    dx0, dy0 = rng.normal(0, 1e-3, n), rng.normal(0, 1e-3, n)
+    v = [a.astype(np.float32).astype(np.float64) for a in (x0, y0, dx0, dy0)]
+    coeffs = _coeffs(rng, 0.2, 3e-3)
+    spec = [{"kind": "lens", "z": 0.2, "focal_length": 0.5},
+            {"kind": "aberrated_lens", "z": 0.5, "focal_length": 0.2, "coeffs": coeffs},
+            {"kind": "deflector", "z": 0.7, "def_x": 2e-4, "def_y": -1e-4},
+            {"kind": "detector", "z": 1.0, "pixel_size": (1e-5, 1e-5), "shape": (8, 8)}]
+    wts = rng.normal(size=(5, n))
+    wts[4] *= 1e-3  # the pathlength's weight
+    f_t = torch.tensor(0.2, dtype=torch.float64, requires_grad=True)
+    xs = [torch.tensor(a, dtype=torch.float32, device=cuda, requires_grad=True) for a in v]
+    model = [t.Lens(z=0.2, focal_length=0.5),
+             t.AberratedLensKrivanek(z=0.5, focal_length=f_t, coeffs=t.KrivanekCoeffs(**coeffs)),
+             t.Deflector(z=0.7, def_x=2e-4, def_y=-1e-4),
+             t.Detector(z=1.0, pixel_size=(1e-5, 1e-5), shape=(8, 8))]
+    out = t.run_to_end(t.Ray(x=xs[0], y=xs[1], dx=xs[2], dy=xs[3], z=0.0, pathlength=0.0), model)
+    W = [torch.tensor(w, device=cuda) for w in wts]
+    loss = sum((W[i] * getattr(out, k).double()).sum() for i, k in enumerate(("x", "y", "dx", "dy")))
+    loss = loss + (W[4] * out.pathlength).sum()
+    loss.backward()
+
+    def per_ray(vals, sp):
+        o = oracle.run_to_end(ORay(*vals, 0.0, 0.0), sp)
+        return (wts[0] * o.x + wts[1] * o.y + wts[2] * o.dx + wts[3] * o.dy
+                + wts[4] * np.broadcast_to(o.pathlength, (n,)))
+    for j, k in enumerate(("x", "y", "dx", "dy")):
+        h = 1e-7 * (1e-3 if k in ("x", "y") else 1e-3)
+        vp = [a.copy() for a in v]
+        vm = [a.copy() for a in v]
+        vp[j] += h
+        vm[j] -= h
+        fd = (per_ray(vp, spec) - per_ray(vm, spec)) / (2 * h)
+        assert normwise_err(np_(xs[j].grad), fd) <= 1e-4, (k, normwise_err(np_(xs[j].grad), fd))
+
+    def total(fv):
+        sp = [dict(c) for c in spec]
+        sp[1]["focal_length"] = fv
+        return float(per_ray(v, sp).sum())
+    fd_f = (total(0.2 + 1e-8) - total(0.2 - 1e-8)) / 2e-8
+    assert abs(float(f_t.grad) - fd_f) <= 1e-4 * abs(fd_f), (float(f_t.grad), fd_f)
+
+
+def test_batched_rejects_aberrated_lens(cuda):
     import temgymcore_gb300 as t
     from temgymcore_gb300 import _native as N
     from temgymcore_gb300.batched import BatchedTrace
     model = [t.AberratedLensKrivanek(z=0.5, focal_length=0.2, coeffs={"C30": 1e3}),
              t.Detector(z=1.0, pixel_size=(1e-5, 1e-5), shape=(8, 8))]
-    x = torch.zeros(4, device=cuda, requires_grad=True)
-    out = t.run_to_end(t.Ray(x=x, y=torch.zeros(4, device=cuda), dx=torch.zeros(4, device=cuda),
-                             dy=torch.zeros(4, device=cuda), z=0.0, pathlength=0.0), model)
-    with pytest.raises(RuntimeError):
-        out.x.sum().backward()
     with pytest.raises(RuntimeError):
         BatchedTrace([model], [16])
     assert N.error_word() == 0

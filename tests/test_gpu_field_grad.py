@@ -1,0 +1,177 @@
+"""Adjoint of the beamlet field (tg_field_vjp behind make_gaussian_image /
+evaluate_gaussian_input_image under torch.autograd) against central finite
+differences of the float64 oracle (oracle/field.py, exact k*pl reduction).
+
+Loss L = Re sum conj(T) F for a seeded complex image T (its gradient with
+respect to F is T; a loss without a large constant keeps the float64
+differences of the oracle well above their rounding).  Bounds (normwise over
+each group of gradients): x, y, dx, dy, focal length, detector z and the
+amplitudes <= 1e-4 relative (finite-difference steps where the float64
+differences have converged); the pathlength gradient equals k times the
+gradient with respect to the amplitude's phase (F depends on pl only through
+exp(i k pl)) to 1e-6."""
+import numpy as np
+import pytest
+import torch
+
+import oracle.field as OF
+from conftest import normwise_err
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-4
+
+
+def _rays_t(d, dev, req=True):
+    """GaussianRay with differentiable float64 / complex64 device tensors."""
+    import temgymcore_gb300 as t
+    f = lambda k: torch.tensor(np.asarray(d[k], np.float64), device=dev, requires_grad=req)  # noqa: E731
+    amp = torch.tensor(np.asarray(d["amplitude"], np.complex64), device=dev, requires_grad=req)
+    return t.GaussianRay(x=f("x"), y=f("y"), dx=f("dx"), dy=f("dy"), z=d["z"], pathlength=f("pathlength"),
+                         amplitude=amp, waist_xy=d["waist_xy"], radii_of_curv=d["radii_of_curv"],
+                         wavelength=d["wavelength"], theta=d["theta"])
+
+
+def _target(shape, seed, scale):
+    rng = np.random.default_rng(seed)
+    return (scale * (rng.normal(size=shape) + 1j * rng.normal(size=shape))).astype(np.complex128)
+
+
+def _oracle_loss(rays, model, target):
+    F = OF.make_gaussian_image(rays, model, phase_mode="exact")
+    return float(np.real(np.sum(np.conj(target) * F)))
+
+
+def _loss_t(F, T):
+    return (torch.conj(T) * F).real.sum()
+
+
+def _fd(fn, v, h):
+    return (fn(v + h) - fn(v - h)) / (2 * h)
+
+
+@pytest.mark.parametrize("astig", [True, False])
+def test_field_gradients_against_oracle_fd(cuda, astig):
+    from temgymcore_gb300 import make_gaussian_image
+    from temgymcore_gb300.components import Detector, Lens
+    from temgymcore_gb300.workloads import beamlet_field
+    w = beamlet_field(seed=2, n_beams=48, det_shape=(40, 56), det_px=3e-5, astigmatic=astig)
+    rays_np = w["rays"]
+    # a lens of 0.4 m at 0.5 m: the detector at 1.0 m sits 0.1 m past the
+    # back focal plane, so the focal length and the detector z both matter
+    spec = [{"kind": "lens", "z": 0.5, "focal_length": 0.4},
+            {"kind": "detector", "z": 1.0, "pixel_size": (3e-5, 3e-5), "shape": (40, 56)}]
+    f_t = torch.tensor(0.4, dtype=torch.float64, requires_grad=True)
+    z_t = torch.tensor(1.0, dtype=torch.float64, requires_grad=True)
+    model = [Lens(z=0.5, focal_length=f_t), Detector(z=z_t, pixel_size=(3e-5, 3e-5), shape=(40, 56))]
+    F0 = OF.make_gaussian_image(rays_np, spec, phase_mode="exact")
+    T = _target(F0.shape, 5, 0.5 * np.abs(F0).max())
+    r = _rays_t(rays_np, cuda)
+    F = make_gaussian_image(r, model)
+    _loss_t(F, torch.tensor(T.astype(np.complex64), device=cuda)).backward()
+    assert normwise_err(F.detach().cpu().numpy(), F0) <= 1e-5
+    beams = [0, 7, 23, 41]
+    # central ray positions and slopes (steps where the float64 differences
+    # have converged: the loss is 1e5 times less sensitive to the slopes)
+    for key, h in (("x", 1e-13), ("y", 1e-13), ("dx", 1e-10), ("dy", 1e-10)):
+        ref, got = [], []
+        for b in beams:
+            def fn(v, b=b, key=key):
+                d = dict(rays_np)
+                a = np.array(d[key], np.float64)
+                a[b] = v
+                d[key] = a
+                return _oracle_loss(d, spec, T)
+            ref.append(_fd(fn, float(rays_np[key][b]), h))
+            got.append(float(getattr(r, key).grad[b]))
+        assert normwise_err(got, ref) <= TOL, (key, got, ref)
+    # amplitudes (the loss is quadratic in them: central differences are exact)
+    ref, got = [], []
+    for b in beams:
+        for part in (1.0, 1j):
+            def fn(v, b=b, part=part):
+                d = dict(rays_np)
+                a = np.array(d["amplitude"], np.complex128)
+                a[b] = a[b] + v * part
+                d["amplitude"] = a
+                return _oracle_loss(d, spec, T)
+            ref.append(_fd(fn, 0.0, 1e-3))
+        g = complex(r.amplitude.grad[b])
+        got += [g.real, g.imag]
+    assert normwise_err(got, ref) <= TOL
+    # model parameters: the lens focal length and the detector's z
+    def f_loss(v):
+        s2 = [dict(c) for c in spec]
+        s2[0]["focal_length"] = v
+        return _oracle_loss(rays_np, s2, T)
+
+    def z_loss(v):
+        s2 = [dict(c) for c in spec]
+        s2[1]["z"] = v
+        return _oracle_loss(rays_np, s2, T)
+    ref = [_fd(f_loss, 0.4, 1e-10), _fd(z_loss, 1.0, 1e-9)]
+    got = [float(f_t.grad), float(z_t.grad)]
+    assert normwise_err(got, ref) <= TOL, (got, ref)
+    # pathlength: F depends on pl through exp(i k pl) only
+    k = 2 * np.pi / rays_np["wavelength"]
+    a = r.amplitude.detach().cpu().numpy().astype(np.complex128)
+    ga = r.amplitude.grad.cpu().numpy().astype(np.complex128)
+    dphi = np.real(np.conj(ga) * 1j * a)
+    assert normwise_err(r.pathlength.grad.cpu().numpy(), k * dphi) <= 1e-6
+
+
+def test_input_field_gradients_against_oracle_fd(cuda):
+    from temgymcore_gb300 import evaluate_gaussian_input_image
+    from temgymcore_gb300.workloads import build_model, input_field
+    w = input_field(seed=3, n_beams=40, grid_shape=(36, 44), px=1e-5)
+    rays_np, grid_spec = w["rays"], w["grid"]
+    grid = build_model([grid_spec])[0]
+    F0 = OF.evaluate_gaussian_input_image(rays_np, grid_spec, phase_mode="exact")
+    T = _target(F0.shape, 6, 0.5 * np.abs(F0).max())
+    r = _rays_t(rays_np, cuda)
+    F = evaluate_gaussian_input_image(r, grid)
+    _loss_t(F, torch.tensor(T.astype(np.complex64), device=cuda)).backward()
+    beams = [1, 9, 30]
+    for key, h in (("x", 1e-9), ("y", 1e-9), ("dx", 1e-7), ("dy", 1e-7)):
+        ref, got = [], []
+        for b in beams:
+            def fn(v, b=b, key=key):
+                d = dict(rays_np)
+                a = np.array(d[key], np.float64)
+                a[b] = v
+                d[key] = a
+                return float(np.real(np.sum(np.conj(T) * OF.evaluate_gaussian_input_image(
+                    d, grid_spec, phase_mode="exact"))))
+            ref.append(_fd(fn, float(rays_np[key][b]), h))
+            got.append(float(getattr(r, key).grad[b]))
+        assert normwise_err(got, ref) <= TOL, (key, got, ref)
+
+
+def test_field_vjp_full_size_directional_derivative(cuda):
+    """16,384 beams on 512 x 512 pixels (the benchmark's beamlet workload):
+    the adjoint's gradient along random directions of the central rays against
+    central differences of the all-float64 field kernel on the GPU."""
+    import temgymcore_gb300 as t
+    from temgymcore_gb300.workloads import beamlet_field, build_model, gaussian_rays
+    w = beamlet_field(seed=0)
+    comps = build_model(w["model"])
+    plan = t.FieldPlan(gaussian_rays(w["rays"]), comps, method="fp64")
+    F = plan.evaluate("fp64").clone()
+    T = torch.tensor(_target(plan.shape, 8, 0.5 * float(F.abs().max())).astype(np.complex64), device=cuda)
+    r = plan.vjp(T)  # L = Re sum conj(T) F: its gradient image is T
+    rng = np.random.default_rng(4)
+    for key in ("x", "dx"):
+        v = rng.normal(size=16384)
+        # the same phase change for both: the field is ~1e6 times less
+        # sensitive to the slopes than to the positions at the focal plane
+        h = 1e-13 if key == "x" else 1e-7
+
+        def L(sign):
+            d = dict(w["rays"])
+            d[key] = np.asarray(d[key], np.float64) + sign * h * v
+            p = t.FieldPlan(gaussian_rays(d), comps, method="fp64")
+            Fp = p.evaluate("fp64").to(torch.complex128)
+            return float((torch.conj(T.to(torch.complex128)) * Fp).real.sum())
+        ref = (L(1) - L(-1)) / (2 * h)
+        got = float((r[key].cpu().numpy() * v).sum())
+        assert abs(got - ref) <= 1e-3 * abs(ref), (key, got, ref)
