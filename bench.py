@@ -646,7 +646,7 @@ def run_only(args):
         from temgymcore_gb300.workloads import batched_sweep, build_model
         w = batched_sweep(seed=0, n_models=args.models or 512)
         bt = BatchedTrace([build_model(s) for s in w["specs"]], w["counts"], tile_rays=16384)
-        bt.block, bt.rpt = 256, 2
+        bt.block, bt.rpt = 512, 2
         x, y, dx, dy, tx, ty = (torch.tensor(w[k], device=dev) for k in ("x", "y", "dx", "dy", "tx", "ty"))
         out, raw, alive, loss = bt.alloc_outputs(), bt.alloc_raw(), bt.alloc_alive(), bt.alloc_loss()
         fn = lambda: bt.run(x, y, dx, dy, out, (tx, ty), raw, alive=alive, loss=loss)  # noqa: E731
