@@ -161,7 +161,7 @@ int tg_trace_fwd(const tg_model *model, const tg_rays *in, tg_rays *out,
  * tg_trace_image_workspace(n, grid) is non-zero and workspace holds that many
  * bytes (16-byte aligned device memory), each SM keeps a private copy of the
  * detector in shared memory and the copies are summed at the end (one shared
- * atomic per warp and bin instead of one global atomic); otherwise the call
+ * atomic per hit instead of one global atomic); otherwise the call
  * is tg_trace_fwd.  The workspace query is 0 for detectors above ~100k pixels
  * or fewer than 32 rays per pixel, where global atomics are the better choice.
  */

@@ -52,7 +52,8 @@ N.register("tg_batch_run", C.c_int, [C.c_void_p, C.POINTER(TgBatchInfo), C.POINT
 
 # (tile rays, block, rays per thread) candidates
 CANDIDATES = [(2048, 256, 2), (4096, 256, 2), (4096, 128, 4), (8192, 256, 2), (16384, 256, 2),
-              (4096, 256, 4), (4096, 512, 2), (8192, 256, 4), (2048, 256, 1)]
+              (4096, 256, 4), (4096, 512, 2), (8192, 256, 4), (2048, 256, 1),
+              (8192, 512, 2), (16384, 512, 2), (16384, 512, 1)]
 
 
 class _TuneCache:

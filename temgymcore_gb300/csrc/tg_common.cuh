@@ -260,6 +260,21 @@ __device__ __forceinline__ void mbar_expect_tx(uint32_t a, uint32_t bytes) {
                : "memory");
 }
 
+// Per-thread asynchronous 16-byte copy global -> shared (cached in L2 only);
+// both addresses 16-byte aligned.  A thread that reads back only the slots it
+// filled itself needs no barrier: cp_async_wait orders its own copies.
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+}
+
 __device__ __forceinline__ bool mbar_try(uint32_t a, uint32_t parity) {
   uint32_t ok;
   asm volatile(
@@ -331,7 +346,7 @@ __device__ __forceinline__ void op_forward(const Op& op, const float4* pshift,
     } break;
     case OP_LENS: {
       float x = r.x, y = r.y;
-      r.plv -= (x * x + y * y) * op.c[1];
+      r.plv = fmaf(-fmaf(x, x, y * y), op.c[1], r.plv);
       r.dx = fmaf(-x, op.c[0], r.dx);
       r.dy = fmaf(-y, op.c[0], r.dy);
     } break;
@@ -349,12 +364,12 @@ __device__ __forceinline__ void op_forward(const Op& op, const float4* pshift,
       r.dy += s.w;
     } break;
     case OP_DEFLECT: {
-      r.plv += r.dx * r.x + r.dy * r.y;
+      r.plv += fmaf(r.dx, r.x, r.dy * r.y);
       r.dx += op.c[0];
       r.dy += op.c[1];
     } break;
     case OP_BIPRISM: {
-      r.plv += r.dx * r.x + r.dy * r.y;
+      r.plv += fmaf(r.dx, r.x, r.dy * r.y);
       float s = sgnf(r.x);
       sbits |= (uint64_t)(s > 0.f ? 1u : (s < 0.f ? 2u : 0u)) << (2 * op.aux);
       r.dx = fmaf(op.c[0], s, r.dx);
@@ -362,14 +377,14 @@ __device__ __forceinline__ void op_forward(const Op& op, const float4* pshift,
     case OP_ROTATE: {
       float c = op.c[0], s = op.c[1];
       float x = r.x, y = r.y, dx = r.dx, dy = r.dy;
-      r.x = x * c - y * s;
-      r.y = x * s + y * c;
-      r.dx = dx * c - dy * s;
-      r.dy = dx * s + dy * c;
+      r.x = fmaf(x, c, -(y * s));
+      r.y = fmaf(x, s, y * c);
+      r.dx = fmaf(dx, c, -(dy * s));
+      r.dy = fmaf(dx, s, dy * c);
     } break;
     case OP_APERTURE: {
       float ex = r.x - op.c[1], ey = r.y - op.c[2];
-      if (!(ex * ex + ey * ey < op.c[0])) alive = false;
+      if (!(fmaf(ex, ex, ey * ey) < op.c[0])) alive = false;
     } break;
     case OP_ABER:
       if (aber) aber_forward(aber + op.aux * kAberFloats, op.c[0], op.c[1], r);

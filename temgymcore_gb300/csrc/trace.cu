@@ -33,50 +33,49 @@ struct FwdArgs {
   int32_t h, w;
   int32_t do_bin;
   int32_t opl_vec;  // opl is 16-byte aligned: paired double stores
-  uint32_t* rows;   // shared-histogram variant: per-CTA uint32 histograms [gridDim.x][h * w]
+  int32_t pix_vec;  // pix_y / pix_x (those given) are 16-byte aligned
+  uint32_t* rows;   // shared-histogram variant: per-CTA packed uint16 counters [gridDim.x][(h * w + 1) / 2]
 };
 
 // Shared-histogram variant of the forward kernel: each CTA (kShThreads
 // threads, one per SM) keeps the whole detector in shared memory as uint16
-// counters packed in pairs, adds each hit with one shared atomic, and
-// every kShFlush iterations (at most 65535 rays per CTA, so no counter can
-// wrap) adds the counters into its own uint32 row of the workspace; k_hist_rows
-// then sums the rows into the caller's histogram.  Global atomics (even
-// warp-aggregated) then no longer bound the fused pass: measured at 16.8 M
-// rays, 256x256 spread 0.193 -> 0.167 ms, 64x64 (~4k hits per pixel)
-// 0.482 -> 0.143 ms.  Each hit is one plain shared atomic: warp aggregation
-// by __match_any_sync measured slower here (0.168 / 0.154 ms).
+// counters packed in pairs and adds each hit with one shared atomic.  A hit
+// that brings its counter to 32768 moves those 32768 counts into the caller's
+// histogram (one global atomic, rare: only pixels with more than 32767 hits
+// on one SM) and takes them off the counter, so no counter reaches 65536 (a
+// CTA has at most a few thousand hits in flight when the subtraction lands)
+// and no periodic flush is needed: at the end the CTA writes its packed
+// counters once to its own row of the workspace, and k_hist_rows adds the
+// rows into the histogram.  Global atomics (even warp-aggregated) then no
+// longer bound the fused pass: measured at 16.8 M rays, 256x256 spread 0.193
+// -> 0.167 ms, 64x64 (~4k hits per pixel) 0.482 -> 0.143 ms.  Each hit is one
+// plain shared atomic: warp aggregation by __match_any_sync measured slower
+// here (0.168 / 0.154 ms).
 constexpr int kShThreads = 1024;
 constexpr int kShMaxBins = 2 * (200 * 1024 / 4);  // 200 KB of packed counters
 
-__device__ __forceinline__ void hist_add_warp_sh(uint32_t* shw, int bin, bool valid) {
-  if (valid) atomicAdd(shw + (bin >> 1), 1u << (16 * (bin & 1)));
-}
+__host__ __device__ inline int sh_words(int bins) { return (bins + 1) >> 1; }
 
-// Adds the CTA's packed counters into its workspace row (written on the first
-// flush) and clears them; all threads of the CTA call it.
-__device__ __forceinline__ void sh_flush(uint32_t* shw, uint32_t* row, int bins, bool first) {
-  __syncthreads();
-  const int words = (bins + 1) >> 1;
-  for (int i = threadIdx.x; i < words; i += blockDim.x) {
-    const uint32_t v = shw[i];
-    shw[i] = 0u;
-    const int b0 = 2 * i;
-    const uint32_t lo = v & 0xffffu, hi = v >> 16;
-    if (b0 + 1 < bins) {
-      uint2* r2 = reinterpret_cast<uint2*>(row + b0);  // bins even: 8-byte aligned
-      if ((bins & 1) == 0) {
-        uint2 o = first ? make_uint2(0u, 0u) : *r2;
-        *r2 = make_uint2(o.x + lo, o.y + hi);
-      } else {
-        row[b0] = (first ? 0u : row[b0]) + lo;
-        row[b0 + 1] = (first ? 0u : row[b0 + 1]) + hi;
-      }
-    } else {
-      row[b0] = (first ? 0u : row[b0]) + lo;
+template <typename CountT>
+__device__ __forceinline__ void hist_add_sh(uint32_t* shw, int bin, bool valid, CountT* hist) {
+  if (valid) {
+    const uint32_t sh = 16u * (uint32_t)(bin & 1);
+    const uint32_t old = atomicAdd(shw + (bin >> 1), 1u << sh);
+    if (((old >> sh) & 0xffffu) == 0x7fffu) {  // this hit made the count 32768
+      atomicSub(shw + (bin >> 1), 0x8000u << sh);
+      if constexpr (sizeof(CountT) == 8)
+        atomicAdd(reinterpret_cast<unsigned long long*>(hist) + bin, 32768ull);
+      else
+        atomicAdd(reinterpret_cast<unsigned int*>(hist) + bin, 32768u);
     }
   }
+}
+
+// Writes the CTA's packed counters to its workspace row; all threads of the
+// CTA call it once, at the end.
+__device__ __forceinline__ void sh_store_row(const uint32_t* shw, uint32_t* row, int words) {
   __syncthreads();
+  for (int i = threadIdx.x; i < words; i += blockDim.x) row[i] = shw[i];
 }
 
 // R consecutive floats from p + i0: 16-byte vector loads when vec (R = 4 or
@@ -109,7 +108,9 @@ __device__ __forceinline__ void load4(const float* __restrict__ p, int64_t i0,
 template <int R>
 __device__ __forceinline__ void store4(float* __restrict__ p, int64_t i0,
                                        int64_t n, const float v[R], bool vec) {
-  if (R % 4 == 0 && vec) {
+  if (R == 2 && vec) {
+    *reinterpret_cast<float2*>(p + i0) = make_float2(v[0], v[R - 1]);
+  } else if (R % 4 == 0 && vec) {
 #pragma unroll
     for (int q = 0; q + 3 < R; q += 4)
       *reinterpret_cast<float4*>(p + i0 + q) = make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]);
@@ -120,32 +121,24 @@ __device__ __forceinline__ void store4(float* __restrict__ p, int64_t i0,
   }
 }
 
-template <int R, typename CountT, bool kSh = false>
-__global__ void __launch_bounds__(kSh ? kShThreads : 256)
-k_trace_fwd(const __grid_constant__ Program P, const __grid_constant__ FwdArgs A,
-            const __grid_constant__ BinCoef B) {
-  extern __shared__ uint32_t shw[];  // kSh: [(h * w + 1) / 2] packed uint16 counters
-  constexpr int kShFlush = 65535 / (kShThreads * R);  // iterations between flushes
+struct NoOp {
+  __device__ __forceinline__ void operator()() const {}
+};
+
+// The chain, the outputs, the pixels and the histogram for rays i0 .. i0+R-1
+// whose inputs are in x, y, dx, dy (vec: all R in range and every output
+// array aligned for R-wide vector stores).  All 32 lanes of the warp call it
+// (the global histogram's warp aggregation).  after_chain runs once the
+// coordinates are stored (every input consumed), before the pathlength, the
+// binning and the histogram.
+template <int R, typename CountT, bool kSh, typename AfterChain = NoOp>
+__device__ __forceinline__ void fwd_rays(const Program& P, const FwdArgs& A, const BinCoef& B,
+                                         uint32_t* shw, int64_t i0, float (&x)[R],
+                                         float (&y)[R], float (&dx)[R], float (&dy)[R],
+                                         bool vec, AfterChain after_chain = AfterChain()) {
   const int64_t n = A.n;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x * R;
   const double pl_uniform = A.pl_scalar + P.pl_const;
-  const int bins = A.h * A.w;
-  int since = 0;
-  bool first = true;
-  if (kSh) {
-    for (int i = threadIdx.x; i < ((bins + 1) >> 1); i += blockDim.x) shw[i] = 0u;
-    __syncthreads();
-  }
-  // block-uniform loop: every lane of every warp takes the same trip count,
-  // so warp-collective histogram aggregation below is always legal.
-  for (int64_t blk = (int64_t)blockIdx.x * blockDim.x * R; blk < n; blk += stride) {
-    const int64_t i0 = blk + (int64_t)threadIdx.x * R;
-    const bool vec = (R == 4) && (i0 + 3 < n);
-    float x[R], y[R], dx[R], dy[R];
-    load4<R>(A.x, i0, n, x, vec);
-    load4<R>(A.y, i0, n, y, vec);
-    load4<R>(A.dx, i0, n, dx, vec);
-    load4<R>(A.dy, i0, n, dy, vec);
+  {
     RayS r[R];
     double dvar[R];  // per-ray first distance (per-ray input z only), float64 once per ray
     float dvf[R];
@@ -180,6 +173,9 @@ k_trace_fwd(const __grid_constant__ Program P, const __grid_constant__ FwdArgs A
     store4<R>(A.oy, i0, n, y, vec);
     store4<R>(A.odx, i0, n, dx, vec);
     store4<R>(A.ody, i0, n, dy, vec);
+    // every input value has reached an issued instruction (the output of each
+    // coordinate depends on its input), so their registers hold the data
+    after_chain();
     if (A.opl) {
       // no float64 arithmetic per ray for a uniform base (one add per
       // per-ray input): GB300 issues float64 at ~1/64 of the float32 rate,
@@ -195,6 +191,8 @@ k_trace_fwd(const __grid_constant__ Program P, const __grid_constant__ FwdArgs A
       if (R == 4 && vec && A.opl_vec) {  // two 16-byte stores (i0 is a multiple of 4)
         reinterpret_cast<double2*>(A.opl + i0)[0] = make_double2(o[0], o[1]);
         reinterpret_cast<double2*>(A.opl + i0)[1] = make_double2(o[2 % R], o[3 % R]);
+      } else if (R == 2 && vec && A.opl_vec) {  // one 16-byte store (i0 even)
+        *reinterpret_cast<double2*>(A.opl + i0) = make_double2(o[0], o[R - 1]);
       } else {
 #pragma unroll
         for (int k = 0; k < R; ++k)
@@ -215,46 +213,135 @@ k_trace_fwd(const __grid_constant__ Program P, const __grid_constant__ FwdArgs A
         }
     }
     if (A.do_bin) {
+      int pys[R], pxs[R];
 #pragma unroll
       for (int k = 0; k < R; ++k) {
         int py, px;
         bin_yx(x[k], y[k], B, py, px);
+        pys[k] = py;
+        pxs[k] = px;
         const bool inr = (i0 + k < n);
-        if (inr) {
-          if (A.pix_y) A.pix_y[i0 + k] = py;
-          if (A.pix_x) A.pix_x[i0 + k] = px;
-          if (!(isfinite(x[k]) && isfinite(y[k]))) atomicOr(&g_tg_err, TG_EW_NONFINITE);
-        }
+        if (inr && !(isfinite(x[k]) && isfinite(y[k]))) atomicOr(&g_tg_err, TG_EW_NONFINITE);
         if (A.hist) {
           bool ok = inr && alive[k] && py >= 0 && py < A.h && px >= 0 && px < A.w;
-          if (kSh) hist_add_warp_sh(shw, ok ? py * A.w + px : 0, ok);
+          if (kSh) hist_add_sh<CountT>(shw, ok ? py * A.w + px : 0, ok, reinterpret_cast<CountT*>(A.hist));
           else hist_add_warp<CountT>(reinterpret_cast<CountT*>(A.hist), ok ? py * A.w + px : 0, ok);
         }
       }
-    }
-    if (kSh && ++since == kShFlush) {  // block-uniform: every thread takes the same trips
-      sh_flush(shw, A.rows + (size_t)blockIdx.x * bins, bins, first);
-      since = 0;
-      first = false;
+      // pixel indices: one vector store per array where aligned
+      if ((R == 2 || R == 4) && vec && A.pix_vec) {
+        if (R == 2) {
+          if (A.pix_y) *reinterpret_cast<int2*>(A.pix_y + i0) = make_int2(pys[0], pys[R - 1]);
+          if (A.pix_x) *reinterpret_cast<int2*>(A.pix_x + i0) = make_int2(pxs[0], pxs[R - 1]);
+        } else {
+          if (A.pix_y) *reinterpret_cast<int4*>(A.pix_y + i0) = make_int4(pys[0], pys[1 % R], pys[2 % R], pys[3 % R]);
+          if (A.pix_x) *reinterpret_cast<int4*>(A.pix_x + i0) = make_int4(pxs[0], pxs[1 % R], pxs[2 % R], pxs[3 % R]);
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < R; ++k)
+          if (i0 + k < n) {
+            if (A.pix_y) A.pix_y[i0 + k] = pys[k];
+            if (A.pix_x) A.pix_x[i0 + k] = pxs[k];
+          }
+      }
     }
   }
-  if (kSh && (since > 0 || first)) sh_flush(shw, A.rows + (size_t)blockIdx.x * bins, bins, first);
 }
 
-// hist[b] += sum over the CTA rows of rows[r][b] (one thread per bin, rows
-// read coalesced; integer sums, so the order does not matter).
+// kPf (shared-histogram variant, R = 4): each thread prefetches its next
+// four rays (x, y, dx, dy: four 16-byte cp.async) into its own 64-byte slot of
+// shared memory as soon as the chain has consumed the current ones, so the
+// loads run under the stores, the binning and the histogram atomics.  The
+// slots take kPfBytes ahead of the histogram words.
+constexpr int kPfBytes = 4 * kShThreads * 16;  // 64 KB
+
+template <int R, typename CountT, bool kSh = false, bool kPf = false>
+__global__ void __launch_bounds__(kSh ? kShThreads : 256)
+k_trace_fwd(const __grid_constant__ Program P, const __grid_constant__ FwdArgs A,
+            const __grid_constant__ BinCoef B) {
+  static_assert(!kPf || (kSh && R == 4), "prefetch: shared-histogram variant, four rays per thread");
+  extern __shared__ __align__(16) uint32_t shm[];
+  // kSh: [(h * w + 1) / 2] packed uint16 counters (after the prefetch slots with kPf)
+  uint32_t* shw = kPf ? shm + kPfBytes / 4 : shm;
+  const int64_t n = A.n;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x * R;
+  const int bins = A.h * A.w;
+  if (kSh) {
+    for (int i = threadIdx.x; i < ((bins + 1) >> 1); i += blockDim.x) shw[i] = 0u;
+    __syncthreads();
+  }
+  // prefetch slot of array a (x, y, dx, dy) for this thread
+  const uint32_t slot = smem_u32(shm) + 16u * threadIdx.x;
+  auto prefetch = [&](int64_t j0) {
+    cp_async16(slot, A.x + j0);
+    cp_async16(slot + 16u * kShThreads, A.y + j0);
+    cp_async16(slot + 32u * kShThreads, A.dx + j0);
+    cp_async16(slot + 48u * kShThreads, A.dy + j0);
+  };
+  if (kPf) {
+    const int64_t j0 = (int64_t)blockIdx.x * blockDim.x * R + (int64_t)threadIdx.x * R;
+    if (j0 + 3 < n) prefetch(j0);
+    cp_async_commit();
+  }
+  // block-uniform loop: every lane of every warp takes the same trip count,
+  // so warp-collective histogram aggregation below is always legal.
+  for (int64_t blk = (int64_t)blockIdx.x * blockDim.x * R; blk < n; blk += stride) {
+    const int64_t i0 = blk + (int64_t)threadIdx.x * R;
+    const bool vec = (R == 4) && (i0 + 3 < n);
+    float x[R], y[R], dx[R], dy[R];
+    if (kPf && vec) {  // the copies issued for these rays (same condition)
+      cp_async_wait_all();
+      const float4* sl = reinterpret_cast<const float4*>(shm) + threadIdx.x;
+      const float4 a = sl[0], b = sl[kShThreads], c = sl[2 * kShThreads], d = sl[3 * kShThreads];
+      x[0] = a.x; x[1 % R] = a.y; x[2 % R] = a.z; x[3 % R] = a.w;
+      y[0] = b.x; y[1 % R] = b.y; y[2 % R] = b.z; y[3 % R] = b.w;
+      dx[0] = c.x; dx[1 % R] = c.y; dx[2 % R] = c.z; dx[3 % R] = c.w;
+      dy[0] = d.x; dy[1 % R] = d.y; dy[2 % R] = d.z; dy[3 % R] = d.w;
+    } else {
+      load4<R>(A.x, i0, n, x, vec);
+      load4<R>(A.y, i0, n, y, vec);
+      load4<R>(A.dx, i0, n, dx, vec);
+      load4<R>(A.dy, i0, n, dy, vec);
+    }
+    const int64_t ni0 = i0 + stride;
+    // the slot is free once the chain has used the values read from it
+    auto next = [&]() {
+      if (kPf) {
+        if (ni0 + 3 < n) prefetch(ni0);
+        cp_async_commit();
+      }
+    };
+    fwd_rays<R, CountT, kSh>(P, A, B, shw, i0, x, y, dx, dy, vec, next);
+  }
+  if (kSh) sh_store_row(shw, A.rows + (size_t)blockIdx.x * sh_words(bins), sh_words(bins));
+}
+
+// hist[b] += sum over the CTA rows of their packed uint16 counters (one
+// thread per word = two bins, rows read coalesced; integer sums, so the order
+// does not matter).
 template <typename CountT>
 __global__ void k_hist_rows(const uint32_t* __restrict__ rows, int nrows, int bins,
                             CountT* __restrict__ hist) {
-  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < bins; b += gridDim.x * blockDim.x) {
-    unsigned long long a[4] = {0ull, 0ull, 0ull, 0ull};
+  const int words = sh_words(bins);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < words; i += gridDim.x * blockDim.x) {
+    unsigned long long lo[2] = {0ull, 0ull}, hi[2] = {0ull, 0ull};
     int r = 0;
     for (; r + 4 <= nrows; r += 4) {
 #pragma unroll
-      for (int u = 0; u < 4; ++u) a[u] += rows[(size_t)(r + u) * bins + b];
+      for (int u = 0; u < 4; ++u) {
+        const uint32_t v = rows[(size_t)(r + u) * words + i];
+        lo[u & 1] += v & 0xffffu;
+        hi[u & 1] += v >> 16;
+      }
     }
-    for (; r < nrows; ++r) a[0] += rows[(size_t)r * bins + b];
-    hist[b] += (CountT)((a[0] + a[1]) + (a[2] + a[3]));
+    for (; r < nrows; ++r) {
+      const uint32_t v = rows[(size_t)r * words + i];
+      lo[0] += v & 0xffffu;
+      hi[0] += v >> 16;
+    }
+    hist[2 * i] += (CountT)(lo[0] + lo[1]);
+    if (2 * i + 1 < bins) hist[2 * i + 1] += (CountT)(hi[0] + hi[1]);
   }
 }
 
@@ -265,7 +352,7 @@ struct BinArgs {
   int32_t *pix_y, *pix_x;
   void* hist;
   int32_t h, w;
-  uint32_t* rows;  // shared-histogram variant: per-CTA uint32 histograms
+  uint32_t* rows;  // shared-histogram variant: per-CTA packed uint16 counters
 };
 
 // kSh: the shared-memory histogram variant (as for k_trace_fwd).
@@ -273,11 +360,8 @@ template <typename CountT, bool kSh = false>
 __global__ void __launch_bounds__(kSh ? kShThreads : 256)
 k_bin(const __grid_constant__ BinArgs A, const __grid_constant__ BinCoef B) {
   extern __shared__ uint32_t shw[];
-  constexpr int kShFlush = 65535 / kShThreads;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   const int bins = A.h * A.w;
-  int since = 0;
-  bool first = true;
   if (kSh) {
     for (int i = threadIdx.x; i < ((bins + 1) >> 1); i += blockDim.x) shw[i] = 0u;
     __syncthreads();
@@ -295,16 +379,11 @@ k_bin(const __grid_constant__ BinArgs A, const __grid_constant__ BinCoef B) {
     }
     if (A.hist) {
       bool ok = inr && (!A.mask || A.mask[i]) && py >= 0 && py < A.h && px >= 0 && px < A.w;
-      if (kSh) hist_add_warp_sh(shw, ok ? py * A.w + px : 0, ok);
+      if (kSh) hist_add_sh<CountT>(shw, ok ? py * A.w + px : 0, ok, reinterpret_cast<CountT*>(A.hist));
       else hist_add_warp<CountT>(reinterpret_cast<CountT*>(A.hist), ok ? py * A.w + px : 0, ok);
     }
-    if (kSh && ++since == kShFlush) {  // block-uniform
-      sh_flush(shw, A.rows + (size_t)blockIdx.x * bins, bins, first);
-      since = 0;
-      first = false;
-    }
   }
-  if (kSh && (since > 0 || first)) sh_flush(shw, A.rows + (size_t)blockIdx.x * bins, bins, first);
+  if (kSh) sh_store_row(shw, A.rows + (size_t)blockIdx.x * sh_words(bins), sh_words(bins));
 }
 
 // Histogram of existing pixel indices (grid.py:231-280 into_image given
@@ -314,11 +393,8 @@ __global__ void __launch_bounds__(kSh ? kShThreads : 256)
 k_hist_pix(int64_t n, const IdxT* __restrict__ pix_y, const IdxT* __restrict__ pix_x, int h, int w,
            CountT* __restrict__ hist, uint32_t* __restrict__ rows) {
   extern __shared__ uint32_t shw[];
-  constexpr int kShFlush = 65535 / kShThreads;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   const int bins = h * w;
-  int since = 0;
-  bool first = true;
   if (kSh) {
     for (int i = threadIdx.x; i < ((bins + 1) >> 1); i += blockDim.x) shw[i] = 0u;
     __syncthreads();
@@ -329,15 +405,10 @@ k_hist_pix(int64_t n, const IdxT* __restrict__ pix_y, const IdxT* __restrict__ p
     const long long py = inr ? (long long)pix_y[i] : -1, px = inr ? (long long)pix_x[i] : -1;
     const bool ok = py >= 0 && py < h && px >= 0 && px < w;
     const int bin = ok ? (int)(py * w + px) : 0;
-    if (kSh) hist_add_warp_sh(shw, bin, ok);
+    if (kSh) hist_add_sh<CountT>(shw, bin, ok, hist);
     else hist_add_warp<CountT>(hist, bin, ok);
-    if (kSh && ++since == kShFlush) {
-      sh_flush(shw, rows + (size_t)blockIdx.x * bins, bins, first);
-      since = 0;
-      first = false;
-    }
   }
-  if (kSh && (since > 0 || first)) sh_flush(shw, rows + (size_t)blockIdx.x * bins, bins, first);
+  if (kSh) sh_store_row(shw, rows + (size_t)blockIdx.x * sh_words(bins), sh_words(bins));
 }
 
 static int sm_count() {
@@ -390,10 +461,29 @@ static cudaError_t shared_hist_attr() {
 }
 
 static size_t shared_hist_bytes(int64_t h, int64_t w) {
-  return (size_t)sm_count() * (size_t)h * (size_t)w * sizeof(uint32_t);
+  return (size_t)sm_count() * (size_t)sh_words((int)(h * w)) * sizeof(uint32_t);
 }
 
 static size_t shared_hist_bytes(const tg_grid* grid) { return shared_hist_bytes(grid->h, grid->w); }
+
+static int smem_optin() {
+  static int v = 0;
+  if (!v) {
+    int dev = 0, q = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&q, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    v = q > 0 ? q : 48 * 1024;
+  }
+  return v;
+}
+
+// The prefetching shared-histogram kernel with the whole opt-in budget.
+template <auto Kernel>
+static cudaError_t prefetch_attr() {
+  static cudaError_t done =
+      cudaFuncSetAttribute(Kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin());
+  return done;
+}
 
 static int trace_fwd_impl(const tg_model* model, const tg_rays* in, tg_rays* out,
                           double* z_out, const tg_grid* grid, int32_t* pix_y,
@@ -433,6 +523,7 @@ static int trace_fwd_impl(const tg_model* model, const tg_rays* in, tg_rays* out
   bool vec = al16(A.x) && al16(A.y) && al16(A.dx) && al16(A.dy) && al16(A.ox) &&
              al16(A.oy) && al16(A.odx) && al16(A.ody);
   A.opl_vec = A.opl && al16(A.opl);
+  A.pix_vec = (!pix_y || al16(pix_y)) && (!pix_x || al16(pix_x));
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   if (hist && workspace && use_shared_hist(A.n, grid) && ws_bytes >= shared_hist_bytes(grid) &&
       (reinterpret_cast<uintptr_t>(workspace) & 15) == 0) {
@@ -444,7 +535,17 @@ static int trace_fwd_impl(const tg_model* model, const tg_rays* in, tg_rays* out
     const int blocks = (int)(need < sm_count() ? need : sm_count());
     A.rows = reinterpret_cast<uint32_t*>(workspace);
     cudaError_t e = cudaSuccess;
-    if (vec) {
+    if (vec && smem + kPfBytes <= (size_t)smem_optin()) {  // prefetch slots fit
+      if (hist_i64) {
+        e = prefetch_attr<k_trace_fwd<4, long long, true, true>>();
+        if (e == cudaSuccess)
+          k_trace_fwd<4, long long, true, true><<<blocks, kShThreads, smem + kPfBytes, s>>>(P, A, B);
+      } else {
+        e = prefetch_attr<k_trace_fwd<4, int, true, true>>();
+        if (e == cudaSuccess)
+          k_trace_fwd<4, int, true, true><<<blocks, kShThreads, smem + kPfBytes, s>>>(P, A, B);
+      }
+    } else if (vec) {
       if (hist_i64) {
         e = shared_hist_attr<k_trace_fwd<4, long long, true>>();
         if (e == cudaSuccess) k_trace_fwd<4, long long, true><<<blocks, kShThreads, smem, s>>>(P, A, B);
@@ -462,7 +563,7 @@ static int trace_fwd_impl(const tg_model* model, const tg_rays* in, tg_rays* out
       }
     }
     if (e != cudaSuccess || cudaGetLastError() != cudaSuccess) return TG_ERR_CUDA;
-    const int rb = (bins + 255) / 256;
+    const int rb = (sh_words(bins) + 255) / 256;
     if (hist_i64) k_hist_rows<long long><<<rb, 256, 0, s>>>(A.rows, blocks, bins, reinterpret_cast<long long*>(hist));
     else k_hist_rows<int><<<rb, 256, 0, s>>>(A.rows, blocks, bins, reinterpret_cast<int*>(hist));
     return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
@@ -537,7 +638,7 @@ static int bin_impl(int64_t n, const float* x, const float* y, const uint8_t* ma
       if (e == cudaSuccess) k_bin<int, true><<<blocks, kShThreads, smem, s>>>(A, B);
     }
     if (e != cudaSuccess || cudaGetLastError() != cudaSuccess) return TG_ERR_CUDA;
-    const int rb = (bins + 255) / 256;
+    const int rb = (sh_words(bins) + 255) / 256;
     if (hist_i64) k_hist_rows<long long><<<rb, 256, 0, s>>>(A.rows, blocks, bins, reinterpret_cast<long long*>(hist));
     else k_hist_rows<int><<<rb, 256, 0, s>>>(A.rows, blocks, bins, reinterpret_cast<int*>(hist));
     return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
@@ -587,7 +688,7 @@ static int hist_pix_launch(int64_t n, const void* py, const void* px, int h, int
     if (e != cudaSuccess) return TG_ERR_CUDA;
     k_hist_pix<IdxT, CountT, true><<<blocks, kShThreads, smem, s>>>(n, y, x, h, w, hh, rows);
     if (cudaGetLastError() != cudaSuccess) return TG_ERR_CUDA;
-    k_hist_rows<CountT><<<(bins + 255) / 256, 256, 0, s>>>(rows, blocks, bins, hh);
+    k_hist_rows<CountT><<<(sh_words(bins) + 255) / 256, 256, 0, s>>>(rows, blocks, bins, hh);
   } else {
     int per_sm = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hist_pix<IdxT, CountT>, 256, 0);

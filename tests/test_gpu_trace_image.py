@@ -69,9 +69,10 @@ def test_trace_image_spread(cuda, shape):
     assert ref.sum() > n // 2
 
 
-def test_trace_image_one_pixel_many_flushes(cuda):
-    # every ray in the centre pixel: 10M rays over the SMs, several flushes per
-    # CTA with 61,440 hits per counter between flushes
+def test_trace_image_one_pixel_many_carries(cuda):
+    # every ray in the centre pixel: 10M rays over the SMs, about 66k hits per
+    # CTA on one uint16 counter, which moves 32768 counts into the histogram
+    # each time it reaches that value
     n = 10_000_000
     h_sh, h_gl, ref = _run(n, (32, 32), spread=0.0)
     assert np.array_equal(h_sh, ref) and np.array_equal(h_gl, ref)
@@ -115,6 +116,27 @@ def test_into_image_pixel_indices(cuda, idt):
         ok = (py >= 0) & (py < 40) & (px >= 0) & (px < 56)
         ref = np.bincount(py[ok] * 56 + px[ok], minlength=40 * 56).reshape(40, 56) + 2
         assert np.array_equal(out.cpu().numpy(), ref), n
+
+
+@pytest.mark.parametrize("hdt", [torch.int32, torch.int64])
+def test_hist_pixels_carry_on_one_word(cuda, hdt):
+    """Every hit on the two pixels that share one packed shared-memory word:
+    each CTA drives both uint16 halves past 32768 twice (the carry
+    into the histogram must leave the neighbouring half intact), on top of
+    prefilled counts; the remaining hits stay in the per-CTA rows."""
+    import temgymcore_gb300 as t
+    n = 24_000_001
+    rng = np.random.default_rng(9)
+    det = t.Detector(z=1.0, pixel_size=(1e-5, 1e-5), shape=(30, 30))
+    b = rng.integers(0, 2, n)  # bins 2 * 225 + b: one packed word
+    py = torch.tensor(np.full(n, 15, np.int32), device=cuda)
+    px = torch.tensor((b + 0).astype(np.int32), device=cuda)
+    acc = torch.full((30, 30), 5, dtype=hdt, device=cuda)
+    out = det.into_image((py, px), acc)
+    ref = np.full((30, 30), 5, np.int64)
+    ref[15, 0] += int((b == 0).sum())
+    ref[15, 1] += int((b == 1).sum())
+    assert np.array_equal(out.cpu().numpy().astype(np.int64), ref)
 
 
 def test_into_image_rays_shared_vs_global(cuda):
@@ -164,3 +186,67 @@ def test_trace_plan_shared_hist_graph(cuda):
     g.replay()
     torch.cuda.synchronize()
     assert torch.equal(plan.image, 2 * img)
+
+
+@pytest.mark.parametrize("n", [2047, 2048, 4099, 2 * 152 * 2048 + 1234])
+def test_vector_and_scalar_variants_agree_bit_for_bit(cuda, n):
+    """Aligned arrays take the four-rays-per-thread kernels (16-byte vector
+    loads and stores); a one-element offset view of the same data takes the
+    one-ray-per-thread kernels.  The chain's arithmetic is written with
+    explicit fused multiply-adds, so both give every output (coordinates,
+    float64 pathlength, z, amplitude, pixel indices, global and shared-memory
+    histograms) bit for bit: through a lens, an aperture and a biprism, with
+    per-ray z and pathlength inputs, at ragged and whole sizes."""
+    from temgymcore_gb300 import _native as N
+    from temgymcore_gb300.run import _rays_struct, pack_model
+    from temgymcore_gb300.workloads import build_model
+    lib = N.lib()
+    rng = np.random.default_rng(n)
+    shape = (64, 64)
+    model = build_model([{"kind": "lens", "z": 0.5, "focal_length": 0.2},
+                         {"kind": "aperture", "z": 0.6, "radius": 2.5e-4},
+                         {"kind": "biprism", "z": 0.7, "def_x": 3e-5},
+                         {"kind": "detector", "z": 1.0, "pixel_size": (1e-5, 1e-5), "shape": shape}])
+    m, keep_m = pack_model(model)
+    g = model[-1]._tg_grid()
+    cols = {"x": rng.uniform(-4e-4, 4e-4, n), "y": rng.uniform(-4e-4, 4e-4, n),
+            "dx": rng.normal(0, 5e-4, n), "dy": rng.normal(0, 5e-4, n)}
+    z = rng.uniform(-1e-3, 1e-3, n)
+    pl = rng.uniform(0, 1e-2, n)
+    amp = rng.uniform(0.5, 1.0, n)
+
+    def put(v, dt, off):
+        t = torch.empty(n + off, dtype=dt, device=cuda)
+        t[off:] = torch.from_numpy(np.asarray(v)).to(dt).to(cuda)
+        return t[off:]
+
+    def run(off, shared):
+        xs = [put(cols[k], torch.float32, off) for k in ("x", "y", "dx", "dy")]
+        zt, plt, at = put(z, torch.float64, off), put(pl, torch.float64, off), put(amp, torch.float32, off)
+        rin = _rays_struct(n, *xs, zt, 0.0, plt, 0.0, at)
+        o = [put(np.zeros(n), torch.float32, off) for _ in range(4)]
+        opl, oz, oa = put(np.zeros(n), torch.float64, off), put(np.zeros(n), torch.float64, off), \
+            put(np.zeros(n), torch.float32, off)
+        rout = _rays_struct(n, *o, oz, 0.0, opl, 0.0, oa)
+        py, px = put(np.zeros(n), torch.int32, off), put(np.zeros(n), torch.int32, off)
+        hist = torch.zeros(shape, dtype=torch.int64, device=cuda)
+        if shared:
+            ws_bytes = lib.tg_trace_image_workspace(n, C.byref(g))
+            assert ws_bytes > 0
+            ws = torch.empty(ws_bytes, dtype=torch.uint8, device=cuda)
+            N.check(lib.tg_trace_image(C.byref(m), C.byref(rin), C.byref(rout), None, C.byref(g),
+                                       N.ptr(py), N.ptr(px), N.ptr(hist), 1, N.ptr(ws), ws_bytes,
+                                       N.stream_ptr()), "tg_trace_image")
+        else:
+            N.check(lib.tg_trace_fwd(C.byref(m), C.byref(rin), C.byref(rout), None, C.byref(g),
+                                     N.ptr(py), N.ptr(px), N.ptr(hist), 1, N.stream_ptr()), "tg_trace_fwd")
+        torch.cuda.synchronize()
+        return [t.cpu().numpy() for t in (*o, opl, oz, oa, py, px, hist)]
+
+    modes = [False] + ([True] if n >= 32 * shape[0] * shape[1] else [])
+    for shared in modes:
+        a, b = run(0, shared), run(1, shared)
+        for u, v in zip(a, b):
+            assert np.array_equal(u, v), shared
+        assert a[-1].sum() > 0
+    assert N.error_word() == 0
