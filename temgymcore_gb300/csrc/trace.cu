@@ -82,20 +82,26 @@ __device__ __forceinline__ void sh_store_row(const uint32_t* shw, uint32_t* row,
 // 8, p + i0 16-byte aligned and all R in range), else per element with the
 // tail past n read as 0.  For R = 8 both vector loads are issued before the
 // values are unpacked (this form also spills fewer registers in the
-// 128-register adjoint).
-template <int R>
+// 128-register adjoint).  kStream: evict-first loads (ld.global.cs), for data
+// read once by a kernel that streams many arrays.
+template <bool kStream>
+__device__ __forceinline__ float4 ld4(const float* p) {
+  return kStream ? __ldcs(reinterpret_cast<const float4*>(p)) : __ldg(reinterpret_cast<const float4*>(p));
+}
+
+template <int R, bool kStream = false>
 __device__ __forceinline__ void load4(const float* __restrict__ p, int64_t i0,
                                       int64_t n, float v[R], bool vec) {
   if constexpr (R == 4) {
     if (vec) {
-      const float4 t = __ldg(reinterpret_cast<const float4*>(p + i0));
+      const float4 t = ld4<kStream>(p + i0);
       v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
       return;
     }
   } else if constexpr (R == 8) {
     if (vec) {
-      const float4 t = __ldg(reinterpret_cast<const float4*>(p + i0));
-      const float4 u = __ldg(reinterpret_cast<const float4*>(p + i0 + 4));
+      const float4 t = ld4<kStream>(p + i0);
+      const float4 u = ld4<kStream>(p + i0 + 4);
       v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
       v[4] = u.x; v[5] = u.y; v[6] = u.z; v[7] = u.w;
       return;
@@ -105,15 +111,19 @@ __device__ __forceinline__ void load4(const float* __restrict__ p, int64_t i0,
   for (int k = 0; k < R; ++k) v[k] = (i0 + k < n) ? __ldg(p + i0 + k) : 0.f;
 }
 
-template <int R>
+// kStream: evict-first vector stores (st.global.cs).
+template <int R, bool kStream = false>
 __device__ __forceinline__ void store4(float* __restrict__ p, int64_t i0,
                                        int64_t n, const float v[R], bool vec) {
   if (R == 2 && vec) {
     *reinterpret_cast<float2*>(p + i0) = make_float2(v[0], v[R - 1]);
   } else if (R % 4 == 0 && vec) {
 #pragma unroll
-    for (int q = 0; q + 3 < R; q += 4)
-      *reinterpret_cast<float4*>(p + i0 + q) = make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]);
+    for (int q = 0; q + 3 < R; q += 4) {
+      const float4 t = make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]);
+      if (kStream) __stcs(reinterpret_cast<float4*>(p + i0 + q), t);
+      else *reinterpret_cast<float4*>(p + i0 + q) = t;
+    }
   } else {
 #pragma unroll
     for (int k = 0; k < R; ++k)
@@ -885,6 +895,215 @@ k_trace_vjp(const __grid_constant__ Program P, const __grid_constant__ VjpArgs A
   }
 }
 
+// ---------------------------------------------------- lean adjoint
+// k_trace_vjp_lean: the adjoint for the chains most calls trace: free space
+// (paraxial or direction cosines, uniform distances), lenses, scanners /
+// descanners (shifts), deflectors, rotators and apertures, with no upstream
+// pathlength gradient.  The pathlength adjoint is then zero at every step
+// (no step feeds it), no biprism sign or per-ray distance has to be kept,
+// and an aperture's mask does not enter the adjoint, so each ray carries its
+// state (x, y, dx, dy) and its adjoint (lx, ly, ldx, ldy) only: 8 registers
+// a ray instead of ~14, which buys more rays in flight per SM.  The step
+// arithmetic is op_forward / op_reverse with the pathlength terms taken out
+// (they multiply the zero adjoint).
+__host__ __device__ inline bool lean_kind(int kind) {
+  return kind == OP_NOP || kind == OP_FREE || kind == OP_LENS || kind == OP_SHIFT ||
+         kind == OP_DEFLECT || kind == OP_ROTATE || kind == OP_APERTURE;
+}
+
+struct Ray4 {
+  float x, y, dx, dy;
+};
+
+__device__ __forceinline__ void lean_forward(const Op& op, Ray4& r) {
+  switch (op.kind) {
+    case OP_FREE: {
+      const float d = op.c[0];
+      if (op.aux) {
+        const float t = d / (1.f + fmaf(r.dx, r.dx, r.dy * r.dy));
+        r.x = fmaf(r.dx, t, r.x);
+        r.y = fmaf(r.dy, t, r.y);
+      } else {
+        r.x = fmaf(r.dx, d, r.x);
+        r.y = fmaf(r.dy, d, r.y);
+      }
+    } break;
+    case OP_LENS:
+      r.dx = fmaf(-r.x, op.c[0], r.dx);
+      r.dy = fmaf(-r.y, op.c[0], r.dy);
+      break;
+    case OP_SHIFT:
+      r.x += op.c[0]; r.y += op.c[1]; r.dx += op.c[2]; r.dy += op.c[3];
+      break;
+    case OP_DEFLECT:
+      r.dx += op.c[0]; r.dy += op.c[1];
+      break;
+    case OP_ROTATE: {
+      const float c = op.c[0], sn = op.c[1];
+      const float x = r.x, y = r.y, dx = r.dx, dy = r.dy;
+      r.x = fmaf(x, c, -(y * sn));
+      r.y = fmaf(x, sn, y * c);
+      r.dx = fmaf(dx, c, -(dy * sn));
+      r.dy = fmaf(dx, sn, dy * c);
+    } break;
+    default:  // OP_NOP, OP_APERTURE (its mask does not enter the adjoint)
+      break;
+  }
+}
+
+__device__ __forceinline__ void lean_reverse(const Op& op, Ray4& r, Ray4& a, float c[4]) {
+  switch (op.kind) {
+    case OP_FREE: {
+      const float d = op.c[0];
+      if (op.aux) {
+        const float dx = r.dx, dy = r.dy;
+        const float n2 = 1.f + fmaf(dx, dx, dy * dy);
+        const float inv = 1.f / n2;
+        c[0] = (a.x * dx + a.y * dy) * inv;
+        const float t = d / n2;
+        r.x = fmaf(-dx, t, r.x);
+        r.y = fmaf(-dy, t, r.y);
+        const float di = d * inv, di2 = 2.f * di * inv;
+        const float jxx = di - di2 * dx * dx, jyy = di - di2 * dy * dy, jxy = -di2 * dx * dy;
+        a.dx += a.x * jxx + a.y * jxy;
+        a.dy += a.x * jxy + a.y * jyy;
+      } else {
+        c[0] = a.x * r.dx + a.y * r.dy;
+        r.x = fmaf(-r.dx, d, r.x);
+        r.y = fmaf(-r.dy, d, r.y);
+        a.dx = fmaf(a.x, d, a.dx);
+        a.dy = fmaf(a.y, d, a.dy);
+      }
+    } break;
+    case OP_LENS: {
+      const float k = op.c[0];
+      const float x = r.x, y = r.y;
+      r.dx = fmaf(x, k, r.dx);
+      r.dy = fmaf(y, k, r.dy);
+      c[0] = (a.dx * x + a.dy * y) * (k * k);
+      a.x = a.x - a.dx * k;
+      a.y = a.y - a.dy * k;
+    } break;
+    case OP_SHIFT:
+      r.x -= op.c[0]; r.y -= op.c[1]; r.dx -= op.c[2]; r.dy -= op.c[3];
+      c[0] = a.x; c[1] = a.y; c[2] = a.dx; c[3] = a.dy;
+      break;
+    case OP_DEFLECT:
+      c[0] = a.dx; c[1] = a.dy;
+      r.dx -= op.c[0]; r.dy -= op.c[1];
+      break;
+    case OP_ROTATE: {
+      const float cs = op.c[0], sn = op.c[1];
+      c[0] = -a.x * r.y + a.y * r.x - a.dx * r.dy + a.dy * r.dx;
+      const float x = r.x, y = r.y, dx = r.dx, dy = r.dy;
+      r.x = x * cs + y * sn;
+      r.y = -x * sn + y * cs;
+      r.dx = dx * cs + dy * sn;
+      r.dy = -dx * sn + dy * cs;
+      const float lx = a.x, ly = a.y, ldx = a.dx, ldy = a.dy;
+      a.x = lx * cs + ly * sn;
+      a.y = -lx * sn + ly * cs;
+      a.dx = ldx * cs + ldy * sn;
+      a.dy = -ldx * sn + ldy * cs;
+    } break;
+    default:
+      break;
+  }
+}
+
+// Shape measured at 16.8 M rays (Lens + Detector, CUDA events): 8 rays a
+// thread at two blocks per SM (124 registers) 0.160 ms, three blocks (80
+// registers) 0.209 ms, 4 rays at four / five blocks 0.214 / 0.261 ms; with
+// evict-first loads and stores 0.157 ms (three blocks 0.189 ms).
+constexpr int kLeanRays = 8;    // rays per thread
+constexpr int kLeanBlocks = 2;  // resident blocks per SM (register bound)
+
+template <int R>
+__global__ void __launch_bounds__(kVjpThreads, kLeanBlocks)
+k_trace_vjp_lean(const __grid_constant__ Program P, const __grid_constant__ VjpArgs A) {
+  __shared__ float wacc[kVjpThreads / 32][kMaxSteps * 4];
+  const bool sums = A.partial != nullptr;
+  if (sums)
+    for (int i = threadIdx.x; i < (kVjpThreads / 32) * kMaxSteps * 4; i += blockDim.x) (&wacc[0][0])[i] = 0.f;
+  __syncthreads();
+  const int64_t n = A.n;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x * R;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int64_t blk = (int64_t)blockIdx.x * blockDim.x * R; blk < n; blk += stride) {
+    const int64_t i0 = blk + (int64_t)threadIdx.x * R;
+    const bool vec = i0 + R - 1 < n;
+    Ray4 r[R], ad[R];
+    {
+      float x[R], y[R], dx[R], dy[R], gx[R], gy[R], gdx[R], gdy[R];
+      load4<R, true>(A.x, i0, n, x, vec);
+      load4<R, true>(A.y, i0, n, y, vec);
+      load4<R, true>(A.dx, i0, n, dx, vec);
+      load4<R, true>(A.dy, i0, n, dy, vec);
+      load4<R, true>(A.gx, i0, n, gx, vec);
+      load4<R, true>(A.gy, i0, n, gy, vec);
+      load4<R, true>(A.gdx, i0, n, gdx, vec);
+      load4<R, true>(A.gdy, i0, n, gdy, vec);
+#pragma unroll
+      for (int k = 0; k < R; ++k) {
+        r[k] = Ray4{x[k], y[k], dx[k], dy[k]};
+        // rays beyond n carry zero adjoints (load4 reads them as 0)
+        ad[k] = Ray4{gx[k], gy[k], gdx[k], gdy[k]};
+      }
+    }
+    for (int s = 0; s < P.n_steps; ++s) {
+      const Op op = P.op[s];
+#pragma unroll
+      for (int k = 0; k < R; ++k) lean_forward(op, r[k]);
+    }
+    for (int s = P.n_steps - 1; s >= 0; --s) {
+      const Op op = P.op[s];
+      float c[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int k = 0; k < R; ++k) {
+        float ck[4] = {0.f, 0.f, 0.f, 0.f};
+        lean_reverse(op, r[k], ad[k], ck);
+        c[0] += ck[0]; c[1] += ck[1]; c[2] += ck[2]; c[3] += ck[3];
+      }
+      if (sums) {
+        const int ns = op_nsums(op.kind);
+        for (int j = 0; j < ns; ++j) {
+          float v = warp_sum(c[j]);
+          if (lane == 0) wacc[warp][4 * s + j] += v;
+        }
+      }
+    }
+    float o[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) o[k] = ad[k].x;
+    if (A.ix) store4<R, true>(A.ix, i0, n, o, vec);
+#pragma unroll
+    for (int k = 0; k < R; ++k) o[k] = ad[k].y;
+    if (A.iy) store4<R, true>(A.iy, i0, n, o, vec);
+#pragma unroll
+    for (int k = 0; k < R; ++k) o[k] = ad[k].dx;
+    if (A.idx) store4<R, true>(A.idx, i0, n, o, vec);
+#pragma unroll
+    for (int k = 0; k < R; ++k) o[k] = ad[k].dy;
+    if (A.idy) store4<R, true>(A.idy, i0, n, o, vec);
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+      if (i0 + k < n) {
+        if (A.ipl) A.ipl[i0 + k] = 0.0;  // no upstream pathlength gradient
+        if (A.iz) A.iz[i0 + k] = 0.0;    // uniform input z
+      }
+    }
+  }
+  if (sums) {
+    __syncthreads();
+    double* dst = A.partial + (size_t)blockIdx.x * P.n_steps * 4;
+    for (int i = threadIdx.x; i < P.n_steps * 4; i += blockDim.x) {
+      double t = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += (double)wacc[w][i];
+      dst[i] = t;
+    }
+  }
+}
+
 // raw[i] += sum over blocks of partial[b][i], in block order.
 __global__ void k_reduce_partials(const double* __restrict__ partial, int nblocks,
                                   int width, double* __restrict__ raw) {
@@ -904,25 +1123,37 @@ __global__ void k_reduce_partials(const double* __restrict__ partial, int nblock
 // Grid of the adjoint: every block resident at once (the grid-stride loop
 // gives each block the same share, so a block that waits for a free slot
 // would double the tail).  The residency of the wider variant bounds both.
-static int vjp_grid(int64_t n) {
+template <auto Kernel>
+static int vjp_per_sm() {
   static int per_sm = 0;
   if (!per_sm) {
     int v = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_trace_vjp<kVjpRays, false>, kVjpThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, Kernel, kVjpThreads, 0);
     per_sm = v > 0 ? v : 1;
   }
-  const int64_t per_block = (int64_t)kVjpThreads * kVjpRays;
+  return per_sm;
+}
+
+static int vjp_grid(int64_t n, bool lean) {
+  const int per_sm = lean ? vjp_per_sm<k_trace_vjp_lean<kLeanRays>>() : vjp_per_sm<k_trace_vjp<kVjpRays, false>>();
+  const int64_t per_block = (int64_t)kVjpThreads * (lean ? kLeanRays : kVjpRays);
   int64_t need = (n + per_block - 1) / per_block;
   int64_t cap = (int64_t)sm_count() * per_sm;
   int64_t g = need < cap ? need : cap;
   return (int)(g < 1 ? 1 : g);
 }
 
+// Blocks whose partial sums a workspace must hold (either kernel).
+static int vjp_grid_max(int64_t n) {
+  const int a = vjp_grid(n, false), b = vjp_grid(n, true);
+  return a > b ? a : b;
+}
+
 }  // namespace tg
 
 extern "C" size_t tg_trace_vjp_workspace(int64_t n, const tg_model* model) {
   if (!model || n < 0) return 0;
-  return (size_t)vjp_grid(n) * (size_t)(2 * model->n_components) * 4 * sizeof(double);
+  return (size_t)vjp_grid_max(n) * (size_t)(2 * model->n_components) * 4 * sizeof(double);
 }
 
 extern "C" int tg_trace_vjp(const tg_model* model, const tg_rays* in, const tg_rays* gout,
@@ -938,9 +1169,6 @@ extern "C" int tg_trace_vjp(const tg_model* model, const tg_rays* in, const tg_r
   if (st != TG_OK) return st;
   if (P.n_probe_ops) return TG_ERR_UNSUPPORTED;
   if (in->n == 0) return TG_OK;
-  const int grid = vjp_grid(in->n);
-  const size_t need = (size_t)grid * P.n_steps * 4 * sizeof(double);
-  if (raw && P.n_steps > 0 && (!workspace || ws_bytes < need)) return TG_ERR_WORKSPACE;
   VjpArgs A;
   std::memset(&A, 0, sizeof(A));
   A.n = in->n;
@@ -957,12 +1185,18 @@ extern "C" int tg_trace_vjp(const tg_model* model, const tg_rays* in, const tg_r
   bool vec = al16(A.x) && al16(A.y) && al16(A.dx) && al16(A.dy) && al16(A.gx) &&
              al16(A.gy) && al16(A.gdx) && al16(A.gdy) && (!A.ix || al16(A.ix)) &&
              (!A.iy || al16(A.iy)) && (!A.idx || al16(A.idx)) && (!A.idy || al16(A.idy));
+  bool lean = vec && P.n_aber == 0 && !A.z && !A.gpl;
+  for (int i = 0; i < P.n_steps && lean; ++i) lean = lean_kind(P.op[i].kind);
+  const int grid = vjp_grid(in->n, lean);
+  const size_t need = (size_t)grid * P.n_steps * 4 * sizeof(double);
+  if (A.partial && (!workspace || ws_bytes < need)) return TG_ERR_WORKSPACE;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   if (P.n_aber > 0) {
     if (vec) k_trace_vjp<4, true><<<grid, kVjpThreads, 0, s>>>(P, A);
     else k_trace_vjp<1, true><<<grid, kVjpThreads, 0, s>>>(P, A);
   } else {
-    if (vec) k_trace_vjp<kVjpRays, false><<<grid, kVjpThreads, 0, s>>>(P, A);
+    if (lean) k_trace_vjp_lean<kLeanRays><<<grid, kVjpThreads, 0, s>>>(P, A);
+    else if (vec) k_trace_vjp<kVjpRays, false><<<grid, kVjpThreads, 0, s>>>(P, A);
     else k_trace_vjp<1, false><<<grid, kVjpThreads, 0, s>>>(P, A);
   }
   if (A.partial) {
