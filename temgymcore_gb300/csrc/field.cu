@@ -336,16 +336,6 @@ struct DirArgs {
   float2* out;         // [gridDim.y][h][w] partials (or the image if gridDim.y == 1)
 };
 
-__device__ __forceinline__ float2 cexpf_turn(float logamp, uint64_t turns) {
-  // angle in radians from the top 32 bits (signed): [-pi, pi)
-  int32_t hi = (int32_t)(turns >> 32);
-  float ang = (float)hi * 1.4629180792671596e-09f;  // 2*pi / 2^32
-  float s, c;
-  __sincosf(ang, &s, &c);
-  float a = __expf(logamp);
-  return make_float2(a * c, a * s);
-}
-
 // Per (beam, strip) the log-amplitude decides how the strip is summed: skip
 // when it stays below kDirSkipLog (e^-60 of a unit amplitude), the geometric
 // recurrence while its start and per-step ratios stay inside float32 range
@@ -509,13 +499,6 @@ struct OperandArgs {
 
 namespace tg {
 
-__device__ __forceinline__ void split_bf16(float v, __nv_bfloat16_raw& hi, __nv_bfloat16_raw& lo) {
-  __nv_bfloat16 h = __float2bfloat16_rn(v);
-  __nv_bfloat16 l = __float2bfloat16_rn(v - __bfloat162float(h));
-  hi = static_cast<__nv_bfloat16_raw>(h);
-  lo = static_cast<__nv_bfloat16_raw>(l);
-}
-
 // One thread per (beam, block of kOpLines lines): the beam's coefficients are
 // loaded once and the phase advances by exact 64-bit increments from line to
 // line.  blockIdx.y is the line block ([0, lines_v / kOpLines) V rows, then U
@@ -549,24 +532,21 @@ __global__ void __launch_bounds__(256) k_field_operands(const __grid_constant__ 
   uint64_t th = p2 * (u0 * u0) + p1 * u0 + p0;
   uint64_t dth = p2 * (2 * u0 + 1) + p1;
   const uint64_t ddth = 2 * p2;
-  float d = (float)line0 - cen;
 #pragma unroll 4
   for (int j = 0; j < kOpLines; ++j) {
     float re = 0.f, im = 0.f;
     if (live_b && line0 + j < live_lines) {
-      const float2 z = cexpf_turn(e0 - (bq * d * d + bl * d), th);
+      const float2 z = sep_operand(e0, bq, bl, cen, line0 + j, th);
       re = z.x;
       im = z.y;
     }
-    __nv_bfloat16_raw h, l;
-    split_bf16(re, h, l);
-    dst[0] = h;
-    dst[plane] = l;
-    split_bf16(im, h, l);
-    dst[2 * plane] = h;
-    dst[3 * plane] = l;
+    uint32_t h2, l2;  // low half re, high half im
+    split_bf16x2(re, im, h2, l2);
+    dst[0] = __nv_bfloat16_raw{(unsigned short)(h2 & 0xffffu)};
+    dst[plane] = __nv_bfloat16_raw{(unsigned short)(l2 & 0xffffu)};
+    dst[2 * plane] = __nv_bfloat16_raw{(unsigned short)(h2 >> 16)};
+    dst[3 * plane] = __nv_bfloat16_raw{(unsigned short)(l2 >> 16)};
     dst += kpad;
-    d += 1.f;
     th += dth;
     dth += ddth;
   }
@@ -715,13 +695,17 @@ int launch_field_gemm(const __nv_bfloat16_raw* vplanes, const __nv_bfloat16_raw*
                       int lines_v, int lines_u, int64_t kpad, int splits, int h, int w,
                       float2* part, cudaStream_t s);  // field_gemm.cu
 
+static bool field_method_ok(int method) {
+  return method == TG_FIELD_DIRECT || method == TG_FIELD_SEPARABLE || method == TG_FIELD_DIRECT_F64;
+}
+
 }  // namespace tg
 
 using namespace tg;
 
 extern "C" size_t tg_field_workspace(int64_t n_beams, int32_t h, int32_t w, int32_t method) {
   if (n_beams < 0 || h <= 0 || w <= 0) return 0;
-  if (method != TG_FIELD_DIRECT && method != TG_FIELD_SEPARABLE && method != TG_FIELD_DIRECT_F64)
+  if (!field_method_ok(method))
     return 0;
   return field_layout(n_beams, h, w, method).total;
 }
@@ -801,7 +785,7 @@ extern "C" int tg_field_prep_input(const tg_beams* beams, const tg_pixel_map* pm
 extern "C" int tg_field_eval(int32_t method, int64_t n_beams, const tg_pixel_map* pm,
                              float* out, void* workspace, size_t ws_bytes, void* stream) {
   if (!pm || pm->h <= 0 || pm->w <= 0 || n_beams < 0 || !out) return TG_ERR_INVALID;
-  if (method != TG_FIELD_DIRECT && method != TG_FIELD_SEPARABLE && method != TG_FIELD_DIRECT_F64)
+  if (!field_method_ok(method))
     return TG_ERR_INVALID;
   FieldLayout L = field_layout(n_beams, pm->h, pm->w, method);
   if (!workspace || ws_bytes < L.total) return TG_ERR_WORKSPACE;

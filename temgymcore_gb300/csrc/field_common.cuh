@@ -17,11 +17,41 @@
 // the envelope maximum.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <stdint.h>
 
 #include "tg_common.cuh"
 
 namespace tg {
+
+// exp(logamp) * exp(i 2 pi turns / 2^64), the angle from the top 32 bits of
+// the turn fraction (signed): [-pi, pi).
+__device__ __forceinline__ float2 cexpf_turn(float logamp, uint64_t turns) {
+  int32_t hi = (int32_t)(turns >> 32);
+  float ang = (float)hi * 1.4629180792671596e-09f;  // 2*pi / 2^32
+  float s, c;
+  __sincosf(ang, &s, &c);
+  float a = __expf(logamp);
+  return make_float2(a * c, a * s);
+}
+
+// One separable operand value (a beam's row or column factor) at the integer
+// line g: exp(e0 - (bq d^2 + bl d) + i 2 pi th / 2^64) with d = g - cen and
+// th the exact fixed-point phase at g.
+__device__ __forceinline__ float2 sep_operand(float e0, float bq, float bl, float cen, int g,
+                                              uint64_t th) {
+  const float d = (float)g - cen;
+  return cexpf_turn(fmaf(-d, fmaf(bq, d, bl), e0), th);
+}
+
+// bf16 hi and lo parts of two floats (hi = bf16(v), lo = bf16(v - hi), both
+// round-to-nearest-even), each pair packed with a in the low half.
+__device__ __forceinline__ void split_bf16x2(float a, float b, uint32_t& hi, uint32_t& lo) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  const __nv_bfloat162 l = __floats2bfloat162_rn(a - __low2float(h), b - __high2float(h));
+  hi = *reinterpret_cast<const uint32_t*>(&h);
+  lo = *reinterpret_cast<const uint32_t*>(&l);
+}
 
 // Fast record (fixed-point phase, float32 envelope), 96 bytes.
 struct alignas(16) BeamFast {

@@ -21,6 +21,7 @@
 #include <cuda_runtime.h>
 
 #include <cstring>
+#include <mutex>
 
 #include "tg_common.cuh"
 
@@ -259,12 +260,40 @@ int field_gemm_splits(int64_t n, int h, int w) {
 int launch_field_gemm(const __nv_bfloat16_raw* vplanes, const __nv_bfloat16_raw* uplanes, int lines_v,
                       int lines_u, int64_t kpad, int splits, int h, int w, float2* part,
                       cudaStream_t s) {
+  // the eight tensor maps of a plane buffer, encoded once per (buffers,
+  // shape) and kept in a small round-robin cache (an evaluation cycles through
+  // two buffers; a few plans may alternate)
+  struct Entry {
+    const void *v, *u;
+    int64_t kpad;
+    int lv, lu;
+    GemmMaps maps;
+  };
+  static std::mutex mu;
+  static Entry cache[8];
+  static int used = 0, next = 0;
   GemmMaps maps;
-  std::memset(&maps, 0, sizeof(maps));
-  const size_t pv = (size_t)lines_v * kpad, pu = (size_t)lines_u * kpad;
-  for (int p = 0; p < 4; ++p) {
-    if (!make_map(&maps.v[p], vplanes + p * pv, kpad, lines_v)) return TG_ERR_CUDA;
-    if (!make_map(&maps.u[p], uplanes + p * pu, kpad, lines_u)) return TG_ERR_CUDA;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    int hit = -1;
+    for (int i = 0; i < used; ++i)
+      if (cache[i].v == vplanes && cache[i].u == uplanes && cache[i].kpad == kpad && cache[i].lv == lines_v &&
+          cache[i].lu == lines_u)
+        hit = i;
+    if (hit < 0) {
+      Entry e;
+      std::memset(&e, 0, sizeof(e));
+      e.v = vplanes; e.u = uplanes; e.kpad = kpad; e.lv = lines_v; e.lu = lines_u;
+      const size_t pv = (size_t)lines_v * kpad, pu = (size_t)lines_u * kpad;
+      for (int p = 0; p < 4; ++p) {
+        if (!make_map(&e.maps.v[p], vplanes + p * pv, kpad, lines_v)) return TG_ERR_CUDA;
+        if (!make_map(&e.maps.u[p], uplanes + p * pu, kpad, lines_u)) return TG_ERR_CUDA;
+      }
+      hit = used < 8 ? used++ : next;
+      next = (hit + 1) % 8;
+      cache[hit] = e;
+    }
+    maps = cache[hit].maps;
   }
   GemmArgs A;
   A.nkb = (int)(kpad / 32 / splits);
