@@ -327,33 +327,53 @@ k_trace_fwd(const __grid_constant__ Program P, const __grid_constant__ FwdArgs A
   if (kSh) sh_store_row(shw, A.rows + (size_t)blockIdx.x * sh_words(bins), sh_words(bins));
 }
 
-// hist[b] += sum over the CTA rows of their packed uint16 counters (one
-// thread per word = two bins, rows read coalesced; integer sums, so the order
-// does not matter).
+// hist[b] += sum over the CTA rows of their packed uint16 counters.  A block
+// takes 32 words (64 bins) and splits the rows over its 8 warps (warp g sums
+// rows g, g + 8, ...: each load of a warp is one 128-byte run), so that a
+// thread keeps only ~nrows / 8 loads in its chain; the 8 partial sums are
+// then added in shared memory.  Integer sums: the order does not matter.
+constexpr int kRowsWords = 32, kRowsGroups = 8;
+
 template <typename CountT>
-__global__ void k_hist_rows(const uint32_t* __restrict__ rows, int nrows, int bins,
-                            CountT* __restrict__ hist) {
+__global__ void __launch_bounds__(kRowsWords * kRowsGroups)
+k_hist_rows(const uint32_t* __restrict__ rows, int nrows, int bins, CountT* __restrict__ hist) {
+  __shared__ unsigned long long slo[kRowsGroups][kRowsWords], shi[kRowsGroups][kRowsWords];
   const int words = sh_words(bins);
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < words; i += gridDim.x * blockDim.x) {
-    unsigned long long lo[2] = {0ull, 0ull}, hi[2] = {0ull, 0ull};
-    int r = 0;
-    for (; r + 4 <= nrows; r += 4) {
+  const int wi = threadIdx.x % kRowsWords, g = threadIdx.x / kRowsWords;
+  const int i = blockIdx.x * kRowsWords + wi;
+  unsigned long long lo[4] = {0ull, 0ull, 0ull, 0ull}, hi[4] = {0ull, 0ull, 0ull, 0ull};
+  if (i < words) {
+    int r = g;
+    for (; r + 3 * kRowsGroups < nrows; r += 4 * kRowsGroups) {  // four loads in flight
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        const uint32_t v = rows[(size_t)(r + u) * words + i];
-        lo[u & 1] += v & 0xffffu;
-        hi[u & 1] += v >> 16;
+        const uint32_t v = __ldcs(rows + (size_t)(r + u * kRowsGroups) * words + i);
+        lo[u] += v & 0xffffu;
+        hi[u] += v >> 16;
       }
     }
-    for (; r < nrows; ++r) {
-      const uint32_t v = rows[(size_t)r * words + i];
+    for (; r < nrows; r += kRowsGroups) {
+      const uint32_t v = __ldcs(rows + (size_t)r * words + i);
       lo[0] += v & 0xffffu;
       hi[0] += v >> 16;
     }
-    hist[2 * i] += (CountT)(lo[0] + lo[1]);
-    if (2 * i + 1 < bins) hist[2 * i + 1] += (CountT)(hi[0] + hi[1]);
+  }
+  slo[g][wi] = (lo[0] + lo[1]) + (lo[2] + lo[3]);
+  shi[g][wi] = (hi[0] + hi[1]) + (hi[2] + hi[3]);
+  __syncthreads();
+  if (g == 0 && i < words) {
+    unsigned long long a = 0ull, b = 0ull;
+#pragma unroll
+    for (int k = 0; k < kRowsGroups; ++k) {
+      a += slo[k][wi];
+      b += shi[k][wi];
+    }
+    hist[2 * i] += (CountT)a;
+    if (2 * i + 1 < bins) hist[2 * i + 1] += (CountT)b;
   }
 }
+
+static inline int hist_rows_blocks(int bins) { return (sh_words(bins) + kRowsWords - 1) / kRowsWords; }
 
 struct BinArgs {
   int64_t n;
@@ -573,9 +593,9 @@ static int trace_fwd_impl(const tg_model* model, const tg_rays* in, tg_rays* out
       }
     }
     if (e != cudaSuccess || cudaGetLastError() != cudaSuccess) return TG_ERR_CUDA;
-    const int rb = (sh_words(bins) + 255) / 256;
-    if (hist_i64) k_hist_rows<long long><<<rb, 256, 0, s>>>(A.rows, blocks, bins, reinterpret_cast<long long*>(hist));
-    else k_hist_rows<int><<<rb, 256, 0, s>>>(A.rows, blocks, bins, reinterpret_cast<int*>(hist));
+    const int rb = hist_rows_blocks(bins);
+    if (hist_i64) k_hist_rows<long long><<<rb, kRowsWords * kRowsGroups, 0, s>>>(A.rows, blocks, bins, reinterpret_cast<long long*>(hist));
+    else k_hist_rows<int><<<rb, kRowsWords * kRowsGroups, 0, s>>>(A.rows, blocks, bins, reinterpret_cast<int*>(hist));
     return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
   }
   const int threads = 256;
@@ -648,9 +668,9 @@ static int bin_impl(int64_t n, const float* x, const float* y, const uint8_t* ma
       if (e == cudaSuccess) k_bin<int, true><<<blocks, kShThreads, smem, s>>>(A, B);
     }
     if (e != cudaSuccess || cudaGetLastError() != cudaSuccess) return TG_ERR_CUDA;
-    const int rb = (sh_words(bins) + 255) / 256;
-    if (hist_i64) k_hist_rows<long long><<<rb, 256, 0, s>>>(A.rows, blocks, bins, reinterpret_cast<long long*>(hist));
-    else k_hist_rows<int><<<rb, 256, 0, s>>>(A.rows, blocks, bins, reinterpret_cast<int*>(hist));
+    const int rb = hist_rows_blocks(bins);
+    if (hist_i64) k_hist_rows<long long><<<rb, kRowsWords * kRowsGroups, 0, s>>>(A.rows, blocks, bins, reinterpret_cast<long long*>(hist));
+    else k_hist_rows<int><<<rb, kRowsWords * kRowsGroups, 0, s>>>(A.rows, blocks, bins, reinterpret_cast<int*>(hist));
     return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
   }
   int64_t need = (n + 255) / 256;
@@ -698,7 +718,7 @@ static int hist_pix_launch(int64_t n, const void* py, const void* px, int h, int
     if (e != cudaSuccess) return TG_ERR_CUDA;
     k_hist_pix<IdxT, CountT, true><<<blocks, kShThreads, smem, s>>>(n, y, x, h, w, hh, rows);
     if (cudaGetLastError() != cudaSuccess) return TG_ERR_CUDA;
-    k_hist_rows<CountT><<<(sh_words(bins) + 255) / 256, 256, 0, s>>>(rows, blocks, bins, hh);
+    k_hist_rows<CountT><<<hist_rows_blocks(bins), kRowsWords * kRowsGroups, 0, s>>>(rows, blocks, bins, hh);
   } else {
     int per_sm = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hist_pix<IdxT, CountT>, 256, 0);
@@ -1104,25 +1124,27 @@ k_trace_vjp_lean(const __grid_constant__ Program P, const __grid_constant__ VjpA
   }
 }
 
-// raw[i] += sum over blocks of partial[b][i], in block order.
-__global__ void k_reduce_partials(const double* __restrict__ partial, int nblocks,
-                                  int width, double* __restrict__ raw) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= width) return;
-  // eight independent partial sums keep eight loads in flight (fixed order)
-  double a[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-  int b = 0;
-  for (; b + 8 <= nblocks; b += 8) {
+// raw[i] += sum over blocks of partial[b][i]: one block per entry i, thread t
+// adds the blocks t, t + 256, ... in order, then a fixed shared-memory tree
+// combines the 256 sums (the same order on every run).
+constexpr int kReduceThreads = 256;
+
+__global__ void __launch_bounds__(kReduceThreads)
+k_reduce_partials(const double* __restrict__ partial, int nblocks, int width, double* __restrict__ raw) {
+  __shared__ double sh[kReduceThreads];
+  const int i = blockIdx.x;
+  double a = 0.0;
+  for (int b = threadIdx.x; b < nblocks; b += kReduceThreads) a += partial[(size_t)b * width + i];
+  sh[threadIdx.x] = a;
+  __syncthreads();
 #pragma unroll
-    for (int u = 0; u < 8; ++u) a[u] += partial[(size_t)(b + u) * width + i];
+  for (int h = kReduceThreads / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h) sh[threadIdx.x] += sh[threadIdx.x + h];
+    __syncthreads();
   }
-  for (int u = 0; b < nblocks; ++b, ++u) a[u] += partial[(size_t)b * width + i];
-  raw[i] += ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
+  if (threadIdx.x == 0) raw[i] += sh[0];
 }
 
-// Grid of the adjoint: every block resident at once (the grid-stride loop
-// gives each block the same share, so a block that waits for a free slot
-// would double the tail).  The residency of the wider variant bounds both.
 template <auto Kernel>
 static int vjp_per_sm() {
   static int per_sm = 0;
@@ -1201,7 +1223,7 @@ extern "C" int tg_trace_vjp(const tg_model* model, const tg_rays* in, const tg_r
   }
   if (A.partial) {
     int width = P.n_steps * 4;
-    k_reduce_partials<<<(width + 127) / 128, 128, 0, s>>>(A.partial, grid, width, raw);
+    k_reduce_partials<<<width, kReduceThreads, 0, s>>>(A.partial, grid, width, raw);
   }
   return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
 }
