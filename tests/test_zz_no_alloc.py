@@ -5,7 +5,8 @@ The entry point keeps its scratch in a fixed array inside the library.
 
 Called through the C ABI twice in a row; each result must match the regular
 entry points (tg_field_prep + tg_field_eval, direct method) to the direct
-kernel's tolerance, and requests beyond the stated limits are rejected.
+kernel's tolerance and the float64 oracle on a pixel sample, and requests
+beyond the stated limits are rejected.
 This file sorts last so a failure here does not hide any other test."""
 import ctypes as C
 
@@ -66,6 +67,12 @@ def test_noalloc_matches_regular_direct_path(cuda):
         assert np.max(np.abs(g - r)) / np.max(np.abs(r)) <= TOL
     assert torch.equal(outs[0], outs[1])
     assert N.error_word() == 0
+    # and directly against the float64 oracle on a pixel sample
+    import oracle.field as OF
+    idx = np.random.default_rng(1).choice(96 * 160, 256, replace=False)
+    ref_o = OF.make_gaussian_image(w["rays"], w["model"], pixel_index=idx, chunk=1024)
+    g0 = outs[0].cpu().numpy().reshape(-1)[idx]
+    assert np.max(np.abs(g0 - ref_o)) / np.max(np.abs(ref_o)) <= 1e-4
     del keep
 
 
