@@ -676,6 +676,26 @@ int tg_field_vjp_input(const tg_beams *beams, const tg_pixel_map *pm, const floa
                        const tg_field_grads *out, void *workspace, size_t ws_bytes, void *stream);
 
 /*
+ * tg_field_vjp_ex / tg_field_vjp_input_ex - tg_field_vjp / tg_field_vjp_input
+ * with the per-beam moments formed by `method`: TG_FIELD_DIRECT (the pass
+ * over beams x pixels above) or TG_FIELD_SEPARABLE (beams with diagonal Q2
+ * on an unrotated grid, as the separable forward: the field factors into
+ * row and column phasors, E_b(r, c) = V_b(r) U_b(c), so the moments come
+ * from one split-BF16 complex GEMM on the tensor cores,
+ * X_a[r][b] = sum_c conj(grad[r][c]) U_b(c) dc^a for a = 0, 1, 2, and a pass
+ * over the rows with V_b(r) dr^k; a beam that is not separable sets
+ * TG_EW_NONSEPARABLE).  Same outputs; workspace tg_field_vjp_workspace_ex
+ * (the separable method holds the bf16 planes of conj(grad) and of the 3n
+ * column factors and the h x 3n product).
+ */
+size_t tg_field_vjp_workspace_ex(int32_t method, int64_t n_beams, int32_t h, int32_t w);
+int tg_field_vjp_ex(int32_t method, const tg_model *model, const tg_beams *beams, const tg_pixel_map *pm,
+                    const float *grad, const tg_field_grads *out, void *workspace, size_t ws_bytes,
+                    void *stream);
+int tg_field_vjp_input_ex(int32_t method, const tg_beams *beams, const tg_pixel_map *pm, const float *grad,
+                          const tg_field_grads *out, void *workspace, size_t ws_bytes, void *stream);
+
+/*
  * tg_field_direct_noalloc - tg_field_prep + tg_field_eval(TG_FIELD_DIRECT)
  * in one call that allocates nothing.  No counterpart in the reference: it
  * exists for callers that cannot call cudaMalloc (an allocator owned by

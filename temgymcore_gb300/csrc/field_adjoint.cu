@@ -25,12 +25,16 @@
 //   4. k_field_model_sum: the model parameters' per-block sums in a fixed
 //      order, written as per-step sums in the layout of tg_trace_vjp.
 // Every reduction runs in a fixed order, so the gradients are deterministic.
+#include <cuda_bf16.h>
+
 #include <cmath>
 #include <cstring>
 #include <vector>
 
 #include "field_common.cuh"
 #include "tg_common.cuh"
+
+TG_DEFINE_ERROR_WORD(fadj)
 
 namespace tg {
 
@@ -548,15 +552,164 @@ __global__ void k_field_model_sum(const double* __restrict__ part, const __grid_
   raw[A.target[d]] = a;
 }
 
+// ------------------------------------------- separable moments (tensor cores)
+// For separable beams E_b(r, c) = V_b(r) U_b(c) (the factors of the separable
+// forward), so the six moments factor through one complex GEMM:
+//   X_a[r][b] = sum_c conj(G[r][c]) U_b(c) dc^a,  a = 0, 1, 2,  dc = c - c0_b,
+//   mu_{a,k}[b] = sum_r V_b(r) dr^k X_a[r][b],      dr = r - r0_b,
+// with (a, k) over (0,0) (1,0) (0,1) (2,0) (1,1) (0,2).  conj(G) and
+// U_b dc^a go into bf16 hi + lo planes (K = the column index, contiguous) for
+// the split-BF16 tcgen05 GEMM of the forward (field_gemm.cu): its "V" operand
+// is conj(G) ([rows][cols]), its "U" operand the 3 x beams lines U_b dc^a
+// (line a * bpad + b), so X = [rows][3 * bpad] complex.  The moments about
+// the envelope centre keep dc and dr small where the beam lives (no
+// cancellation between large powers).
+
+// conj(G) as four bf16 planes [rows_pad][cols_pad] (zero beyond h x w).
+__global__ void k_adj_gplanes(const float2* __restrict__ g, int h, int w, int rows_pad, int cols_pad,
+                              __nv_bfloat16_raw* __restrict__ planes) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t total = (int64_t)rows_pad * cols_pad;
+  if (i >= total) return;
+  const int r = (int)(i / cols_pad), c = (int)(i % cols_pad);
+  float re = 0.f, im = 0.f;
+  if (r < h && c < w) {
+    const float2 v = g[(size_t)r * w + c];
+    re = v.x;
+    im = -v.y;
+  }
+  uint32_t h2, l2;
+  split_bf16x2(re, im, h2, l2);
+  planes[i] = __nv_bfloat16_raw{(unsigned short)(h2 & 0xffffu)};
+  planes[total + i] = __nv_bfloat16_raw{(unsigned short)(l2 & 0xffffu)};
+  planes[2 * total + i] = __nv_bfloat16_raw{(unsigned short)(h2 >> 16)};
+  planes[3 * total + i] = __nv_bfloat16_raw{(unsigned short)(l2 >> 16)};
+}
+
+// U_b(c) dc^a as four bf16 planes [3 * bpad][cols_pad]: one thread per (beam,
+// block of 16 columns), the column factor of the separable forward (exact
+// fixed-point phase stepped by 64-bit differences), three powers of dc, 32
+// bytes per plane and power stored as two 16-byte vectors.
+constexpr int kAdjCols = 16;
+
+__global__ void __launch_bounds__(128) k_adj_uplanes(const BeamFast* __restrict__ beams, int64_t n,
+                                                     int64_t bpad, int w, int cols_pad,
+                                                     __nv_bfloat16_raw* __restrict__ planes) {
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= bpad) return;
+  const int c0 = (int)blockIdx.y * kAdjCols;
+  const int64_t plane = 3 * bpad * (int64_t)cols_pad;
+  const bool live = b < n;
+  uint64_t p2 = 0, p1 = 0;
+  float cen = 0.f, bq = 0.f, bl = 0.f;
+  if (live) {
+    const BeamFast& B = beams[b];
+    if (B.p_rc != 0 || B.b_rc != 0.f) atomicOr(&g_tg_err, 0x10u);
+    p2 = B.p_cc; p1 = B.p_c; cen = B.c0; bq = B.b_cc; bl = B.l_c;
+  }
+  const uint64_t u0 = (uint64_t)c0;
+  uint64_t th = p2 * (u0 * u0) + p1 * u0;
+  uint64_t dth = p2 * (2 * u0 + 1) + p1;
+  const uint64_t ddth = 2 * p2;
+  float ur[kAdjCols], ui[kAdjCols];
+#pragma unroll
+  for (int j = 0; j < kAdjCols; ++j) {
+    ur[j] = 0.f;
+    ui[j] = 0.f;
+    if (live && c0 + j < w) {
+      const float2 z = sep_operand(0.f, bq, bl, cen, c0 + j, th);
+      ur[j] = z.x;
+      ui[j] = z.y;
+    }
+    th += dth;
+    dth += ddth;
+  }
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    uint32_t rh[kAdjCols / 2], rl[kAdjCols / 2], ih[kAdjCols / 2], il[kAdjCols / 2];
+#pragma unroll
+    for (int j = 0; j < kAdjCols; j += 2) {
+      float m0 = 1.f, m1 = 1.f;
+      if (a > 0) {
+        const float d0 = (float)(c0 + j) - cen, d1 = (float)(c0 + j + 1) - cen;
+        m0 = a == 1 ? d0 : d0 * d0;
+        m1 = a == 1 ? d1 : d1 * d1;
+      }
+      uint32_t h2, l2;
+      split_bf16x2(ur[j] * m0, ur[j + 1] * m1, h2, l2);
+      rh[j / 2] = h2; rl[j / 2] = l2;
+      split_bf16x2(ui[j] * m0, ui[j + 1] * m1, h2, l2);
+      ih[j / 2] = h2; il[j / 2] = l2;
+    }
+    const int64_t row = (int64_t)a * bpad + b;
+    uint4* dst = reinterpret_cast<uint4*>(planes + row * cols_pad + c0);
+    const int64_t pv = plane / 8;  // plane stride in uint4
+    dst[0] = make_uint4(rh[0], rh[1], rh[2], rh[3]); dst[1] = make_uint4(rh[4], rh[5], rh[6], rh[7]);
+    dst[pv] = make_uint4(rl[0], rl[1], rl[2], rl[3]); dst[pv + 1] = make_uint4(rl[4], rl[5], rl[6], rl[7]);
+    dst[2 * pv] = make_uint4(ih[0], ih[1], ih[2], ih[3]); dst[2 * pv + 1] = make_uint4(ih[4], ih[5], ih[6], ih[7]);
+    dst[3 * pv] = make_uint4(il[0], il[1], il[2], il[3]); dst[3 * pv + 1] = make_uint4(il[4], il[5], il[6], il[7]);
+  }
+}
+
+// mom[b] from X: one thread per beam walks the rows with the row factor
+// V_b(r) (exact fixed-point phase, as the forward's V operand), float32 sums
+// over 16 rows added in float64.
+__global__ void __launch_bounds__(128) k_adj_sep_moments(const BeamFast* __restrict__ beams, int64_t n,
+                                                         const float2* __restrict__ x, int h, int64_t bpad,
+                                                         double* __restrict__ mom) {
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= n) return;
+  const BeamFast& B = beams[b];
+  const uint64_t p2 = B.p_rr, p1 = B.p_r, p0 = B.p_0;
+  uint64_t th = p0, dth = p2 + p1;
+  const uint64_t ddth = 2 * p2;
+  const int64_t ld = 3 * bpad;
+  double acc[12];
+#pragma unroll
+  for (int i = 0; i < 12; ++i) acc[i] = 0.0;
+  for (int r0 = 0; r0 < h; r0 += 16) {
+    float s[12];
+#pragma unroll
+    for (int i = 0; i < 12; ++i) s[i] = 0.f;
+    const int r1 = min(h, r0 + 16);
+    for (int r = r0; r < r1; ++r) {
+      const float2 v = sep_operand(B.e0, B.b_rr, B.l_r, B.r0, r, th);
+      th += dth;
+      dth += ddth;
+      const float dr = (float)r - B.r0;
+      const float2* xr = x + (size_t)r * ld + b;
+      const float2 x0 = xr[0], x1 = xr[bpad], x2 = xr[2 * bpad];
+      const float p0r = v.x * x0.x - v.y * x0.y, p0i = v.x * x0.y + v.y * x0.x;
+      const float p1r = v.x * x1.x - v.y * x1.y, p1i = v.x * x1.y + v.y * x1.x;
+      const float p2r = v.x * x2.x - v.y * x2.y, p2i = v.x * x2.y + v.y * x2.x;
+      s[0] += p0r; s[1] += p0i;                                // 1
+      s[2] += p1r; s[3] += p1i;                                // dc
+      s[4] = fmaf(dr, p0r, s[4]); s[5] = fmaf(dr, p0i, s[5]);  // dr
+      s[6] += p2r; s[7] += p2i;                                // dc^2
+      s[8] = fmaf(dr, p1r, s[8]); s[9] = fmaf(dr, p1i, s[9]);  // dr dc
+      const float dr2 = dr * dr;
+      s[10] = fmaf(dr2, p0r, s[10]); s[11] = fmaf(dr2, p0i, s[11]);  // dr^2
+    }
+#pragma unroll
+    for (int i = 0; i < 12; ++i) acc[i] += (double)s[i];
+  }
+#pragma unroll
+  for (int i = 0; i < 12; ++i) mom[b * 12 + i] = acc[i];
+}
+
 // ------------------------------------------------------------ host
 struct AdjLayout {
   size_t rec, part, mom, model, total;
   int col_chunks, row_splits, rows_per_split, beam_chunks, bg_blocks;
+  // separable moments on the tensor cores (method TG_FIELD_SEPARABLE)
+  size_t gplanes, uplanes, xprod;
+  int rows_pad, cols_pad;
+  int64_t bpad;
 };
 
 static inline size_t al256a(size_t v) { return (v + 255) & ~(size_t)255; }
 
-static AdjLayout adj_layout(int64_t n, int h, int w) {
+static AdjLayout adj_layout(int64_t n, int h, int w, int method = TG_FIELD_DIRECT) {
   AdjLayout L;
   std::memset(&L, 0, sizeof(L));
   L.col_chunks = (w + kMCols - 1) / kMCols;
@@ -577,6 +730,14 @@ static AdjLayout adj_layout(int64_t n, int h, int w) {
   L.part = off; off = al256a(off + (size_t)L.col_chunks * L.row_splits * n * 12 * sizeof(float));
   L.mom = off; off = al256a(off + (size_t)n * 12 * sizeof(double));
   L.model = off; off = al256a(off + (size_t)L.bg_blocks * kND * sizeof(double));
+  if (method == TG_FIELD_SEPARABLE) {
+    L.rows_pad = (h + 127) / 128 * 128;
+    L.cols_pad = (w + 31) / 32 * 32;
+    L.bpad = (n + 127) / 128 * 128;
+    L.gplanes = off; off = al256a(off + (size_t)4 * L.rows_pad * L.cols_pad * 2);
+    L.uplanes = off; off = al256a(off + (size_t)4 * 3 * L.bpad * L.cols_pad * 2);
+    L.xprod = off; off = al256a(off + (size_t)h * 3 * L.bpad * sizeof(float2));
+  }
   L.total = off;
   return L;
 }
@@ -596,9 +757,22 @@ extern "C" size_t tg_field_vjp_workspace(int64_t n_beams, int32_t h, int32_t w) 
   return adj_layout(n_beams, h, w).total;
 }
 
+extern "C" size_t tg_field_vjp_workspace_ex(int32_t method, int64_t n_beams, int32_t h, int32_t w) {
+  if (n_beams < 0 || h <= 0 || w <= 0) return 0;
+  if (method != TG_FIELD_DIRECT && method != TG_FIELD_SEPARABLE) return 0;
+  return adj_layout(n_beams, h, w, method).total;
+}
+
+namespace tg {
+int launch_field_gemm(const __nv_bfloat16_raw* vplanes, const __nv_bfloat16_raw* uplanes, int lines_v,
+                      int lines_u, int64_t kpad, int splits, int h, int w, float2* part,
+                      cudaStream_t s);  // field_gemm.cu
+}
+
 static int field_vjp_impl(const tg_model* model, const tg_beams* beams, const tg_pixel_map* pm,
                           const float* grad, const tg_field_grads* out, void* workspace, size_t ws_bytes,
-                          void* stream) {
+                          void* stream, int method = TG_FIELD_DIRECT) {
+  if (method != TG_FIELD_DIRECT && method != TG_FIELD_SEPARABLE) return TG_ERR_INVALID;
   if (!beams || !pm || !grad || !out || pm->h <= 0 || pm->w <= 0 || beams->n < 0) return TG_ERR_INVALID;
   const bool input_plane = model == nullptr;
   if (input_plane && out->raw) return TG_ERR_INVALID;  // no model, no per-step sums
@@ -613,7 +787,7 @@ static int field_vjp_impl(const tg_model* model, const tg_beams* beams, const tg
     if (st != TG_OK) return st;
     if (dm.n_aber) return TG_ERR_UNSUPPORTED;  // the aberrated lens has no field adjoint here
   }
-  const AdjLayout L = adj_layout(n, pm->h, pm->w);
+  const AdjLayout L = adj_layout(n, pm->h, pm->w, method);
   if (!workspace || ws_bytes < L.total) return TG_ERR_WORKSPACE;
   if (((uintptr_t)workspace & 255) != 0) return TG_ERR_ALIGN;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
@@ -635,9 +809,25 @@ static int field_vjp_impl(const tg_model* model, const tg_beams* beams, const tg
   MA.col_chunks = L.col_chunks;
   MA.rows_per_split = L.rows_per_split;
   MA.part = reinterpret_cast<float*>(ws + L.part);
-  k_field_moments<<<dim3(L.col_chunks * L.row_splits, L.beam_chunks), kMThreads, 0, s>>>(MA);
   double* mom = reinterpret_cast<double*>(ws + L.mom);
-  k_field_moment_sum<<<(int)((n * 12 + 255) / 256), 256, 0, s>>>(MA.part, L.col_chunks * L.row_splits, n, mom);
+  if (method == TG_FIELD_SEPARABLE) {
+    // the GEMM X = conj(G) (U dc^a)^T on the tensor cores, then the rows
+    auto* gp = reinterpret_cast<__nv_bfloat16_raw*>(ws + L.gplanes);
+    auto* up = reinterpret_cast<__nv_bfloat16_raw*>(ws + L.uplanes);
+    float2* xp = reinterpret_cast<float2*>(ws + L.xprod);
+    const int64_t gtot = (int64_t)L.rows_pad * L.cols_pad;
+    k_adj_gplanes<<<(unsigned)((gtot + 255) / 256), 256, 0, s>>>(MA.g, pm->h, pm->w, L.rows_pad, L.cols_pad, gp);
+    k_adj_uplanes<<<dim3((unsigned)((L.bpad + 127) / 128), (unsigned)(L.cols_pad / kAdjCols)), 128, 0, s>>>(
+        MA.beams, n, L.bpad, pm->w, L.cols_pad, up);
+    if (3 * L.bpad > INT32_MAX) return TG_ERR_TOO_LARGE;
+    int st2 = launch_field_gemm(gp, up, L.rows_pad, (int)(3 * L.bpad), L.cols_pad, 1, pm->h, (int)(3 * L.bpad),
+                                xp, s);
+    if (st2 != TG_OK) return st2;
+    k_adj_sep_moments<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(MA.beams, n, xp, pm->h, L.bpad, mom);
+  } else {
+    k_field_moments<<<dim3(L.col_chunks * L.row_splits, L.beam_chunks), kMThreads, 0, s>>>(MA);
+    k_field_moment_sum<<<(int)((n * 12 + 255) / 256), 256, 0, s>>>(MA.part, L.col_chunks * L.row_splits, n, mom);
+  }
   // 3. directions: the central ray's x, y, dx, dy, then the model's step parameters
   std::vector<Dir> dirs;
   const bool ray = out->x || out->y || out->dx || out->dy;
@@ -726,4 +916,17 @@ extern "C" int tg_field_vjp(const tg_model* model, const tg_beams* beams, const 
 extern "C" int tg_field_vjp_input(const tg_beams* beams, const tg_pixel_map* pm, const float* grad,
                                   const tg_field_grads* out, void* workspace, size_t ws_bytes, void* stream) {
   return field_vjp_impl(nullptr, beams, pm, grad, out, workspace, ws_bytes, stream);
+}
+
+extern "C" int tg_field_vjp_ex(int32_t method, const tg_model* model, const tg_beams* beams,
+                               const tg_pixel_map* pm, const float* grad, const tg_field_grads* out,
+                               void* workspace, size_t ws_bytes, void* stream) {
+  if (!model) return TG_ERR_INVALID;
+  return field_vjp_impl(model, beams, pm, grad, out, workspace, ws_bytes, stream, method);
+}
+
+extern "C" int tg_field_vjp_input_ex(int32_t method, const tg_beams* beams, const tg_pixel_map* pm,
+                                     const float* grad, const tg_field_grads* out, void* workspace,
+                                     size_t ws_bytes, void* stream) {
+  return field_vjp_impl(nullptr, beams, pm, grad, out, workspace, ws_bytes, stream, method);
 }

@@ -386,6 +386,7 @@ extern "C" int tg_internal_err_field(uint32_t*, int);
 extern "C" int tg_internal_err_gemm(uint32_t*, int);
 extern "C" int tg_internal_err_fit(uint32_t*, int);
 extern "C" int tg_internal_err_batch(uint32_t*, int);
+extern "C" int tg_internal_err_fadj(uint32_t*, int);
 
 extern "C" int tg_get_error_word(uint32_t* out, int clear);
 
@@ -404,5 +405,6 @@ extern "C" int tg_get_error_word(uint32_t* out, int clear) {
   if (s == TG_OK) s = tg_internal_err_gemm(out, clear);
   if (s == TG_OK) s = tg_internal_err_fit(out, clear);
   if (s == TG_OK) s = tg_internal_err_batch(out, clear);
+  if (s == TG_OK) s = tg_internal_err_fadj(out, clear);
   return s;
 }

@@ -70,6 +70,12 @@ N.register("tg_field_vjp", C.c_int, [C.POINTER(N.TgModel), C.POINTER(TgBeams), C
                                      C.c_void_p, C.POINTER(TgFieldGrads), C.c_void_p, C.c_size_t, C.c_void_p])
 N.register("tg_field_vjp_input", C.c_int, [C.POINTER(TgBeams), C.POINTER(TgPixelMap), C.c_void_p,
                                            C.POINTER(TgFieldGrads), C.c_void_p, C.c_size_t, C.c_void_p])
+N.register("tg_field_vjp_workspace_ex", C.c_size_t, [C.c_int32, C.c_int64, C.c_int32, C.c_int32])
+N.register("tg_field_vjp_ex", C.c_int, [C.c_int32, C.POINTER(N.TgModel), C.POINTER(TgBeams),
+                                        C.POINTER(TgPixelMap), C.c_void_p, C.POINTER(TgFieldGrads),
+                                        C.c_void_p, C.c_size_t, C.c_void_p])
+N.register("tg_field_vjp_input_ex", C.c_int, [C.c_int32, C.POINTER(TgBeams), C.POINTER(TgPixelMap), C.c_void_p,
+                                              C.POINTER(TgFieldGrads), C.c_void_p, C.c_size_t, C.c_void_p])
 
 
 def _f64(v, n, dev, width=None):
@@ -228,17 +234,22 @@ class FieldPlan:
     def separable(self) -> bool:
         return int(self.flags.item()) == 0
 
-    def vjp(self, grad: torch.Tensor, beams: bool = True, model: bool = True) -> dict:
+    def vjp(self, grad: torch.Tensor, beams: bool = True, model: bool = True, method: str | None = None) -> dict:
         """Gradients of a real loss L from its gradient with respect to the
         field, ``grad`` = dL/dRe F + i dL/dIm F (complex (H, W), PyTorch's
         convention): per beam ``amplitude`` (complex64), ``pathlength``,
         ``x``, ``y``, ``dx``, ``dy`` (float64) when ``beams``, and the model's
         per-step sums ``raw`` (float64 [2 * components, 4], the layout of the
-        trace adjoint) when ``model`` (tg_field_vjp / tg_field_vjp_input)."""
+        trace adjoint) when ``model`` (tg_field_vjp_ex / tg_field_vjp_input_ex).
+        ``method`` ("separable" or "direct", default: the plan's) picks how the
+        per-beam moments are formed: a GEMM on the tensor cores for separable
+        beams, or the direct pass over beams x pixels."""
         n, dev = self.beams.n, self.dev
+        method = method or self.method
+        code = FIELD_SEPARABLE if method == "separable" else FIELD_DIRECT
         g = torch.view_as_real(grad.to(device=dev, dtype=torch.complex64).reshape(self.shape).contiguous())
-        if self._vjp_ws is None:
-            nb = N.lib().tg_field_vjp_workspace(n, self.pm.h, self.pm.w)
+        nb = N.lib().tg_field_vjp_workspace_ex(code, n, self.pm.h, self.pm.w)
+        if self._vjp_ws is None or self._vjp_ws.numel() < nb + 256:
             self._vjp_ws = torch.empty(nb + 256, dtype=torch.uint8, device=dev)
         ws = self._vjp_ws
         off = (-ws.data_ptr()) % 256
@@ -254,17 +265,17 @@ class FieldPlan:
             res["raw"] = torch.empty((2 * len(self.comps), 4), dtype=torch.float64, device=dev)
             out.raw = res["raw"].data_ptr()
         if self.comps is None:
-            st = N.lib().tg_field_vjp_input(C.byref(self.beams.struct()), C.byref(self.pm), g.data_ptr(),
-                                            C.byref(out), ws.data_ptr() + off, ws.numel() - off,
-                                            N.stream_ptr())
-            N.check(st, "tg_field_vjp_input")
+            st = N.lib().tg_field_vjp_input_ex(code, C.byref(self.beams.struct()), C.byref(self.pm),
+                                               g.data_ptr(), C.byref(out), ws.data_ptr() + off,
+                                               ws.numel() - off, N.stream_ptr())
+            N.check(st, "tg_field_vjp_input_ex")
         else:
             m, keep = pack_model(self.comps)
-            st = N.lib().tg_field_vjp(C.byref(m), C.byref(self.beams.struct()), C.byref(self.pm),
-                                      g.data_ptr(), C.byref(out), ws.data_ptr() + off, ws.numel() - off,
-                                      N.stream_ptr())
+            st = N.lib().tg_field_vjp_ex(code, C.byref(m), C.byref(self.beams.struct()), C.byref(self.pm),
+                                         g.data_ptr(), C.byref(out), ws.data_ptr() + off, ws.numel() - off,
+                                         N.stream_ptr())
             del keep
-            N.check(st, "tg_field_vjp")
+            N.check(st, "tg_field_vjp_ex")
         return res
 
 

@@ -29,8 +29,9 @@ def cuda():
 
 
 def normwise_err(got, ref):
-    got = np.asarray(got, dtype=np.float64)
-    ref = np.asarray(ref, dtype=np.float64)
+    got, ref = np.asarray(got), np.asarray(ref)
+    dt = np.complex128 if (np.iscomplexobj(got) or np.iscomplexobj(ref)) else np.float64
+    got, ref = got.astype(dt), ref.astype(dt)
     scale = np.max(np.abs(ref)) if ref.size else 1.0
     if scale == 0:
         scale = 1.0
