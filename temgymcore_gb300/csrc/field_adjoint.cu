@@ -16,12 +16,16 @@
 //   1. k_field_moments: the six complex moments of every beam, a reduction
 //      over (beam, pixel) that evaluates E_b with the direct kernel's exact
 //      fixed-point phase and float32 recurrence (unit-amplitude records),
-//      about the beam's envelope centre for conditioning;
+//      about the beam's envelope centre for conditioning; for separable
+//      beams (method TG_FIELD_SEPARABLE) instead one split-BF16 GEMM on the
+//      tensor cores and a pass over the rows (k_adj_gplanes, k_adj_uplanes,
+//      the forward's k_field_gemm, k_adj_sep_moments; see below);
 //   2. k_field_moment_sum: the per-block partials summed in a fixed order;
-//   3. k_field_beam_grad<8>: per beam, the preparation arithmetic again in
-//      float64 forward mode (dual numbers carrying 8 directions: the central
-//      ray's x, y, dx, dy and the model's step parameters) for d kap / dp and
-//      d log pref / dp, contracted with the moments;
+//   3. k_field_beam_grad<4>: per beam, the preparation arithmetic again in
+//      float64 forward mode (dual numbers carrying 4 directions a launch, as
+//      many launches as there are directions: the central ray's x, y, dx, dy
+//      and the model's step parameters) for d kap / dp and d log pref / dp,
+//      contracted with the moments;
 //   4. k_field_model_sum: the model parameters' per-block sums in a fixed
 //      order, written as per-step sums in the layout of tg_trace_vjp.
 // Every reduction runs in a fixed order, so the gradients are deterministic.
@@ -288,7 +292,12 @@ __device__ __forceinline__ M2<N> nan0(const M2<N>& m) {
 
 // ------------------------------------------------------------ beam gradient
 constexpr int kND = 8;               // directions per launch
+// Four directions a launch, 64 threads a block.  Measured on the separable
+// 16,384-beam adjoint (whole call): 8 directions (14 KB of stack a thread)
+// 1.40 ms, 4 directions 0.99 ms, 2 directions 1.07-1.08 ms, 1 direction
+// (no stack, twice the recomputation) 1.14-1.17 ms.
 constexpr int kBGThreads = 64;
+constexpr int kBGDirs = 4;  // directions per launch of k_field_beam_grad
 enum DirKind : int32_t { DIR_X = 0, DIR_Y = 1, DIR_DX = 2, DIR_DY = 3, DIR_STEP = 4 };
 
 struct BGArgs {
@@ -313,19 +322,23 @@ struct BGArgs {
   double* model_part;           // [gridDim.x][kND] sums over the block's beams (DIR_STEP)
 };
 
+// ND: directions carried by this launch (the host runs ceil(directions / ND)
+// launches; fewer directions a launch keep the dual numbers small enough for
+// registers, at the cost of recomputing the values once per launch).
+template <int ND>
 __global__ void __launch_bounds__(kBGThreads)
 k_field_beam_grad(const __grid_constant__ DModel M, const __grid_constant__ BGArgs A) {
-  using D = Du<kND>;
-  using X = Cx<kND>;
-  __shared__ double red[kBGThreads][kND];
+  using D = Du<ND>;
+  using X = Cx<ND>;
+  __shared__ double red[kBGThreads][ND];
   const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  double contrib[kND];
+  double contrib[ND];
 #pragma unroll
-  for (int d = 0; d < kND; ++d) contrib[d] = 0.0;
+  for (int d = 0; d < ND; ++d) contrib[d] = 0.0;
   if (b < A.n) {
-    D x = dc_<kND>(A.x[b]), y = dc_<kND>(A.y[b]), dx = dc_<kND>(A.dx[b]), dy = dc_<kND>(A.dy[b]);
+    D x = dc_<ND>(A.x[b]), y = dc_<ND>(A.y[b]), dx = dc_<ND>(A.dx[b]), dy = dc_<ND>(A.dy[b]);
 #pragma unroll
-    for (int d = 0; d < kND; ++d) {
+    for (int d = 0; d < ND; ++d) {
       if (d >= A.n_dir) break;
       if (A.dir_kind[d] == DIR_X) x.d[d] = 1.0;
       if (A.dir_kind[d] == DIR_Y) y.d[d] = 1.0;
@@ -344,21 +357,21 @@ k_field_beam_grad(const __grid_constant__ DModel M, const __grid_constant__ BGAr
     const double th = A.theta ? A.theta[b] : 0.0;
     double sth, cth;
     sincos(th, &sth, &cth);
-    const M2<kND> Q1i{cx_<kND>(cth * cth * qxr + sth * sth * qyr, cth * cth * qxi + sth * sth * qyi),
-                      cx_<kND>(cth * sth * (qxr - qyr), cth * sth * (qxi - qyi)),
-                      cx_<kND>(cth * sth * (qxr - qyr), cth * sth * (qxi - qyi)),
-                      cx_<kND>(sth * sth * qxr + cth * cth * qyr, sth * sth * qxi + cth * cth * qyi)};
+    const M2<ND> Q1i{cx_<ND>(cth * cth * qxr + sth * sth * qyr, cth * cth * qxi + sth * sth * qyi),
+                      cx_<ND>(cth * sth * (qxr - qyr), cth * sth * (qxi - qyi)),
+                      cx_<ND>(cth * sth * (qxr - qyr), cth * sth * (qxi - qyi)),
+                      cx_<ND>(sth * sth * qxr + cth * cth * qyr, sth * sth * qxi + cth * cth * qyi)};
     X Sxx, Syy, Sxy, Lx, Ly, c0;
     D ox, oy;
     X dlp[1];  // d log pref as a complex dual (its derivative parts are used)
-    dlp[0] = cx_<kND>(0.0, 0.0);
+    dlp[0] = cx_<ND>(0.0, 0.0);
     if (A.input_plane) {  // gaussian.py:402-409: s = r1 - r1m, S = Q1^-1, L = 2 theta1m
       Sxx = Q1i.a;
       Syy = Q1i.d;
       Sxy = 0.5 * (Q1i.b + Q1i.c);
-      Lx = cx_<kND>(2.0 * dx0);
-      Ly = cx_<kND>(2.0 * dy0);
-      c0 = cx_<kND>(0.0, 0.0);
+      Lx = cx_<ND>(2.0 * dx0);
+      Ly = cx_<ND>(2.0 * dy0);
+      c0 = cx_<ND>(0.0, 0.0);
       ox = x0;
       oy = y0;
     } else {
@@ -368,14 +381,14 @@ k_field_beam_grad(const __grid_constant__ DModel M, const __grid_constant__ BGAr
 #pragma unroll
       for (int i = 0; i < 5; ++i)
 #pragma unroll
-        for (int j = 0; j < 5; ++j) m[i][j] = dc_<kND>(i == j ? 1.0 : 0.0);
+        for (int j = 0; j < 5; ++j) m[i][j] = dc_<ND>(i == j ? 1.0 : 0.0);
       for (int s = 0; s < M.n; ++s) {
         const DStep& st = M.s[s];
         D a[4];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) a[j] = dc_<kND>(st.a[j]);
+        for (int j = 0; j < 4; ++j) a[j] = dc_<ND>(st.a[j]);
 #pragma unroll
-        for (int d = 0; d < kND; ++d) {
+        for (int d = 0; d < ND; ++d) {
           if (d >= A.n_dir || A.dir_kind[d] != DIR_STEP || A.dir_step[d] != s) continue;
           if (A.dir_a[d] >= 0) {
             a[A.dir_a[d] & 3].d[d] = A.dir_seed[d];
@@ -429,15 +442,15 @@ k_field_beam_grad(const __grid_constant__ DModel M, const __grid_constant__ BGAr
             break;
         }
       }
-      const M2<kND> Am{cx_<kND>(m[0][0]), cx_<kND>(m[0][1]), cx_<kND>(m[1][0]), cx_<kND>(m[1][1])};
-      const M2<kND> Bm{cx_<kND>(m[0][2]), cx_<kND>(m[0][3]), cx_<kND>(m[1][2]), cx_<kND>(m[1][3])};
-      const M2<kND> Cm{cx_<kND>(m[2][0]), cx_<kND>(m[2][1]), cx_<kND>(m[3][0]), cx_<kND>(m[3][1])};
-      const M2<kND> Dm{cx_<kND>(m[2][2]), cx_<kND>(m[2][3]), cx_<kND>(m[3][2]), cx_<kND>(m[3][3])};
+      const M2<ND> Am{cx_<ND>(m[0][0]), cx_<ND>(m[0][1]), cx_<ND>(m[1][0]), cx_<ND>(m[1][1])};
+      const M2<ND> Bm{cx_<ND>(m[0][2]), cx_<ND>(m[0][3]), cx_<ND>(m[1][2]), cx_<ND>(m[1][3])};
+      const M2<ND> Cm{cx_<ND>(m[2][0]), cx_<ND>(m[2][1]), cx_<ND>(m[3][0]), cx_<ND>(m[3][1])};
+      const M2<ND> Dm{cx_<ND>(m[2][2]), cx_<ND>(m[2][3]), cx_<ND>(m[3][2]), cx_<ND>(m[3][3])};
       // Q2^-1 = (A + B Q1^-1)^-1 (C + D Q1^-1)   (gaussian.py:92-96)
-      const M2<kND> denom = Am + Bm * Q1i;
-      const M2<kND> Q2 = inv2(denom) * (Cm + Dm * Q1i);
-      const M2<kND> Binv = nan0(inv2(Bm));
-      const M2<kND> Q1 = nan0(inv2(Q1i));
+      const M2<ND> denom = Am + Bm * Q1i;
+      const M2<ND> Q2 = inv2(denom) * (Cm + Dm * Q1i);
+      const M2<ND> Binv = nan0(inv2(Bm));
+      const M2<ND> Q1 = nan0(inv2(Q1i));
       const D r2mx = m[0][0] * x0 + m[0][1] * y0 + m[0][2] * dx0 + m[0][3] * dy0;
       const D r2my = m[1][0] * x0 + m[1][1] * y0 + m[1][2] * dx0 + m[1][3] * dy0;
       // pref = amp / sqrt(det): d log pref = -d det / (2 det)
@@ -448,33 +461,33 @@ k_field_beam_grad(const __grid_constant__ DModel M, const __grid_constant__ BGAr
         dd.im = det.im;
         dd.re.v = 0.0;  // the quotient below uses only the derivative parts
         dd.im.v = 0.0;
-        const X q = (-0.5) * (dd / cx_<kND>(det.re.v, det.im.v));
+        const X q = (-0.5) * (dd / cx_<ND>(det.re.v, det.im.v));
         dlp[0] = q;
       }
-      const M2<kND> ABinv = Am * Binv;
-      const M2<kND> P = Q1 * inv2(Bm * (Am * Q1 + Bm));
+      const M2<ND> ABinv = Am * Binv;
+      const M2<ND> P = Q1 * inv2(Bm * (Am * Q1 + Bm));
       Sxx = Q2.a;
       Syy = Q2.d;
       Sxy = 0.5 * (Q2.b + Q2.c);
-      const X bx = Binv.a * cx_<kND>(x0) + Binv.c * cx_<kND>(y0), by = Binv.b * cx_<kND>(x0) + Binv.d * cx_<kND>(y0);
-      const X px = P.a * cx_<kND>(r2mx) + P.c * cx_<kND>(r2my), py = P.b * cx_<kND>(r2mx) + P.d * cx_<kND>(r2my);
-      Lx = 2.0 * (cx_<kND>(m[2][4]) - bx + px);
-      Ly = 2.0 * (cx_<kND>(m[3][4]) - by + py);
-      const X q1 = cx_<kND>(x0) * (ABinv.a * cx_<kND>(x0) + ABinv.b * cx_<kND>(y0)) +
-                   cx_<kND>(y0) * (ABinv.c * cx_<kND>(x0) + ABinv.d * cx_<kND>(y0));
-      const X q2 = cx_<kND>(r2mx) * (P.a * cx_<kND>(r2mx) + P.b * cx_<kND>(r2my)) +
-                   cx_<kND>(r2my) * (P.c * cx_<kND>(r2mx) + P.d * cx_<kND>(r2my));
+      const X bx = Binv.a * cx_<ND>(x0) + Binv.c * cx_<ND>(y0), by = Binv.b * cx_<ND>(x0) + Binv.d * cx_<ND>(y0);
+      const X px = P.a * cx_<ND>(r2mx) + P.c * cx_<ND>(r2my), py = P.b * cx_<ND>(r2mx) + P.d * cx_<ND>(r2my);
+      Lx = 2.0 * (cx_<ND>(m[2][4]) - bx + px);
+      Ly = 2.0 * (cx_<ND>(m[3][4]) - by + py);
+      const X q1 = cx_<ND>(x0) * (ABinv.a * cx_<ND>(x0) + ABinv.b * cx_<ND>(y0)) +
+                   cx_<ND>(y0) * (ABinv.c * cx_<ND>(x0) + ABinv.d * cx_<ND>(y0));
+      const X q2 = cx_<ND>(r2mx) * (P.a * cx_<ND>(r2mx) + P.b * cx_<ND>(r2my)) +
+                   cx_<ND>(r2my) * (P.c * cx_<ND>(r2mx) + P.d * cx_<ND>(r2my));
       c0 = q1 - q2;
       ox = m[0][4];
       oy = m[1][4];
     }
     // the polynomial in (row, col): s = s0 + row u + col v
-    const D s0x = dc_<kND>(A.pm.t[5]) - ox, s0y = dc_<kND>(A.pm.t[2]) - oy;
+    const D s0x = dc_<ND>(A.pm.t[5]) - ox, s0y = dc_<ND>(A.pm.t[2]) - oy;
     const double ux = A.pm.t[3], uy = A.pm.t[0], vx = A.pm.t[4], vy = A.pm.t[1];
     auto quad = [&](const D& ax, const D& ay, const D& bx2, const D& by2) -> X {  // a^T S b
       return (ax * bx2) * Sxx + (ay * by2) * Syy + (ax * by2 + ay * bx2) * Sxy;
     };
-    const D U0 = dc_<kND>(ux), U1 = dc_<kND>(uy), V0 = dc_<kND>(vx), V1 = dc_<kND>(vy);
+    const D U0 = dc_<ND>(ux), U1 = dc_<ND>(uy), V0 = dc_<ND>(vx), V1 = dc_<ND>(vy);
     X kap[6];  // cc, rr, rc, c, r, 0
     kap[0] = hk * quad(V0, V1, V0, V1);
     kap[1] = hk * quad(U0, U1, U0, U1);
@@ -506,7 +519,7 @@ k_field_beam_grad(const __grid_constant__ DModel M, const __grid_constant__ BGAr
     }
     // dL/dp = Re(i sum_j dkap_j w_j + dlogpref w_1) = -sum_j Im(dkap_j w_j) + Re(dlogpref w_1)
 #pragma unroll
-    for (int d = 0; d < kND; ++d) {
+    for (int d = 0; d < ND; ++d) {
       if (d >= A.n_dir) break;
       double g = 0.0;
       for (int j = 0; j < 6; ++j) g -= kap[j].re.d[d] * wi[j] + kap[j].im.d[d] * wr[j];
@@ -526,15 +539,15 @@ k_field_beam_grad(const __grid_constant__ DModel M, const __grid_constant__ BGAr
   }
   // the block's sums of the model directions, in a fixed order
 #pragma unroll
-  for (int d = 0; d < kND; ++d) red[threadIdx.x][d] = (d < A.n_dir && A.dir_kind[d] == DIR_STEP) ? contrib[d] : 0.0;
+  for (int d = 0; d < ND; ++d) red[threadIdx.x][d] = (d < A.n_dir && A.dir_kind[d] == DIR_STEP) ? contrib[d] : 0.0;
   __syncthreads();
   for (int s = kBGThreads / 2; s > 0; s >>= 1) {
     if ((int)threadIdx.x < s)
 #pragma unroll
-      for (int d = 0; d < kND; ++d) red[threadIdx.x][d] += red[threadIdx.x + s][d];
+      for (int d = 0; d < ND; ++d) red[threadIdx.x][d] += red[threadIdx.x + s][d];
     __syncthreads();
   }
-  if (threadIdx.x < kND && A.model_part) A.model_part[(size_t)blockIdx.x * kND + threadIdx.x] = red[0][threadIdx.x];
+  if (threadIdx.x < ND && A.model_part) A.model_part[(size_t)blockIdx.x * kND + threadIdx.x] = red[0][threadIdx.x];
 }
 
 // raw[target[d]] = sum over blocks (in order) of the group's per-block sums
@@ -651,50 +664,48 @@ __global__ void __launch_bounds__(128) k_adj_uplanes(const BeamFast* __restrict_
   }
 }
 
-// mom[b] from X: one thread per beam walks the rows with the row factor
-// V_b(r) (exact fixed-point phase, as the forward's V operand), float32 sums
-// over 16 rows added in float64.
+// Moment partials from X: one thread per (beam, group of kAdjRows rows) walks
+// its rows with the row factor V_b(r) (exact fixed-point phase from the
+// group's first row, as the forward's V operand), float32 sums written as
+// the partial of its row group; k_field_moment_sum adds the groups in order.
+constexpr int kAdjRows = 32;
+
 __global__ void __launch_bounds__(128) k_adj_sep_moments(const BeamFast* __restrict__ beams, int64_t n,
                                                          const float2* __restrict__ x, int h, int64_t bpad,
-                                                         double* __restrict__ mom) {
+                                                         float* __restrict__ part) {
   const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= n) return;
+  const int r0 = (int)blockIdx.y * kAdjRows, r1 = min(h, r0 + kAdjRows);
   const BeamFast& B = beams[b];
-  const uint64_t p2 = B.p_rr, p1 = B.p_r, p0 = B.p_0;
-  uint64_t th = p0, dth = p2 + p1;
+  const uint64_t p2 = B.p_rr, p1 = B.p_r, u0 = (uint64_t)r0;
+  uint64_t th = p2 * (u0 * u0) + p1 * u0 + B.p_0;
+  uint64_t dth = p2 * (2 * u0 + 1) + p1;
   const uint64_t ddth = 2 * p2;
   const int64_t ld = 3 * bpad;
-  double acc[12];
+  float s[12];
 #pragma unroll
-  for (int i = 0; i < 12; ++i) acc[i] = 0.0;
-  for (int r0 = 0; r0 < h; r0 += 16) {
-    float s[12];
-#pragma unroll
-    for (int i = 0; i < 12; ++i) s[i] = 0.f;
-    const int r1 = min(h, r0 + 16);
-    for (int r = r0; r < r1; ++r) {
-      const float2 v = sep_operand(B.e0, B.b_rr, B.l_r, B.r0, r, th);
-      th += dth;
-      dth += ddth;
-      const float dr = (float)r - B.r0;
-      const float2* xr = x + (size_t)r * ld + b;
-      const float2 x0 = xr[0], x1 = xr[bpad], x2 = xr[2 * bpad];
-      const float p0r = v.x * x0.x - v.y * x0.y, p0i = v.x * x0.y + v.y * x0.x;
-      const float p1r = v.x * x1.x - v.y * x1.y, p1i = v.x * x1.y + v.y * x1.x;
-      const float p2r = v.x * x2.x - v.y * x2.y, p2i = v.x * x2.y + v.y * x2.x;
-      s[0] += p0r; s[1] += p0i;                                // 1
-      s[2] += p1r; s[3] += p1i;                                // dc
-      s[4] = fmaf(dr, p0r, s[4]); s[5] = fmaf(dr, p0i, s[5]);  // dr
-      s[6] += p2r; s[7] += p2i;                                // dc^2
-      s[8] = fmaf(dr, p1r, s[8]); s[9] = fmaf(dr, p1i, s[9]);  // dr dc
-      const float dr2 = dr * dr;
-      s[10] = fmaf(dr2, p0r, s[10]); s[11] = fmaf(dr2, p0i, s[11]);  // dr^2
-    }
-#pragma unroll
-    for (int i = 0; i < 12; ++i) acc[i] += (double)s[i];
+  for (int i = 0; i < 12; ++i) s[i] = 0.f;
+  for (int r = r0; r < r1; ++r) {
+    const float2 v = sep_operand(B.e0, B.b_rr, B.l_r, B.r0, r, th);
+    th += dth;
+    dth += ddth;
+    const float dr = (float)r - B.r0;
+    const float2* xr = x + (size_t)r * ld + b;
+    const float2 x0 = xr[0], x1 = xr[bpad], x2 = xr[2 * bpad];
+    const float p0r = v.x * x0.x - v.y * x0.y, p0i = v.x * x0.y + v.y * x0.x;
+    const float p1r = v.x * x1.x - v.y * x1.y, p1i = v.x * x1.y + v.y * x1.x;
+    const float p2r = v.x * x2.x - v.y * x2.y, p2i = v.x * x2.y + v.y * x2.x;
+    s[0] += p0r; s[1] += p0i;                                // 1
+    s[2] += p1r; s[3] += p1i;                                // dc
+    s[4] = fmaf(dr, p0r, s[4]); s[5] = fmaf(dr, p0i, s[5]);  // dr
+    s[6] += p2r; s[7] += p2i;                                // dc^2
+    s[8] = fmaf(dr, p1r, s[8]); s[9] = fmaf(dr, p1i, s[9]);  // dr dc
+    const float dr2 = dr * dr;
+    s[10] = fmaf(dr2, p0r, s[10]); s[11] = fmaf(dr2, p0i, s[11]);  // dr^2
   }
+  float* dst = part + ((size_t)blockIdx.y * n + b) * 12;
 #pragma unroll
-  for (int i = 0; i < 12; ++i) mom[b * 12 + i] = acc[i];
+  for (int i = 0; i < 12; ++i) dst[i] = s[i];
 }
 
 // ------------------------------------------------------------ host
@@ -727,7 +738,12 @@ static AdjLayout adj_layout(int64_t n, int h, int w, int method = TG_FIELD_DIREC
   if (L.bg_blocks < 1) L.bg_blocks = 1;
   size_t off = 0;
   L.rec = off; off = al256a(off + field_records_bytes(n));
-  L.part = off; off = al256a(off + (size_t)L.col_chunks * L.row_splits * n * 12 * sizeof(float));
+  size_t nparts = (size_t)L.col_chunks * L.row_splits;
+  if (method == TG_FIELD_SEPARABLE) {  // the row groups of k_adj_sep_moments
+    const size_t rg = (size_t)(h + kAdjRows - 1) / kAdjRows;
+    if (rg > nparts) nparts = rg;
+  }
+  L.part = off; off = al256a(off + nparts * n * 12 * sizeof(float));
   L.mom = off; off = al256a(off + (size_t)n * 12 * sizeof(double));
   L.model = off; off = al256a(off + (size_t)L.bg_blocks * kND * sizeof(double));
   if (method == TG_FIELD_SEPARABLE) {
@@ -823,7 +839,10 @@ static int field_vjp_impl(const tg_model* model, const tg_beams* beams, const tg
     int st2 = launch_field_gemm(gp, up, L.rows_pad, (int)(3 * L.bpad), L.cols_pad, 1, pm->h, (int)(3 * L.bpad),
                                 xp, s);
     if (st2 != TG_OK) return st2;
-    k_adj_sep_moments<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(MA.beams, n, xp, pm->h, L.bpad, mom);
+    const int rgroups = (pm->h + kAdjRows - 1) / kAdjRows;
+    k_adj_sep_moments<<<dim3((unsigned)((n + 127) / 128), (unsigned)rgroups), 128, 0, s>>>(
+        MA.beams, n, xp, pm->h, L.bpad, MA.part);
+    k_field_moment_sum<<<(int)((n * 12 + 255) / 256), 256, 0, s>>>(MA.part, rgroups, n, mom);
   } else {
     k_field_moments<<<dim3(L.col_chunks * L.row_splits, L.beam_chunks), kMThreads, 0, s>>>(MA);
     k_field_moment_sum<<<(int)((n * 12 + 255) / 256), 256, 0, s>>>(MA.part, L.col_chunks * L.row_splits, n, mom);
@@ -856,7 +875,7 @@ static int field_vjp_impl(const tg_model* model, const tg_beams* beams, const tg
     }
   }
   double* mpart = reinterpret_cast<double*>(ws + L.model);
-  const int groups = dirs.empty() ? 1 : (int)((dirs.size() + kND - 1) / kND);
+  const int groups = dirs.empty() ? 1 : (int)((dirs.size() + kBGDirs - 1) / kBGDirs);
   for (int gidx = 0; gidx < groups; ++gidx) {
     BGArgs B;
     std::memset(&B, 0, sizeof(B));
@@ -879,7 +898,11 @@ static int field_vjp_impl(const tg_model* model, const tg_beams* beams, const tg
     std::memset(&S, 0, sizeof(S));
     bool any_model = false;
     for (int d = 0; d < kND; ++d) {
-      const size_t i = (size_t)gidx * kND + d;
+      const size_t i = (size_t)gidx * kBGDirs + d;
+      if (d >= kBGDirs) {
+        S.target[d] = -1;
+        continue;
+      }
       S.target[d] = -1;
       if (i >= dirs.size()) continue;
       B.n_dir = d + 1;
@@ -890,13 +913,15 @@ static int field_vjp_impl(const tg_model* model, const tg_beams* beams, const tg
       S.target[d] = dirs[i].target;
       if (dirs[i].kind == DIR_STEP) any_model = true;
     }
+    // every launch writes the ray directions it carries; the pathlength and
+    // amplitude gradients need no direction and come from the first
+    B.gx = out->x; B.gy = out->y; B.gdx = out->dx; B.gdy = out->dy;
     if (gidx == 0) {
-      B.gx = out->x; B.gy = out->y; B.gdx = out->dx; B.gdy = out->dy;
       B.gpl = out->pathlength;
       B.gamp = out->amplitude;
     }
     B.model_part = mpart;
-    k_field_beam_grad<<<L.bg_blocks, kBGThreads, 0, s>>>(dm, B);
+    k_field_beam_grad<kBGDirs><<<L.bg_blocks, kBGThreads, 0, s>>>(dm, B);
     if (any_model && out->raw) {
       S.n_dir = B.n_dir;
       S.blocks = L.bg_blocks;
