@@ -239,13 +239,19 @@ __device__ __forceinline__ void batch_tile(const BatchIO& io, const BModel& M, c
       uint32_t spos = 0u, sneg = 0u;  // NB < 0: bit b set when sign(x) > 0 / < 0
       bool alive = true;
       // row . u over the signs decided so far (rows hold 0 for later ones)
+      // rows are 16-byte aligned and padded to a multiple of 4 floats: the
+      // constant and the first three sign coefficients come in one vector
       auto dot = [&](const float* row, int nbs) {
         const float4 r = *reinterpret_cast<const float4*>(row);
-        float acc = fmaf(r.w, v[3], fmaf(r.z, v[2], fmaf(r.y, v[1], fmaf(r.x, v[0], row[4]))));
+        const float4 r2 = *reinterpret_cast<const float4*>(row + 4);  // const, s_0, s_1, s_2
+        float acc = fmaf(r.w, v[3], fmaf(r.z, v[2], fmaf(r.y, v[1], fmaf(r.x, v[0], r2.x))));
         if (NB >= 0) {
 #pragma unroll
           for (int b = 0; b < NS; ++b)
-            if (b < NB) acc = fmaf(row[5 + b], sg[b], acc);
+            if (b < NB) {
+              const float cb = b == 0 ? r2.y : (b == 1 ? r2.z : (b == 2 ? r2.w : row[5 + b]));
+              acc = fmaf(cb, sg[b], acc);
+            }
         } else {
           for (int b = 0; b < nbs; ++b) acc = fmaf(row[5 + b], sign_of(spos, sneg, b), acc);
         }
@@ -306,7 +312,8 @@ __device__ __forceinline__ void batch_tile(const BatchIO& io, const BModel& M, c
         a0 = fmaf(cb.x, s, a0); a1 = fmaf(cb.y, s, a1); a2 = fmaf(cb.z, s, a2); a3 = fmaf(cb.w, s, a3);
         const float* lb = srec + L.l + 8 * b;
         const float4 l4 = *reinterpret_cast<const float4*>(lb);
-        float lin = fmaf(l4.x, v[0], fmaf(l4.y, v[1], fmaf(l4.z, v[2], fmaf(l4.w, v[3], lb[4]))));
+        const float l5 = reinterpret_cast<const float4*>(lb)[1].x;
+        float lin = fmaf(l4.x, v[0], fmaf(l4.y, v[1], fmaf(l4.z, v[2], fmaf(l4.w, v[3], l5))));
         const float* kb = srec + L.k + b * nb - (b * (b - 1)) / 2;  // K_bb' for b' >= b
         if (NB >= 0) {
 #pragma unroll
