@@ -199,3 +199,20 @@ def test_separable_moments_on_tensor_cores_match_direct(cuda, full):
         u, v = real(a[k]), real(b[k])
         assert normwise_err(u, v) <= 1e-4, (k, normwise_err(u, v))
     assert t._native.error_word() == 0
+
+
+def test_separable_adjoint_flags_astigmatic_beams(cuda):
+    """The tensor-core moments assume separable beams; given astigmatic ones
+    the call reports TG_EW_NONSEPARABLE in the error word (as the separable
+    forward does)."""
+    import temgymcore_gb300 as t
+    from temgymcore_gb300.workloads import beamlet_field, build_model, gaussian_rays
+    w = beamlet_field(seed=2, n_beams=64, det_shape=(32, 40), det_px=3e-5, astigmatic=True)
+    plan = t.FieldPlan(gaussian_rays(w["rays"]), build_model(w["model"]))
+    assert not plan.separable
+    t._native.error_word()
+    T = torch.ones(plan.shape, dtype=torch.complex64, device=cuda)
+    plan.vjp(T, method="separable")
+    assert t._native.error_word() & 0x10
+    plan.vjp(T)  # the plan's own (direct) method
+    assert t._native.error_word() == 0

@@ -79,6 +79,16 @@ def test_trace_image_one_pixel_many_carries(cuda):
     assert int(ref.max()) == n
 
 
+@pytest.mark.parametrize("shape", [(64, 64), (300, 300)])
+def test_trace_image_aligned_int32_prefilled(cuda, shape):
+    # the four-rays-per-thread kernels with an int32 histogram (the
+    # prefetching shared-memory variant at 64 x 64; 300 x 300 leaves no room
+    # for the prefetch slots), counts added to a prefilled histogram
+    n = (1 << 22) + 5
+    h_sh, h_gl, ref = _run(n, shape, spread=0.08 * shape[0] / 64, dtype=torch.int32, prefill=3)
+    assert np.array_equal(h_sh, ref) and np.array_equal(h_gl, ref)
+
+
 @pytest.mark.parametrize("dtype", [torch.int32, torch.int64])
 def test_trace_image_unaligned_and_prefilled(cuda, dtype):
     n = (1 << 21) + 1
