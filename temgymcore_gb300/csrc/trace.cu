@@ -261,9 +261,10 @@ __device__ __forceinline__ void fwd_rays(const Program& P, const FwdArgs& A, con
 
 // kPf (shared-histogram variant, R = 4): each thread prefetches its next
 // four rays (x, y, dx, dy: four 16-byte cp.async) into its own 64-byte slot of
-// shared memory as soon as the chain has consumed the current ones, so the
-// loads run under the stores, the binning and the histogram atomics.  The
-// slots take kPfBytes ahead of the histogram words.
+// shared memory as soon as the current ones' coordinates are stored (every
+// value read from the slot has then been used), so the loads run under the
+// pathlength, the binning and the histogram atomics.  The slots take
+// kPfBytes ahead of the histogram words.
 constexpr int kPfBytes = 4 * kShThreads * 16;  // 64 KB
 
 template <int R, typename CountT, bool kSh = false, bool kPf = false>
@@ -315,7 +316,7 @@ k_trace_fwd(const __grid_constant__ Program P, const __grid_constant__ FwdArgs A
       load4<R>(A.dy, i0, n, dy, vec);
     }
     const int64_t ni0 = i0 + stride;
-    // the slot is free once the chain has used the values read from it
+    // the slot is free once the values read from it have been used
     auto next = [&]() {
       if (kPf) {
         if (ni0 + 3 < n) prefetch(ni0);
