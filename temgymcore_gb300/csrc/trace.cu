@@ -40,11 +40,12 @@ struct FwdArgs {
 // Shared-histogram variant of the forward kernel: each CTA (kShThreads
 // threads, one per SM) keeps the whole detector in shared memory as uint16
 // counters packed in pairs and adds each hit with one shared atomic.  A hit
-// that brings its counter to 32768 moves those 32768 counts into the caller's
-// histogram (one global atomic, rare: only pixels with more than 32767 hits
-// on one SM) and takes them off the counter, so no counter reaches 65536 (a
-// CTA has at most a few thousand hits in flight when the subtraction lands)
-// and no periodic flush is needed: at the end the CTA writes its packed
+// that brings its counter to 16384 moves those 16384 counts into the caller's
+// histogram (one global atomic, rare: only pixels with more than 16383 hits
+// on one SM) and takes them off the counter, so no counter reaches 65536
+// (that would take 49152 more hits on the pixel before the subtraction lands;
+// a CTA has at most a few thousand in flight) and no periodic flush is
+// needed: at the end the CTA writes its packed
 // counters once to its own row of the workspace, and k_hist_rows adds the
 // rows into the histogram.  Global atomics (even warp-aggregated) then no
 // longer bound the fused pass: measured at 16.8 M rays, 256x256 spread 0.193
@@ -61,12 +62,12 @@ __device__ __forceinline__ void hist_add_sh(uint32_t* shw, int bin, bool valid, 
   if (valid) {
     const uint32_t sh = 16u * (uint32_t)(bin & 1);
     const uint32_t old = atomicAdd(shw + (bin >> 1), 1u << sh);
-    if (((old >> sh) & 0xffffu) == 0x7fffu) {  // this hit made the count 32768
-      atomicSub(shw + (bin >> 1), 0x8000u << sh);
+    if (((old >> sh) & 0xffffu) == 0x3fffu) {  // this hit made the count 16384
+      atomicSub(shw + (bin >> 1), 0x4000u << sh);
       if constexpr (sizeof(CountT) == 8)
-        atomicAdd(reinterpret_cast<unsigned long long*>(hist) + bin, 32768ull);
+        atomicAdd(reinterpret_cast<unsigned long long*>(hist) + bin, 16384ull);
       else
-        atomicAdd(reinterpret_cast<unsigned int*>(hist) + bin, 32768u);
+        atomicAdd(reinterpret_cast<unsigned int*>(hist) + bin, 16384u);
     }
   }
 }

@@ -71,7 +71,7 @@ def test_trace_image_spread(cuda, shape):
 
 def test_trace_image_one_pixel_many_carries(cuda):
     # every ray in the centre pixel: 10M rays over the SMs, about 66k hits per
-    # CTA on one uint16 counter, which moves 32768 counts into the histogram
+    # CTA on one uint16 counter, which moves 16384 counts into the histogram
     # each time it reaches that value
     n = 10_000_000
     h_sh, h_gl, ref = _run(n, (32, 32), spread=0.0)
@@ -131,7 +131,7 @@ def test_into_image_pixel_indices(cuda, idt):
 @pytest.mark.parametrize("hdt", [torch.int32, torch.int64])
 def test_hist_pixels_carry_on_one_word(cuda, hdt):
     """Every hit on the two pixels that share one packed shared-memory word:
-    each CTA drives both uint16 halves past 32768 twice (the carry
+    each CTA drives both uint16 halves past 16384 four times (the carry
     into the histogram must leave the neighbouring half intact), on top of
     prefilled counts; the remaining hits stay in the per-CTA rows."""
     import temgymcore_gb300 as t
