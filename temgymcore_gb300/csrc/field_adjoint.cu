@@ -602,15 +602,19 @@ __global__ void k_adj_gplanes(const float2* __restrict__ g, int h, int w, int ro
 // U_b(c) dc^a as four bf16 planes [3 * bpad][cols_pad]: one thread per (beam,
 // block of 16 columns), the column factor of the separable forward (exact
 // fixed-point phase stepped by 64-bit differences), three powers of dc, 32
-// bytes per plane and power stored as two 16-byte vectors.
+// bytes per plane and power stored as two 16-byte vectors.  Consecutive
+// threads take consecutive column blocks of one beam, so a warp's store is one
+// contiguous run of a plane row.
 constexpr int kAdjCols = 16;
 
 __global__ void __launch_bounds__(128) k_adj_uplanes(const BeamFast* __restrict__ beams, int64_t n,
                                                      int64_t bpad, int w, int cols_pad,
                                                      __nv_bfloat16_raw* __restrict__ planes) {
-  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= bpad) return;
-  const int c0 = (int)blockIdx.y * kAdjCols;
+  const int cblocks = cols_pad / kAdjCols;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= bpad * cblocks) return;
+  const int64_t b = t / cblocks;
+  const int c0 = (int)(t % cblocks) * kAdjCols;
   const int64_t plane = 3 * bpad * (int64_t)cols_pad;
   const bool live = b < n;
   uint64_t p2 = 0, p1 = 0;
@@ -833,8 +837,8 @@ static int field_vjp_impl(const tg_model* model, const tg_beams* beams, const tg
     float2* xp = reinterpret_cast<float2*>(ws + L.xprod);
     const int64_t gtot = (int64_t)L.rows_pad * L.cols_pad;
     k_adj_gplanes<<<(unsigned)((gtot + 255) / 256), 256, 0, s>>>(MA.g, pm->h, pm->w, L.rows_pad, L.cols_pad, gp);
-    k_adj_uplanes<<<dim3((unsigned)((L.bpad + 127) / 128), (unsigned)(L.cols_pad / kAdjCols)), 128, 0, s>>>(
-        MA.beams, n, L.bpad, pm->w, L.cols_pad, up);
+    const int64_t uthreads = L.bpad * (L.cols_pad / kAdjCols);
+    k_adj_uplanes<<<(unsigned)((uthreads + 127) / 128), 128, 0, s>>>(MA.beams, n, L.bpad, pm->w, L.cols_pad, up);
     if (3 * L.bpad > INT32_MAX) return TG_ERR_TOO_LARGE;
     int st2 = launch_field_gemm(gp, up, L.rows_pad, (int)(3 * L.bpad), L.cols_pad, 1, pm->h, (int)(3 * L.bpad),
                                 xp, s);
