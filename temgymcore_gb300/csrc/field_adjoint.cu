@@ -98,13 +98,20 @@ __global__ void __launch_bounds__(kMThreads, 3) k_field_moments(const __grid_con
       for (int i = 0; i < 12; ++i) s[i] = 0.f;
       if (col0 < A.w) {
         const BeamFast B = A.beams[b0 + k];
+        // exact phase at the strip start of the band's first row, its step to
+        // the next row (and that step's own step), and the column step
+        const uint64_t ub = (uint64_t)band;
+        uint64_t th_row = B.p_cc * ucol2 + B.p_rr * (ub * ub) + B.p_rc * (ub * ucol) + B.p_c * ucol +
+                          B.p_r * ub + B.p_0;
+        uint64_t dth_row = B.p_rr * (2 * ub + 1) + B.p_rc * ucol + B.p_r;
+        uint64_t dth_col = B.p_cc * ustep + B.p_rc * ub + B.p_c;
         for (int rr = 0; rr < kMRows; ++rr) {
           const int row = band + rr;
           if (row >= r_end) break;
-          const uint64_t urow = (uint64_t)row;
-          uint64_t th = B.p_cc * ucol2 + B.p_rr * (urow * urow) + B.p_rc * (urow * ucol) + B.p_c * ucol +
-                        B.p_r * urow + B.p_0;
-          uint64_t dth = B.p_cc * ustep + B.p_rc * urow + B.p_c;
+          uint64_t th = th_row, dth = dth_col;
+          th_row += dth_row;
+          dth_row += 2 * B.p_rr;
+          dth_col += B.p_rc;
           const float dr = (float)row - B.r0, dc = (float)col0 - B.c0;
           const float la = B.e0 - (B.b_cc * dc * dc + B.b_rr * dr * dr + B.b_rc * dr * dc + B.l_c * dc + B.l_r * dr);
           const float dla = -(B.b_cc * (2.f * dc + 1.f) + B.b_rc * dr + B.l_c);
@@ -115,15 +122,17 @@ __global__ void __launch_bounds__(kMThreads, 3) k_field_moments(const __grid_con
           jv = fminf(fmaxf(jv, 0.f), jl);
           const float la_max = fmaxf(fmaxf(la, la_end), la + jv * dla - B.b_cc * jv * (jv - 1.f));
           if (!(la_max > kMSkipLog)) continue;
-          float s0r = 0.f, s0i = 0.f, s1r = 0.f, s1i = 0.f, s2r = 0.f, s2i = 0.f;
+          // sums of conj(G) E times 1, j and j^2 over the strip (j the column
+          // within it, a compile-time constant), shifted to the moments about
+          // the centre, c = dc + j, once per strip
+          float s0r = 0.f, s0i = 0.f, t1r = 0.f, t1i = 0.f, t2r = 0.f, t2i = 0.f;
           auto add = [&](int j, float2 z) {  // conj(G) E at column col0 + j
             if (col0 + j < A.w) {
               const float2 g = sg[rr][j][lane];
               const float pr = g.x * z.x + g.y * z.y, pi = g.x * z.y - g.y * z.x;
-              const float c = dc + (float)j;
               s0r += pr; s0i += pi;
-              s1r = fmaf(c, pr, s1r); s1i = fmaf(c, pi, s1i);
-              s2r = fmaf(c * c, pr, s2r); s2i = fmaf(c * c, pi, s2i);
+              t1r = fmaf((float)j, pr, t1r); t1i = fmaf((float)j, pi, t1i);
+              t2r = fmaf((float)(j * j), pr, t2r); t2i = fmaf((float)(j * j), pi, t2i);
             }
           };
           if (la > -kMRecurMax && fabsf(dla) < kMRecurMax && fabsf(dla_end) < kMRecurMax) {
@@ -145,6 +154,8 @@ __global__ void __launch_bounds__(kMThreads, 3) k_field_moments(const __grid_con
               dth += ddth;
             }
           }
+          const float s1r = fmaf(dc, s0r, t1r), s1i = fmaf(dc, s0i, t1i);
+          const float s2r = fmaf(dc, fmaf(dc, s0r, 2.f * t1r), t2r), s2i = fmaf(dc, fmaf(dc, s0i, 2.f * t1i), t2i);
           // moments about the centre: 1, dc, dr, dc^2, dr dc, dr^2
           s[0] += s0r; s[1] += s0i;
           s[2] += s1r; s[3] += s1i;
