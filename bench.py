@@ -825,8 +825,10 @@ def secondary_transfer(torch, dev, hbm):
             "ms": ms, "ray_planes_per_s": n * m / (ms * 1e-3),
             "achieved_gbs": (out_bytes + n * 40) / (ms * 1e-3) / 1e9,
             "frac_of_hbm": (out_bytes + n * 40) / (ms * 1e-3) / 1e9 / hbm,
-            "fp64_tflops": n * m * 50 / (ms * 1e-3) / 1e12,
-            "note": "25 float64 FMAs per (ray, plane): float64-pipe bound on GB300"}
+            "f64_equivalent_tflops": n * m * 50 / (ms * 1e-3) / 1e12,
+            "note": "25 multiply-adds per (ray, plane) carried in double-float (float32 pairs, "
+                    "k_transfer_rays_df): issue-bound on the float32 arithmetic; the float64 "
+                    "kernel takes only entries outside the double-float range"}
 
 
 def secondary_aberrated_scan(torch, dev, hbm):
