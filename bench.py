@@ -55,6 +55,24 @@ def _peaks():
         return FALLBACK_HBM_GBS, 1900.0, "fallback"
 
 
+def _fp32_roofline(torch, ms, pairs):
+    """The fast direct field against the FP32 issue rate: the strip recurrence
+    costs 10 FP32 instructions per (beam, pixel) (z <- z w and w <- w rho: two
+    FMUL + two FFMA each; two FADD into the sums); the peak is 128 FP32 lanes
+    per SM at the measured maximum SM clock."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            mhz, src = float(json.load(fh)["sm_max_mhz"]), "measured max SM clock"
+    except Exception:
+        mhz, src = 2070.0, "nominal max SM clock"
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    achieved = 10 * pairs / (ms * 1e-3) / 1e12
+    peak = sms * 128 * mhz * 1e6 / 1e12
+    return {"bound": "fp32", "instr_per_beam_px": 10, "achieved": achieved, "peak": peak,
+            "unit": "T FP32 lane-instructions/s", "frac": achieved / peak,
+            "peak_source": f"{sms} SMs x 128 FP32 lanes x {mhz:.0f} MHz ({src})"}
+
+
 def _traffic(name):
     """Per-launch DRAM bytes of a kernel from the committed ncu summary."""
     try:
@@ -455,7 +473,8 @@ def secondary_field(torch, dev, hbm, bf16):
                              "useful_complex_tflops": 8 * pairs / (ms_sep * 1e-3) / 1e12,
                              "frac_of_bf16_peak": gemm_flops / (ms_sep * 1e-3) / 1e12 / bf16,
                              "note": "includes operand generation and split-K reduction"}
-    res["direct_fast"] = {"ms": ms_dir, "beam_px_per_s": pairs / (ms_dir * 1e-3)}
+    res["direct_fast"] = {"ms": ms_dir, "beam_px_per_s": pairs / (ms_dir * 1e-3),
+                          "roofline": _fp32_roofline(torch, ms_dir, pairs)}
     res["direct_fp64"] = {"ms": ms_f64, "beam_px_per_s": pairs / (ms_f64 * 1e-3)}
     res["speedup_separable_vs_fp64"] = ms_f64 / ms_sep
     res["prep_plan_ms"] = ms_prep
@@ -478,7 +497,8 @@ def secondary_field(torch, dev, hbm, bf16):
     wa = beamlet_field(seed=0, astigmatic=True)
     pa = t.FieldPlan(gaussian_rays(wa["rays"]), build_model(wa["model"]))
     ms_a = _time(torch, lambda: pa.evaluate("direct"), 3)
-    res["astigmatic_direct"] = {"ms": ms_a, "beam_px_per_s": pairs / (ms_a * 1e-3), "separable": pa.separable}
+    res["astigmatic_direct"] = {"ms": ms_a, "beam_px_per_s": pairs / (ms_a * 1e-3), "separable": pa.separable,
+                                "roofline": _fp32_roofline(torch, ms_a, pairs)}
     # CPU baseline and the errors against the float64 oracle at a pixel sample
     import oracle.field as of
     idx = _pixel_sample((512, 512))

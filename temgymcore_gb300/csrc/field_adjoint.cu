@@ -22,10 +22,11 @@
 //      the forward's k_field_gemm, k_adj_sep_moments; see below);
 //   2. k_field_moment_sum: the per-block partials summed in a fixed order;
 //   3. k_field_beam_grad<4>: per beam, the preparation arithmetic again in
-//      float64 forward mode (dual numbers carrying 4 directions a launch, as
-//      many launches as there are directions: the central ray's x, y, dx, dy
-//      and the model's step parameters) for d kap / dp and d log pref / dp,
-//      contracted with the moments;
+//      float64 forward mode (dual numbers carrying 4 directions a thread; the
+//      direction groups of a launch on blockIdx.y, up to 32 directions a
+//      launch: the central ray's x, y, dx, dy and the model's step
+//      parameters) for d kap / dp and d log pref / dp, contracted with the
+//      moments;
 //   4. k_field_model_sum: the model parameters' per-block sums in a fixed
 //      order, written as per-step sums in the layout of tg_trace_vjp.
 // Every reduction runs in a fixed order, so the gradients are deterministic.
@@ -302,13 +303,16 @@ __device__ __forceinline__ M2<N> nan0(const M2<N>& m) {
 }
 
 // ------------------------------------------------------------ beam gradient
-constexpr int kND = 8;               // directions per launch
-// Four directions a launch, 64 threads a block.  Measured on the separable
-// 16,384-beam adjoint (whole call): 8 directions (14 KB of stack a thread)
-// 1.40 ms, 4 directions 0.99 ms, 2 directions 1.07-1.08 ms, 1 direction
-// (no stack, twice the recomputation) 1.14-1.17 ms.
+// Four directions a thread, 64 threads a block.  Measured on the separable
+// 16,384-beam adjoint (whole call), one launch per direction group: 8
+// directions a thread (14 KB of stack) 1.40 ms, 4 directions 0.99 ms, 2
+// directions 1.07-1.08 ms, 1 direction (no stack, twice the recomputation)
+// 1.14-1.17 ms.  All groups in one launch (blockIdx.y): 0.932 -> 0.898 ms
+// with 4 directions a thread (2: 0.959, 1: 0.940); the kernel takes 255
+// registers, so an SM holds 8 of its warps and 16,384 beams fill ~7.
 constexpr int kBGThreads = 64;
-constexpr int kBGDirs = 4;  // directions per launch of k_field_beam_grad
+constexpr int kBGDirs = 4;          // directions a thread carries
+constexpr int kBGLaunchDirs = 32;   // directions a launch carries (groups on blockIdx.y)
 enum DirKind : int32_t { DIR_X = 0, DIR_Y = 1, DIR_DX = 2, DIR_DY = 3, DIR_STEP = 4 };
 
 struct BGArgs {
@@ -324,18 +328,18 @@ struct BGArgs {
   const BeamFast* rec;  // unit-amplitude records: the envelope centres
   const double* mom;    // [n][12] moments about the centres
   int32_t input_plane;
-  int32_t n_dir;
-  int32_t dir_kind[kND], dir_step[kND], dir_a[kND];  // dir_a: the step's a[] entry, -1 = rotation angle
-  double dir_seed[kND];                              // d a[dir_a] / d parameter
+  int32_t n_dir;  // directions of this launch: group blockIdx.y takes [ND y, ND y + ND)
+  int32_t dir_kind[kBGLaunchDirs], dir_step[kBGLaunchDirs], dir_a[kBGLaunchDirs];  // dir_a: a[] entry, -1 = angle
+  double dir_seed[kBGLaunchDirs];                                                 // d a[dir_a] / d parameter
   double *gx, *gy, *gdx, *gdy;  // per beam, for DIR_X .. DIR_DY directions (may be NULL)
   double* gpl;                  // per beam d L / d pathlength (may be NULL)
   float* gamp;                  // per beam complex64 gradient of the amplitude (may be NULL)
-  double* model_part;           // [gridDim.x][kND] sums over the block's beams (DIR_STEP)
+  double* model_part;           // [direction][gridDim.x] sums over the block's beams (DIR_STEP)
 };
 
-// ND: directions carried by this launch (the host runs ceil(directions / ND)
-// launches; fewer directions a launch keep the dual numbers small enough for
-// registers, at the cost of recomputing the values once per launch).
+// ND: directions carried by a thread; the launch's direction groups run on
+// blockIdx.y (fewer directions a thread keep the dual numbers small enough
+// for registers, at the cost of recomputing the values once per group).
 template <int ND>
 __global__ void __launch_bounds__(kBGThreads)
 k_field_beam_grad(const __grid_constant__ DModel M, const __grid_constant__ BGArgs A) {
@@ -343,6 +347,7 @@ k_field_beam_grad(const __grid_constant__ DModel M, const __grid_constant__ BGAr
   using X = Cx<ND>;
   __shared__ double red[kBGThreads][ND];
   const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int g0 = (int)blockIdx.y * ND;  // this group's first direction
   double contrib[ND];
 #pragma unroll
   for (int d = 0; d < ND; ++d) contrib[d] = 0.0;
@@ -350,11 +355,11 @@ k_field_beam_grad(const __grid_constant__ DModel M, const __grid_constant__ BGAr
     D x = dc_<ND>(A.x[b]), y = dc_<ND>(A.y[b]), dx = dc_<ND>(A.dx[b]), dy = dc_<ND>(A.dy[b]);
 #pragma unroll
     for (int d = 0; d < ND; ++d) {
-      if (d >= A.n_dir) break;
-      if (A.dir_kind[d] == DIR_X) x.d[d] = 1.0;
-      if (A.dir_kind[d] == DIR_Y) y.d[d] = 1.0;
-      if (A.dir_kind[d] == DIR_DX) dx.d[d] = 1.0;
-      if (A.dir_kind[d] == DIR_DY) dy.d[d] = 1.0;
+      if (g0 + d >= A.n_dir) break;
+      if (A.dir_kind[g0 + d] == DIR_X) x.d[d] = 1.0;
+      if (A.dir_kind[g0 + d] == DIR_Y) y.d[d] = 1.0;
+      if (A.dir_kind[g0 + d] == DIR_DX) dx.d[d] = 1.0;
+      if (A.dir_kind[g0 + d] == DIR_DY) dy.d[d] = 1.0;
     }
     const D x0 = x, y0 = y, dx0 = dx, dy0 = dy;
     const double PI = 3.141592653589793;
@@ -400,9 +405,9 @@ k_field_beam_grad(const __grid_constant__ DModel M, const __grid_constant__ BGAr
         for (int j = 0; j < 4; ++j) a[j] = dc_<ND>(st.a[j]);
 #pragma unroll
         for (int d = 0; d < ND; ++d) {
-          if (d >= A.n_dir || A.dir_kind[d] != DIR_STEP || A.dir_step[d] != s) continue;
-          if (A.dir_a[d] >= 0) {
-            a[A.dir_a[d] & 3].d[d] = A.dir_seed[d];
+          if (g0 + d >= A.n_dir || A.dir_kind[g0 + d] != DIR_STEP || A.dir_step[g0 + d] != s) continue;
+          if (A.dir_a[g0 + d] >= 0) {
+            a[A.dir_a[g0 + d] & 3].d[d] = A.dir_seed[g0 + d];
           } else {  // rotation angle (radians): d(cos, sin) = (-sin, cos)
             a[0].d[d] = -st.a[1];
             a[1].d[d] = st.a[0];
@@ -531,26 +536,27 @@ k_field_beam_grad(const __grid_constant__ DModel M, const __grid_constant__ BGAr
     // dL/dp = Re(i sum_j dkap_j w_j + dlogpref w_1) = -sum_j Im(dkap_j w_j) + Re(dlogpref w_1)
 #pragma unroll
     for (int d = 0; d < ND; ++d) {
-      if (d >= A.n_dir) break;
+      if (g0 + d >= A.n_dir) break;
       double g = 0.0;
       for (int j = 0; j < 6; ++j) g -= kap[j].re.d[d] * wi[j] + kap[j].im.d[d] * wr[j];
       g += dlp[0].re.d[d] * wr[5] - dlp[0].im.d[d] * wi[5];
       contrib[d] = g;
-      const int kd = A.dir_kind[d];
+      const int kd = A.dir_kind[g0 + d];
       if (kd == DIR_X && A.gx) A.gx[b] = g;
       if (kd == DIR_Y && A.gy) A.gy[b] = g;
       if (kd == DIR_DX && A.gdx) A.gdx[b] = g;
       if (kd == DIR_DY && A.gdy) A.gdy[b] = g;
     }
-    if (A.gpl) A.gpl[b] = -k * wi[5];
-    if (A.gamp) {
+    if (A.gpl && blockIdx.y == 0) A.gpl[b] = -k * wi[5];
+    if (A.gamp && blockIdx.y == 0) {
       A.gamp[2 * b] = (float)ur[5];
       A.gamp[2 * b + 1] = (float)(-ui[5]);
     }
   }
   // the block's sums of the model directions, in a fixed order
 #pragma unroll
-  for (int d = 0; d < ND; ++d) red[threadIdx.x][d] = (d < A.n_dir && A.dir_kind[d] == DIR_STEP) ? contrib[d] : 0.0;
+  for (int d = 0; d < ND; ++d)
+    red[threadIdx.x][d] = (g0 + d < A.n_dir && A.dir_kind[g0 + d] == DIR_STEP) ? contrib[d] : 0.0;
   __syncthreads();
   for (int s = kBGThreads / 2; s > 0; s >>= 1) {
     if ((int)threadIdx.x < s)
@@ -558,13 +564,14 @@ k_field_beam_grad(const __grid_constant__ DModel M, const __grid_constant__ BGAr
       for (int d = 0; d < ND; ++d) red[threadIdx.x][d] += red[threadIdx.x + s][d];
     __syncthreads();
   }
-  if (threadIdx.x < ND && A.model_part) A.model_part[(size_t)blockIdx.x * kND + threadIdx.x] = red[0][threadIdx.x];
+  if ((int)threadIdx.x < ND && g0 + (int)threadIdx.x < A.n_dir && A.model_part)
+    A.model_part[(size_t)(g0 + threadIdx.x) * gridDim.x + blockIdx.x] = red[0][threadIdx.x];
 }
 
-// raw[target[d]] = sum over blocks (in order) of the group's per-block sums
+// raw[target[d]] = sum over blocks (in order) of direction d's per-block sums
 struct ModelSumArgs {
   int32_t n_dir, blocks;
-  int32_t target[kND];  // index into raw (step * 4 + slot), -1 = none
+  int32_t target[kBGLaunchDirs];  // index into raw (step * 4 + slot), -1 = none
 };
 
 __global__ void k_field_model_sum(const double* __restrict__ part, const __grid_constant__ ModelSumArgs A,
@@ -572,7 +579,7 @@ __global__ void k_field_model_sum(const double* __restrict__ part, const __grid_
   const int d = threadIdx.x;
   if (d >= A.n_dir || A.target[d] < 0) return;
   double a = 0.0;
-  for (int bk = 0; bk < A.blocks; ++bk) a += part[(size_t)bk * kND + d];
+  for (int bk = 0; bk < A.blocks; ++bk) a += part[(size_t)d * A.blocks + bk];
   raw[A.target[d]] = a;
 }
 
@@ -760,7 +767,7 @@ static AdjLayout adj_layout(int64_t n, int h, int w, int method = TG_FIELD_DIREC
   }
   L.part = off; off = al256a(off + nparts * n * 12 * sizeof(float));
   L.mom = off; off = al256a(off + (size_t)n * 12 * sizeof(double));
-  L.model = off; off = al256a(off + (size_t)L.bg_blocks * kND * sizeof(double));
+  L.model = off; off = al256a(off + (size_t)L.bg_blocks * kBGLaunchDirs * sizeof(double));
   if (method == TG_FIELD_SEPARABLE) {
     L.rows_pad = (h + 127) / 128 * 128;
     L.cols_pad = (w + 31) / 32 * 32;
@@ -890,8 +897,9 @@ static int field_vjp_impl(const tg_model* model, const tg_beams* beams, const tg
     }
   }
   double* mpart = reinterpret_cast<double*>(ws + L.model);
-  const int groups = dirs.empty() ? 1 : (int)((dirs.size() + kBGDirs - 1) / kBGDirs);
-  for (int gidx = 0; gidx < groups; ++gidx) {
+  // launches of up to kBGLaunchDirs directions, kBGDirs a thread (groups on blockIdx.y)
+  const int launches = dirs.empty() ? 1 : (int)((dirs.size() + kBGLaunchDirs - 1) / kBGLaunchDirs);
+  for (int li = 0; li < launches; ++li) {
     BGArgs B;
     std::memset(&B, 0, sizeof(B));
     B.n = n;
@@ -912,12 +920,9 @@ static int field_vjp_impl(const tg_model* model, const tg_beams* beams, const tg
     ModelSumArgs S;
     std::memset(&S, 0, sizeof(S));
     bool any_model = false;
-    for (int d = 0; d < kND; ++d) {
-      const size_t i = (size_t)gidx * kBGDirs + d;
-      if (d >= kBGDirs) {
-        S.target[d] = -1;
-        continue;
-      }
+    B.n_dir = 0;
+    for (int d = 0; d < kBGLaunchDirs; ++d) {
+      const size_t i = (size_t)li * kBGLaunchDirs + d;
       S.target[d] = -1;
       if (i >= dirs.size()) continue;
       B.n_dir = d + 1;
@@ -928,19 +933,20 @@ static int field_vjp_impl(const tg_model* model, const tg_beams* beams, const tg
       S.target[d] = dirs[i].target;
       if (dirs[i].kind == DIR_STEP) any_model = true;
     }
-    // every launch writes the ray directions it carries; the pathlength and
-    // amplitude gradients need no direction and come from the first
+    // every group writes the ray directions it carries; the pathlength and
+    // amplitude gradients need no direction and come from the first group
     B.gx = out->x; B.gy = out->y; B.gdx = out->dx; B.gdy = out->dy;
-    if (gidx == 0) {
+    if (li == 0) {
       B.gpl = out->pathlength;
       B.gamp = out->amplitude;
     }
     B.model_part = mpart;
-    k_field_beam_grad<kBGDirs><<<L.bg_blocks, kBGThreads, 0, s>>>(dm, B);
+    const int groups = B.n_dir > 0 ? (B.n_dir + kBGDirs - 1) / kBGDirs : 1;
+    k_field_beam_grad<kBGDirs><<<dim3(L.bg_blocks, groups), kBGThreads, 0, s>>>(dm, B);
     if (any_model && out->raw) {
       S.n_dir = B.n_dir;
       S.blocks = L.bg_blocks;
-      k_field_model_sum<<<1, kND, 0, s>>>(mpart, S, out->raw);
+      k_field_model_sum<<<1, kBGLaunchDirs, 0, s>>>(mpart, S, out->raw);
     }
   }
   return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
