@@ -22,11 +22,12 @@
 //      the forward's k_field_gemm, k_adj_sep_moments; see below);
 //   2. k_field_moment_sum: the per-block partials summed in a fixed order;
 //   3. k_field_beam_grad<4>: per beam, the preparation arithmetic again in
-//      float64 forward mode (dual numbers carrying 4 directions a thread; the
-//      direction groups of a launch on blockIdx.y, up to 32 directions a
-//      launch: the central ray's x, y, dx, dy and the model's step
-//      parameters) for d kap / dp and d log pref / dp, contracted with the
-//      moments;
+//      float64 forward mode for d kap / dp and d log pref / dp, contracted
+//      with the moments.  The directions (the central ray's x, y, dx, dy and
+//      the model's step parameters, up to 32 a launch) run in groups on
+//      blockIdx.y: the central ray's four together, whose group computes the
+//      ABCD algebra without dual parts (it does not depend on the ray), and
+//      the step parameters two at a time;
 //   4. k_field_model_sum: the model parameters' per-block sums in a fixed
 //      order, written as per-step sums in the layout of tg_trace_vjp.
 // Every reduction runs in a fixed order, so the gradients are deterministic.
@@ -194,7 +195,7 @@ __global__ void k_field_moment_sum(const float* __restrict__ part, int nparts, i
 // value + derivatives along N directions (forward mode, float64)
 template <int N>
 struct Du {
-  double v, d[N];
+  double v, d[N > 0 ? N : 1];  // N = 0: a plain value (d unused)
 };
 template <int N>
 __device__ __forceinline__ Du<N> dc_(double v) {
@@ -303,15 +304,20 @@ __device__ __forceinline__ M2<N> nan0(const M2<N>& m) {
 }
 
 // ------------------------------------------------------------ beam gradient
-// Four directions a thread, 64 threads a block.  Measured on the separable
-// 16,384-beam adjoint (whole call), one launch per direction group: 8
-// directions a thread (14 KB of stack) 1.40 ms, 4 directions 0.99 ms, 2
-// directions 1.07-1.08 ms, 1 direction (no stack, twice the recomputation)
-// 1.14-1.17 ms.  All groups in one launch (blockIdx.y): 0.932 -> 0.898 ms
-// with 4 directions a thread (2: 0.959, 1: 0.940); the kernel takes 255
-// registers, so an SM holds 8 of its warps and 16,384 beams fill ~7.
+// Direction groups, 64 threads a block.  Measured on the separable
+// 16,384-beam adjoint (whole call; Lens + Detector: the central ray's four
+// directions and three step parameters): one launch per group of 4
+// directions 0.93 ms (8 directions a thread, 14 KB of stack: 1.40 ms); all
+// groups in one launch (blockIdx.y) 0.90 ms; the central-ray group without
+// dual parts in the matrix algebra 0.82 ms; step groups carried at the
+// narrowest width that holds them 0.76 ms, and at most 2 step directions a
+// group 0.73 ms (1: 0.78; the central ray in groups of 2: 0.76).  Results
+// are bit-identical across these layouts.  The kernel takes 255 registers,
+// so an SM holds 8 of its warps.
 constexpr int kBGThreads = 64;
-constexpr int kBGDirs = 4;          // directions a thread carries
+constexpr int kBGDirs = 4;          // directions a thread carries (at most)
+constexpr int kBGRayDirs = 4;       // central-ray directions a thread carries
+constexpr int kBGStepDirs = 2;      // model-step directions a thread carries
 constexpr int kBGLaunchDirs = 32;   // directions a launch carries (groups on blockIdx.y)
 enum DirKind : int32_t { DIR_X = 0, DIR_Y = 1, DIR_DX = 2, DIR_DY = 3, DIR_STEP = 4 };
 
@@ -328,7 +334,8 @@ struct BGArgs {
   const BeamFast* rec;  // unit-amplitude records: the envelope centres
   const double* mom;    // [n][12] moments about the centres
   int32_t input_plane;
-  int32_t n_dir;  // directions of this launch: group blockIdx.y takes [ND y, ND y + ND)
+  int32_t n_dir;  // directions of this launch
+  int32_t group_first[kBGLaunchDirs], group_n[kBGLaunchDirs];  // group blockIdx.y: its directions
   int32_t dir_kind[kBGLaunchDirs], dir_step[kBGLaunchDirs], dir_a[kBGLaunchDirs];  // dir_a: a[] entry, -1 = angle
   double dir_seed[kBGLaunchDirs];                                                 // d a[dir_a] / d parameter
   double *gx, *gy, *gdx, *gdy;  // per beam, for DIR_X .. DIR_DY directions (may be NULL)
@@ -337,75 +344,88 @@ struct BGArgs {
   double* model_part;           // [direction][gridDim.x] sums over the block's beams (DIR_STEP)
 };
 
-// ND: directions carried by a thread; the launch's direction groups run on
-// blockIdx.y (fewer directions a thread keep the dual numbers small enough
-// for registers, at the cost of recomputing the values once per group).
-template <int ND>
-__global__ void __launch_bounds__(kBGThreads)
-k_field_beam_grad(const __grid_constant__ DModel M, const __grid_constant__ BGArgs A) {
+// lift a value with NM derivative directions to ND (zeros when NM = 0)
+template <int ND, int NM>
+__device__ __forceinline__ Du<ND> lift(const Du<NM>& a) {
+  if constexpr (NM == ND) {
+    return a;
+  } else {
+    return dc_<ND>(a.v);
+  }
+}
+template <int ND, int NM>
+__device__ __forceinline__ Cx<ND> lift(const Cx<NM>& a) {
+  return Cx<ND>{lift<ND>(a.re), lift<ND>(a.im)};
+}
+
+// One beam's contributions along directions [g0, g0 + ND) of the launch.
+// STEP: the group carries model-step directions, so the ABCD matrices, Q2,
+// the prefactor and everything built from them carry derivatives; without
+// them (the central ray's x, y, dx, dy) those quantities are constants and
+// are computed without dual parts (NM = 0), and only the terms that hold
+// the central ray carry the ND directions.  The propagated central ray is
+// needed by value only (the biprism's sign).
+template <int ND, bool STEP, int NC>
+__device__ __forceinline__ void beam_grad_body(const DModel& M, const BGArgs& A, int64_t b, int g0, int nd,
+                                               double (&contrib)[NC]) {
+  constexpr int NM = STEP ? ND : 0;
   using D = Du<ND>;
   using X = Cx<ND>;
-  __shared__ double red[kBGThreads][ND];
-  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int g0 = (int)blockIdx.y * ND;  // this group's first direction
-  double contrib[ND];
+  using DM = Du<NM>;
+  D x0 = dc_<ND>(A.x[b]), y0 = dc_<ND>(A.y[b]), dx0 = dc_<ND>(A.dx[b]), dy0 = dc_<ND>(A.dy[b]);
 #pragma unroll
-  for (int d = 0; d < ND; ++d) contrib[d] = 0.0;
-  if (b < A.n) {
-    D x = dc_<ND>(A.x[b]), y = dc_<ND>(A.y[b]), dx = dc_<ND>(A.dx[b]), dy = dc_<ND>(A.dy[b]);
+  for (int d = 0; d < ND; ++d) {
+    if (d >= nd) break;
+    if (A.dir_kind[g0 + d] == DIR_X) x0.d[d] = 1.0;
+    if (A.dir_kind[g0 + d] == DIR_Y) y0.d[d] = 1.0;
+    if (A.dir_kind[g0 + d] == DIR_DX) dx0.d[d] = 1.0;
+    if (A.dir_kind[g0 + d] == DIR_DY) dy0.d[d] = 1.0;
+  }
+  const double PI = 3.141592653589793;
+  const double wl = A.wl ? A.wl[b] : A.wl_scalar;
+  const double k = 2.0 * PI / wl, hk = 0.5 * k;
+  // Q1^-1 = R diag(1/qx, 1/qy) R^T (gaussian.py:138-177): no directions
+  const double wx = A.waist[2 * b], wy = A.waist[2 * b + 1];
+  const double Rx = A.radii[2 * b], Ry = A.radii[2 * b + 1];
+  const double qxr = isinf(Rx) ? 0.0 : -1.0 / Rx, qxi = wl / (PI * wx * wx);
+  const double qyr = isinf(Ry) ? 0.0 : -1.0 / Ry, qyi = wl / (PI * wy * wy);
+  const double th = A.theta ? A.theta[b] : 0.0;
+  double sth, cth;
+  sincos(th, &sth, &cth);
+  const M2<NM> Q1i{cx_<NM>(cth * cth * qxr + sth * sth * qyr, cth * cth * qxi + sth * sth * qyi),
+                   cx_<NM>(cth * sth * (qxr - qyr), cth * sth * (qxi - qyi)),
+                   cx_<NM>(cth * sth * (qxr - qyr), cth * sth * (qxi - qyi)),
+                   cx_<NM>(sth * sth * qxr + cth * cth * qyr, sth * sth * qxi + cth * cth * qyi)};
+  X Sxx, Syy, Sxy, Lx, Ly, c0;
+  D ox, oy;
+  X dlp = cx_<ND>(0.0, 0.0);  // d log pref as a complex dual (its derivative parts are used)
+  if (A.input_plane) {  // gaussian.py:402-409: s = r1 - r1m, S = Q1^-1, L = 2 theta1m
+    Sxx = lift<ND>(Q1i.a);
+    Syy = lift<ND>(Q1i.d);
+    Sxy = lift<ND>(0.5 * (Q1i.b + Q1i.c));
+    Lx = cx_<ND>(2.0 * dx0);
+    Ly = cx_<ND>(2.0 * dy0);
+    c0 = cx_<ND>(0.0, 0.0);
+    ox = x0;
+    oy = y0;
+  } else {
+    // central ray and 5x5 ABCD (rows x, y, dx, dy, 1) with the model's
+    // step parameters as directions
+    double x = x0.v, y = y0.v, dx = dx0.v, dy = dy0.v;
+    DM m[5][5];
 #pragma unroll
-    for (int d = 0; d < ND; ++d) {
-      if (g0 + d >= A.n_dir) break;
-      if (A.dir_kind[g0 + d] == DIR_X) x.d[d] = 1.0;
-      if (A.dir_kind[g0 + d] == DIR_Y) y.d[d] = 1.0;
-      if (A.dir_kind[g0 + d] == DIR_DX) dx.d[d] = 1.0;
-      if (A.dir_kind[g0 + d] == DIR_DY) dy.d[d] = 1.0;
-    }
-    const D x0 = x, y0 = y, dx0 = dx, dy0 = dy;
-    const double PI = 3.141592653589793;
-    const double wl = A.wl ? A.wl[b] : A.wl_scalar;
-    const double k = 2.0 * PI / wl, hk = 0.5 * k;
-    // Q1^-1 = R diag(1/qx, 1/qy) R^T (gaussian.py:138-177): no directions
-    const double wx = A.waist[2 * b], wy = A.waist[2 * b + 1];
-    const double Rx = A.radii[2 * b], Ry = A.radii[2 * b + 1];
-    const double qxr = isinf(Rx) ? 0.0 : -1.0 / Rx, qxi = wl / (PI * wx * wx);
-    const double qyr = isinf(Ry) ? 0.0 : -1.0 / Ry, qyi = wl / (PI * wy * wy);
-    const double th = A.theta ? A.theta[b] : 0.0;
-    double sth, cth;
-    sincos(th, &sth, &cth);
-    const M2<ND> Q1i{cx_<ND>(cth * cth * qxr + sth * sth * qyr, cth * cth * qxi + sth * sth * qyi),
-                      cx_<ND>(cth * sth * (qxr - qyr), cth * sth * (qxi - qyi)),
-                      cx_<ND>(cth * sth * (qxr - qyr), cth * sth * (qxi - qyi)),
-                      cx_<ND>(sth * sth * qxr + cth * cth * qyr, sth * sth * qxi + cth * cth * qyi)};
-    X Sxx, Syy, Sxy, Lx, Ly, c0;
-    D ox, oy;
-    X dlp[1];  // d log pref as a complex dual (its derivative parts are used)
-    dlp[0] = cx_<ND>(0.0, 0.0);
-    if (A.input_plane) {  // gaussian.py:402-409: s = r1 - r1m, S = Q1^-1, L = 2 theta1m
-      Sxx = Q1i.a;
-      Syy = Q1i.d;
-      Sxy = 0.5 * (Q1i.b + Q1i.c);
-      Lx = cx_<ND>(2.0 * dx0);
-      Ly = cx_<ND>(2.0 * dy0);
-      c0 = cx_<ND>(0.0, 0.0);
-      ox = x0;
-      oy = y0;
-    } else {
-      // central ray and 5x5 ABCD (rows x, y, dx, dy, 1) with the model's
-      // step parameters as directions
-      D m[5][5];
+    for (int i = 0; i < 5; ++i)
 #pragma unroll
-      for (int i = 0; i < 5; ++i)
+      for (int j = 0; j < 5; ++j) m[i][j] = dc_<NM>(i == j ? 1.0 : 0.0);
+    for (int s = 0; s < M.n; ++s) {
+      const DStep& st = M.s[s];
+      DM a[4];
 #pragma unroll
-        for (int j = 0; j < 5; ++j) m[i][j] = dc_<ND>(i == j ? 1.0 : 0.0);
-      for (int s = 0; s < M.n; ++s) {
-        const DStep& st = M.s[s];
-        D a[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) a[j] = dc_<ND>(st.a[j]);
+      for (int j = 0; j < 4; ++j) a[j] = dc_<NM>(st.a[j]);
+      if constexpr (STEP) {
 #pragma unroll
         for (int d = 0; d < ND; ++d) {
-          if (g0 + d >= A.n_dir || A.dir_kind[g0 + d] != DIR_STEP || A.dir_step[g0 + d] != s) continue;
+          if (d >= nd || A.dir_kind[g0 + d] != DIR_STEP || A.dir_step[g0 + d] != s) continue;
           if (A.dir_a[g0 + d] >= 0) {
             a[A.dir_a[g0 + d] & 3].d[d] = A.dir_seed[g0 + d];
           } else {  // rotation angle (radians): d(cos, sin) = (-sin, cos)
@@ -413,150 +433,194 @@ k_field_beam_grad(const __grid_constant__ DModel M, const __grid_constant__ BGAr
             a[1].d[d] = st.a[0];
           }
         }
-        switch (st.kind) {
-          case D_FREE:
-            for (int j = 0; j < 5; ++j) {
-              m[0][j] = m[0][j] + a[0] * m[2][j];
-              m[1][j] = m[1][j] + a[0] * m[3][j];
-            }
-            x = x + dx * a[0];
-            y = y + dy * a[0];
-            break;
-          case D_LENS:  // a[1] = 1/f
-            for (int j = 0; j < 5; ++j) {
-              m[2][j] = m[2][j] - m[0][j] * a[1];
-              m[3][j] = m[3][j] - m[1][j] * a[1];
-            }
-            dx = dx - x * a[1];
-            dy = dy - y * a[1];
-            break;
-          case D_SHIFT:
-            m[0][4] = m[0][4] + a[0]; m[1][4] = m[1][4] + a[1];
-            m[2][4] = m[2][4] + a[2]; m[3][4] = m[3][4] + a[3];
-            x = x + a[0]; y = y + a[1]; dx = dx + a[2]; dy = dy + a[3];
-            break;
-          case D_BIPRISM: {
-            const double sg = x.v > 0.0 ? 1.0 : (x.v < 0.0 ? -1.0 : 0.0);
-            m[2][4] = m[2][4] + sg * a[0];
-            dx = dx + sg * a[0];
-          } break;
-          case D_ROTATE:
-            for (int j = 0; j < 5; ++j) {
-              const D r0 = m[0][j], r1 = m[1][j], r2 = m[2][j], r3 = m[3][j];
-              m[0][j] = a[0] * r0 - a[1] * r1;
-              m[1][j] = a[1] * r0 + a[0] * r1;
-              m[2][j] = a[0] * r2 - a[1] * r3;
-              m[3][j] = a[1] * r2 + a[0] * r3;
-            }
-            {
-              const D nx = a[0] * x - a[1] * y, ny = a[1] * x + a[0] * y;
-              const D ndx = a[0] * dx - a[1] * dy, ndy = a[1] * dx + a[0] * dy;
-              x = nx; y = ny; dx = ndx; dy = ndy;
-            }
-            break;
-          default:  // D_NOP (an aberrated lens is rejected on the host)
-            break;
-        }
       }
-      const M2<ND> Am{cx_<ND>(m[0][0]), cx_<ND>(m[0][1]), cx_<ND>(m[1][0]), cx_<ND>(m[1][1])};
-      const M2<ND> Bm{cx_<ND>(m[0][2]), cx_<ND>(m[0][3]), cx_<ND>(m[1][2]), cx_<ND>(m[1][3])};
-      const M2<ND> Cm{cx_<ND>(m[2][0]), cx_<ND>(m[2][1]), cx_<ND>(m[3][0]), cx_<ND>(m[3][1])};
-      const M2<ND> Dm{cx_<ND>(m[2][2]), cx_<ND>(m[2][3]), cx_<ND>(m[3][2]), cx_<ND>(m[3][3])};
-      // Q2^-1 = (A + B Q1^-1)^-1 (C + D Q1^-1)   (gaussian.py:92-96)
-      const M2<ND> denom = Am + Bm * Q1i;
-      const M2<ND> Q2 = inv2(denom) * (Cm + Dm * Q1i);
-      const M2<ND> Binv = nan0(inv2(Bm));
-      const M2<ND> Q1 = nan0(inv2(Q1i));
-      const D r2mx = m[0][0] * x0 + m[0][1] * y0 + m[0][2] * dx0 + m[0][3] * dy0;
-      const D r2my = m[1][0] * x0 + m[1][1] * y0 + m[1][2] * dx0 + m[1][3] * dy0;
-      // pref = amp / sqrt(det): d log pref = -d det / (2 det)
-      const X det = denom.a * denom.d - denom.b * denom.c;
-      {
-        X dd;
-        dd.re = det.re;
-        dd.im = det.im;
-        dd.re.v = 0.0;  // the quotient below uses only the derivative parts
-        dd.im.v = 0.0;
-        const X q = (-0.5) * (dd / cx_<ND>(det.re.v, det.im.v));
-        dlp[0] = q;
+      switch (st.kind) {
+        case D_FREE:
+          for (int j = 0; j < 5; ++j) {
+            m[0][j] = m[0][j] + a[0] * m[2][j];
+            m[1][j] = m[1][j] + a[0] * m[3][j];
+          }
+          x += dx * st.a[0];
+          y += dy * st.a[0];
+          break;
+        case D_LENS:  // a[1] = 1/f
+          for (int j = 0; j < 5; ++j) {
+            m[2][j] = m[2][j] - m[0][j] * a[1];
+            m[3][j] = m[3][j] - m[1][j] * a[1];
+          }
+          dx -= x * st.a[1];
+          dy -= y * st.a[1];
+          break;
+        case D_SHIFT:
+          m[0][4] = m[0][4] + a[0]; m[1][4] = m[1][4] + a[1];
+          m[2][4] = m[2][4] + a[2]; m[3][4] = m[3][4] + a[3];
+          x += st.a[0]; y += st.a[1]; dx += st.a[2]; dy += st.a[3];
+          break;
+        case D_BIPRISM: {
+          const double sg = x > 0.0 ? 1.0 : (x < 0.0 ? -1.0 : 0.0);
+          m[2][4] = m[2][4] + sg * a[0];
+          dx += sg * st.a[0];
+        } break;
+        case D_ROTATE:
+          for (int j = 0; j < 5; ++j) {
+            const DM r0 = m[0][j], r1 = m[1][j], r2 = m[2][j], r3 = m[3][j];
+            m[0][j] = a[0] * r0 - a[1] * r1;
+            m[1][j] = a[1] * r0 + a[0] * r1;
+            m[2][j] = a[0] * r2 - a[1] * r3;
+            m[3][j] = a[1] * r2 + a[0] * r3;
+          }
+          {
+            const double c = st.a[0], sn = st.a[1];
+            const double nx = c * x - sn * y, ny = sn * x + c * y;
+            const double ndx = c * dx - sn * dy, ndy = sn * dx + c * dy;
+            x = nx; y = ny; dx = ndx; dy = ndy;
+          }
+          break;
+        default:  // D_NOP (an aberrated lens is rejected on the host)
+          break;
       }
-      const M2<ND> ABinv = Am * Binv;
-      const M2<ND> P = Q1 * inv2(Bm * (Am * Q1 + Bm));
-      Sxx = Q2.a;
-      Syy = Q2.d;
-      Sxy = 0.5 * (Q2.b + Q2.c);
-      const X bx = Binv.a * cx_<ND>(x0) + Binv.c * cx_<ND>(y0), by = Binv.b * cx_<ND>(x0) + Binv.d * cx_<ND>(y0);
-      const X px = P.a * cx_<ND>(r2mx) + P.c * cx_<ND>(r2my), py = P.b * cx_<ND>(r2mx) + P.d * cx_<ND>(r2my);
-      Lx = 2.0 * (cx_<ND>(m[2][4]) - bx + px);
-      Ly = 2.0 * (cx_<ND>(m[3][4]) - by + py);
-      const X q1 = cx_<ND>(x0) * (ABinv.a * cx_<ND>(x0) + ABinv.b * cx_<ND>(y0)) +
-                   cx_<ND>(y0) * (ABinv.c * cx_<ND>(x0) + ABinv.d * cx_<ND>(y0));
-      const X q2 = cx_<ND>(r2mx) * (P.a * cx_<ND>(r2mx) + P.b * cx_<ND>(r2my)) +
-                   cx_<ND>(r2my) * (P.c * cx_<ND>(r2mx) + P.d * cx_<ND>(r2my));
-      c0 = q1 - q2;
-      ox = m[0][4];
-      oy = m[1][4];
     }
-    // the polynomial in (row, col): s = s0 + row u + col v
-    const D s0x = dc_<ND>(A.pm.t[5]) - ox, s0y = dc_<ND>(A.pm.t[2]) - oy;
-    const double ux = A.pm.t[3], uy = A.pm.t[0], vx = A.pm.t[4], vy = A.pm.t[1];
-    auto quad = [&](const D& ax, const D& ay, const D& bx2, const D& by2) -> X {  // a^T S b
-      return (ax * bx2) * Sxx + (ay * by2) * Syy + (ax * by2 + ay * bx2) * Sxy;
-    };
-    const D U0 = dc_<ND>(ux), U1 = dc_<ND>(uy), V0 = dc_<ND>(vx), V1 = dc_<ND>(vy);
-    X kap[6];  // cc, rr, rc, c, r, 0
-    kap[0] = hk * quad(V0, V1, V0, V1);
-    kap[1] = hk * quad(U0, U1, U0, U1);
-    kap[2] = hk * (2.0 * quad(U0, U1, V0, V1));
-    kap[3] = hk * (2.0 * quad(s0x, s0y, V0, V1) + V0 * Lx + V1 * Ly);
-    kap[4] = hk * (2.0 * quad(s0x, s0y, U0, U1) + U0 * Lx + U1 * Ly);
-    kap[5] = hk * (quad(s0x, s0y, s0x, s0y) + s0x * Lx + s0y * Ly + c0);
-    // moments about the envelope centre -> moments of the monomials
-    const double* mo = A.mom + b * 12;
-    const double r0 = (double)A.rec[b].r0, cc0 = (double)A.rec[b].c0;
-    double mr[6], mi[6];  // centred: 1, dc, dr, dc^2, dr dc, dr^2
-    for (int i = 0; i < 6; ++i) { mr[i] = mo[2 * i]; mi[i] = mo[2 * i + 1]; }
-    double ur[6], ui[6];  // by kap order: col^2, row^2, row col, col, row, 1
-    ur[5] = mr[0]; ui[5] = mi[0];
-    ur[3] = mr[1] + cc0 * mr[0]; ui[3] = mi[1] + cc0 * mi[0];
-    ur[4] = mr[2] + r0 * mr[0]; ui[4] = mi[2] + r0 * mi[0];
-    ur[0] = mr[3] + 2.0 * cc0 * mr[1] + cc0 * cc0 * mr[0];
-    ui[0] = mi[3] + 2.0 * cc0 * mi[1] + cc0 * cc0 * mi[0];
-    ur[1] = mr[5] + 2.0 * r0 * mr[2] + r0 * r0 * mr[0];
-    ui[1] = mi[5] + 2.0 * r0 * mi[2] + r0 * r0 * mi[0];
-    ur[2] = mr[4] + cc0 * mr[2] + r0 * mr[1] + r0 * cc0 * mr[0];
-    ui[2] = mi[4] + cc0 * mi[2] + r0 * mi[1] + r0 * cc0 * mi[0];
-    // times the amplitude: F = amp E
-    const double ar = (double)A.amp[2 * b], ai = (double)A.amp[2 * b + 1];
-    double wr[6], wi[6];
-    for (int j = 0; j < 6; ++j) {
-      wr[j] = ar * ur[j] - ai * ui[j];
-      wi[j] = ar * ui[j] + ai * ur[j];
+    const M2<NM> Am{cx_<NM>(m[0][0]), cx_<NM>(m[0][1]), cx_<NM>(m[1][0]), cx_<NM>(m[1][1])};
+    const M2<NM> Bm{cx_<NM>(m[0][2]), cx_<NM>(m[0][3]), cx_<NM>(m[1][2]), cx_<NM>(m[1][3])};
+    const M2<NM> Cm{cx_<NM>(m[2][0]), cx_<NM>(m[2][1]), cx_<NM>(m[3][0]), cx_<NM>(m[3][1])};
+    const M2<NM> Dm{cx_<NM>(m[2][2]), cx_<NM>(m[2][3]), cx_<NM>(m[3][2]), cx_<NM>(m[3][3])};
+    // Q2^-1 = (A + B Q1^-1)^-1 (C + D Q1^-1)   (gaussian.py:92-96)
+    const M2<NM> denom = Am + Bm * Q1i;
+    const M2<NM> Q2 = inv2(denom) * (Cm + Dm * Q1i);
+    const M2<NM> Binv = nan0(inv2(Bm));
+    const M2<NM> Q1 = nan0(inv2(Q1i));
+    const D r2mx = lift<ND>(m[0][0]) * x0 + lift<ND>(m[0][1]) * y0 + lift<ND>(m[0][2]) * dx0 + lift<ND>(m[0][3]) * dy0;
+    const D r2my = lift<ND>(m[1][0]) * x0 + lift<ND>(m[1][1]) * y0 + lift<ND>(m[1][2]) * dx0 + lift<ND>(m[1][3]) * dy0;
+    // pref = amp / sqrt(det): d log pref = -d det / (2 det)
+    if constexpr (STEP) {
+      const Cx<NM> det = denom.a * denom.d - denom.b * denom.c;
+      Cx<NM> dd;
+      dd.re = det.re;
+      dd.im = det.im;
+      dd.re.v = 0.0;  // the quotient below uses only the derivative parts
+      dd.im.v = 0.0;
+      dlp = lift<ND>((-0.5) * (dd / cx_<NM>(det.re.v, det.im.v)));
     }
-    // dL/dp = Re(i sum_j dkap_j w_j + dlogpref w_1) = -sum_j Im(dkap_j w_j) + Re(dlogpref w_1)
+    const M2<NM> ABinv = Am * Binv;
+    const M2<NM> P = Q1 * inv2(Bm * (Am * Q1 + Bm));
+    Sxx = lift<ND>(Q2.a);
+    Syy = lift<ND>(Q2.d);
+    Sxy = lift<ND>(0.5 * (Q2.b + Q2.c));
+    const X bx = lift<ND>(Binv.a) * cx_<ND>(x0) + lift<ND>(Binv.c) * cx_<ND>(y0);
+    const X by = lift<ND>(Binv.b) * cx_<ND>(x0) + lift<ND>(Binv.d) * cx_<ND>(y0);
+    const X px = lift<ND>(P.a) * cx_<ND>(r2mx) + lift<ND>(P.c) * cx_<ND>(r2my);
+    const X py = lift<ND>(P.b) * cx_<ND>(r2mx) + lift<ND>(P.d) * cx_<ND>(r2my);
+    Lx = 2.0 * (cx_<ND>(lift<ND>(m[2][4])) - bx + px);
+    Ly = 2.0 * (cx_<ND>(lift<ND>(m[3][4])) - by + py);
+    const X q1 = cx_<ND>(x0) * (lift<ND>(ABinv.a) * cx_<ND>(x0) + lift<ND>(ABinv.b) * cx_<ND>(y0)) +
+                 cx_<ND>(y0) * (lift<ND>(ABinv.c) * cx_<ND>(x0) + lift<ND>(ABinv.d) * cx_<ND>(y0));
+    const X q2 = cx_<ND>(r2mx) * (lift<ND>(P.a) * cx_<ND>(r2mx) + lift<ND>(P.b) * cx_<ND>(r2my)) +
+                 cx_<ND>(r2my) * (lift<ND>(P.c) * cx_<ND>(r2mx) + lift<ND>(P.d) * cx_<ND>(r2my));
+    c0 = q1 - q2;
+    ox = lift<ND>(m[0][4]);
+    oy = lift<ND>(m[1][4]);
+  }
+  // the polynomial in (row, col): s = s0 + row u + col v
+  const D s0x = dc_<ND>(A.pm.t[5]) - ox, s0y = dc_<ND>(A.pm.t[2]) - oy;
+  const double ux = A.pm.t[3], uy = A.pm.t[0], vx = A.pm.t[4], vy = A.pm.t[1];
+  auto quad = [&](const D& ax, const D& ay, const D& bx2, const D& by2) -> X {  // a^T S b
+    return (ax * bx2) * Sxx + (ay * by2) * Syy + (ax * by2 + ay * bx2) * Sxy;
+  };
+  const D U0 = dc_<ND>(ux), U1 = dc_<ND>(uy), V0 = dc_<ND>(vx), V1 = dc_<ND>(vy);
+  X kap[6];  // cc, rr, rc, c, r, 0
+  kap[0] = hk * quad(V0, V1, V0, V1);
+  kap[1] = hk * quad(U0, U1, U0, U1);
+  kap[2] = hk * (2.0 * quad(U0, U1, V0, V1));
+  kap[3] = hk * (2.0 * quad(s0x, s0y, V0, V1) + V0 * Lx + V1 * Ly);
+  kap[4] = hk * (2.0 * quad(s0x, s0y, U0, U1) + U0 * Lx + U1 * Ly);
+  kap[5] = hk * (quad(s0x, s0y, s0x, s0y) + s0x * Lx + s0y * Ly + c0);
+  // moments about the envelope centre -> moments of the monomials
+  const double* mo = A.mom + b * 12;
+  const double r0 = (double)A.rec[b].r0, cc0 = (double)A.rec[b].c0;
+  double mr[6], mi[6];  // centred: 1, dc, dr, dc^2, dr dc, dr^2
+  for (int i = 0; i < 6; ++i) { mr[i] = mo[2 * i]; mi[i] = mo[2 * i + 1]; }
+  double ur[6], ui[6];  // by kap order: col^2, row^2, row col, col, row, 1
+  ur[5] = mr[0]; ui[5] = mi[0];
+  ur[3] = mr[1] + cc0 * mr[0]; ui[3] = mi[1] + cc0 * mi[0];
+  ur[4] = mr[2] + r0 * mr[0]; ui[4] = mi[2] + r0 * mi[0];
+  ur[0] = mr[3] + 2.0 * cc0 * mr[1] + cc0 * cc0 * mr[0];
+  ui[0] = mi[3] + 2.0 * cc0 * mi[1] + cc0 * cc0 * mi[0];
+  ur[1] = mr[5] + 2.0 * r0 * mr[2] + r0 * r0 * mr[0];
+  ui[1] = mi[5] + 2.0 * r0 * mi[2] + r0 * r0 * mi[0];
+  ur[2] = mr[4] + cc0 * mr[2] + r0 * mr[1] + r0 * cc0 * mr[0];
+  ui[2] = mi[4] + cc0 * mi[2] + r0 * mi[1] + r0 * cc0 * mi[0];
+  // times the amplitude: F = amp E
+  const double ar = (double)A.amp[2 * b], ai = (double)A.amp[2 * b + 1];
+  double wr[6], wi[6];
+  for (int j = 0; j < 6; ++j) {
+    wr[j] = ar * ur[j] - ai * ui[j];
+    wi[j] = ar * ui[j] + ai * ur[j];
+  }
+  // dL/dp = Re(i sum_j dkap_j w_j + dlogpref w_1) = -sum_j Im(dkap_j w_j) + Re(dlogpref w_1)
 #pragma unroll
-    for (int d = 0; d < ND; ++d) {
-      if (g0 + d >= A.n_dir) break;
-      double g = 0.0;
-      for (int j = 0; j < 6; ++j) g -= kap[j].re.d[d] * wi[j] + kap[j].im.d[d] * wr[j];
-      g += dlp[0].re.d[d] * wr[5] - dlp[0].im.d[d] * wi[5];
-      contrib[d] = g;
-      const int kd = A.dir_kind[g0 + d];
-      if (kd == DIR_X && A.gx) A.gx[b] = g;
-      if (kd == DIR_Y && A.gy) A.gy[b] = g;
-      if (kd == DIR_DX && A.gdx) A.gdx[b] = g;
-      if (kd == DIR_DY && A.gdy) A.gdy[b] = g;
-    }
-    if (A.gpl && blockIdx.y == 0) A.gpl[b] = -k * wi[5];
-    if (A.gamp && blockIdx.y == 0) {
-      A.gamp[2 * b] = (float)ur[5];
-      A.gamp[2 * b + 1] = (float)(-ui[5]);
-    }
+  for (int d = 0; d < ND; ++d) {
+    if (d >= nd) break;
+    double g = 0.0;
+    for (int j = 0; j < 6; ++j) g -= kap[j].re.d[d] * wi[j] + kap[j].im.d[d] * wr[j];
+    g += dlp.re.d[d] * wr[5] - dlp.im.d[d] * wi[5];
+    contrib[d] = g;
+    const int kd = A.dir_kind[g0 + d];
+    if (kd == DIR_X && A.gx) A.gx[b] = g;
+    if (kd == DIR_Y && A.gy) A.gy[b] = g;
+    if (kd == DIR_DX && A.gdx) A.gdx[b] = g;
+    if (kd == DIR_DY && A.gdy) A.gdy[b] = g;
+  }
+  if (A.gpl && blockIdx.y == 0) A.gpl[b] = -k * wi[5];
+  if (A.gamp && blockIdx.y == 0) {
+    A.gamp[2 * b] = (float)ur[5];
+    A.gamp[2 * b + 1] = (float)(-ui[5]);
+  }
+}
+
+// the body with the narrowest dual width that holds a group of nd <= CAP
+// directions
+template <bool STEP, int CAP, int NC>
+__device__ __forceinline__ void beam_grad_fit(const DModel& M, const BGArgs& A, int64_t b, int g0, int nd,
+                                              double (&contrib)[NC]) {
+  if constexpr (CAP <= 1) {
+    beam_grad_body<1, STEP>(M, A, b, g0, nd, contrib);
+  } else if constexpr (CAP == 2) {
+    if (nd <= 1) beam_grad_body<1, STEP>(M, A, b, g0, nd, contrib);
+    else beam_grad_body<2, STEP>(M, A, b, g0, nd, contrib);
+  } else {
+    if (nd <= 1) beam_grad_body<1, STEP>(M, A, b, g0, nd, contrib);
+    else if (nd == 2) beam_grad_body<2, STEP>(M, A, b, g0, nd, contrib);
+    else if (nd == 3 || CAP == 3) beam_grad_body<3, STEP>(M, A, b, g0, nd, contrib);
+    else beam_grad_body<CAP, STEP>(M, A, b, g0, nd, contrib);
+  }
+}
+
+// ND: directions carried by a thread; the launch's direction groups run on
+// blockIdx.y (fewer directions a thread keep the dual numbers small enough
+// for registers, at the cost of recomputing the values once per group).
+template <int ND>
+__global__ void __launch_bounds__(kBGThreads)
+k_field_beam_grad(const __grid_constant__ DModel M, const __grid_constant__ BGArgs A) {
+  __shared__ double red[kBGThreads][ND];
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int g0 = A.group_first[blockIdx.y], nd = A.group_n[blockIdx.y];  // this group's directions
+  double contrib[ND];
+#pragma unroll
+  for (int d = 0; d < ND; ++d) contrib[d] = 0.0;
+  bool step = false;  // the same for the whole block
+  for (int d = 0; d < nd; ++d)
+    if (A.dir_kind[g0 + d] == DIR_STEP) step = true;
+  if (b < A.n) {
+    // the dual width that fits the group: fewer directions, shorter chains
+    if (step)
+      beam_grad_fit<true, kBGStepDirs>(M, A, b, g0, nd, contrib);
+    else
+      beam_grad_fit<false, kBGRayDirs>(M, A, b, g0, nd, contrib);
   }
   // the block's sums of the model directions, in a fixed order
 #pragma unroll
   for (int d = 0; d < ND; ++d)
-    red[threadIdx.x][d] = (g0 + d < A.n_dir && A.dir_kind[g0 + d] == DIR_STEP) ? contrib[d] : 0.0;
+    red[threadIdx.x][d] = (d < nd && A.dir_kind[g0 + d] == DIR_STEP) ? contrib[d] : 0.0;
   __syncthreads();
   for (int s = kBGThreads / 2; s > 0; s >>= 1) {
     if ((int)threadIdx.x < s)
@@ -564,7 +628,7 @@ k_field_beam_grad(const __grid_constant__ DModel M, const __grid_constant__ BGAr
       for (int d = 0; d < ND; ++d) red[threadIdx.x][d] += red[threadIdx.x + s][d];
     __syncthreads();
   }
-  if ((int)threadIdx.x < ND && g0 + (int)threadIdx.x < A.n_dir && A.model_part)
+  if ((int)threadIdx.x < nd && A.model_part)
     A.model_part[(size_t)(g0 + threadIdx.x) * gridDim.x + blockIdx.x] = red[0][threadIdx.x];
 }
 
@@ -941,7 +1005,24 @@ static int field_vjp_impl(const tg_model* model, const tg_beams* beams, const tg
       B.gamp = out->amplitude;
     }
     B.model_part = mpart;
-    const int groups = B.n_dir > 0 ? (B.n_dir + kBGDirs - 1) / kBGDirs : 1;
+    // groups: the central ray's four directions together, the model's steps
+    // kBGStepDirs at a time (a group never mixes the two kinds)
+    int groups = 0;
+    for (int d = 0; d < B.n_dir;) {
+      const bool st = B.dir_kind[d] == DIR_STEP;
+      const int cap = st ? kBGStepDirs : kBGRayDirs;
+      int e = d;
+      while (e < B.n_dir && e - d < cap && (B.dir_kind[e] == DIR_STEP) == st) ++e;
+      B.group_first[groups] = d;
+      B.group_n[groups] = e - d;
+      ++groups;
+      d = e;
+    }
+    if (groups == 0) {  // no directions: the pathlength and amplitude gradients only
+      B.group_first[0] = 0;
+      B.group_n[0] = 0;
+      groups = 1;
+    }
     k_field_beam_grad<kBGDirs><<<dim3(L.bg_blocks, groups), kBGThreads, 0, s>>>(dm, B);
     if (any_model && out->raw) {
       S.n_dir = B.n_dir;
