@@ -182,13 +182,22 @@ __global__ void __launch_bounds__(kMThreads, 3) k_field_moments(const __grid_con
 }
 
 // moments[b][i] = sum over the blocks' partials in block order (float64)
+// The sum is carried as an unevaluated float32 pair (TwoSum per partial,
+// exact to ~2^-48 of the terms) and rounded to float64 once with integer
+// operations: no float64 instruction, which GB300 issues at ~1/64 of the
+// float32 rate.
 __global__ void k_field_moment_sum(const float* __restrict__ part, int nparts, int64_t n,
                                    double* __restrict__ mom) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n * 12) return;
-  double a = 0.0;
-  for (int p = 0; p < nparts; ++p) a += (double)part[(size_t)p * n * 12 + i];
-  mom[i] = a;
+  float hi = 0.f, lo = 0.f;
+  for (int p = 0; p < nparts; ++p) {
+    const float v = part[(size_t)p * n * 12 + i];
+    const float s = __fadd_rn(hi, v), bb = __fsub_rn(s, hi);
+    lo = __fadd_rn(lo, __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(v, bb)));
+    hi = s;
+  }
+  mom[i] = add_f64_f32(f32_to_f64(hi), lo);
 }
 
 // ------------------------------------------------------------ dual numbers
@@ -638,13 +647,17 @@ struct ModelSumArgs {
   int32_t target[kBGLaunchDirs];  // index into raw (step * 4 + slot), -1 = none
 };
 
+// One warp per direction: lane l adds blocks l, l + 32, ... in order, then a
+// fixed shuffle tree (deterministic, independent of timing).
 __global__ void k_field_model_sum(const double* __restrict__ part, const __grid_constant__ ModelSumArgs A,
                                   double* __restrict__ raw) {
-  const int d = threadIdx.x;
-  if (d >= A.n_dir || A.target[d] < 0) return;
+  const int d = blockIdx.x, lane = threadIdx.x;
+  if (d >= A.n_dir || A.target[d] < 0) return;  // uniform over the warp
   double a = 0.0;
-  for (int bk = 0; bk < A.blocks; ++bk) a += part[(size_t)d * A.blocks + bk];
-  raw[A.target[d]] = a;
+  for (int bk = lane; bk < A.blocks; bk += 32) a += part[(size_t)d * A.blocks + bk];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+  if (lane == 0) raw[A.target[d]] = a;
 }
 
 // ------------------------------------------- separable moments (tensor cores)
@@ -1027,7 +1040,7 @@ static int field_vjp_impl(const tg_model* model, const tg_beams* beams, const tg
     if (any_model && out->raw) {
       S.n_dir = B.n_dir;
       S.blocks = L.bg_blocks;
-      k_field_model_sum<<<1, kBGLaunchDirs, 0, s>>>(mpart, S, out->raw);
+      k_field_model_sum<<<B.n_dir, 32, 0, s>>>(mpart, S, out->raw);
     }
   }
   return cudaGetLastError() == cudaSuccess ? TG_OK : TG_ERR_CUDA;
