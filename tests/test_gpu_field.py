@@ -134,6 +134,27 @@ def test_ragged_beams_and_detectors(n, shape, cuda):
     assert t._native.error_word() == 0
 
 
+def test_zero_beams_field_and_adjoint(cuda):
+    """No beams: every method returns a zero image; the adjoint returns empty
+    per-beam gradients and zero per-step sums (the reference's chunked sum
+    over an empty beam set is the zero image)."""
+    import temgymcore_gb300 as t
+    from temgymcore_gb300.workloads import build_model, gaussian_rays
+    w = _small(False, n=8, shape=(9, 11))
+    rays0 = {k: (v[:0] if isinstance(v, np.ndarray) and v.ndim >= 1 and v.shape[0] == 8 else v)
+             for k, v in w["rays"].items()}
+    plan = t.FieldPlan(gaussian_rays(rays0), build_model(w["model"]))
+    for meth in ("direct", "separable", "fp64"):
+        img = _np(plan.evaluate(meth))
+        assert img.shape == (9, 11) and not np.any(img), meth
+    for meth in ("direct", "separable"):
+        g = plan.vjp(torch.ones(plan.shape, dtype=torch.complex64, device=cuda), method=meth)
+        for k in ("amplitude", "pathlength", "x", "y", "dx", "dy"):
+            assert g[k].numel() == 0, (meth, k)
+        assert not torch.any(g["raw"]), meth
+    assert t._native.error_word() == 0
+
+
 def test_separable_rejects_astigmatic_beams(cuda):
     import temgymcore_gb300 as t
     from temgymcore_gb300.workloads import build_model, gaussian_rays
