@@ -26,8 +26,9 @@
 //      with the moments.  The directions (the central ray's x, y, dx, dy and
 //      the model's step parameters, up to 32 a launch) run in groups on
 //      blockIdx.y: the central ray's four together, whose group computes the
-//      ABCD algebra without dual parts (it does not depend on the ray), and
-//      the step parameters two at a time;
+//      ABCD algebra in plain float64 (it does not depend on the ray) and the
+//      derivatives of the few ray-dependent terms in closed form, and the
+//      step parameters two at a time;
 //   4. k_field_model_sum: the model parameters' per-block sums in a fixed
 //      order, written as per-step sums in the layout of tg_trace_vjp.
 // Every reduction runs in a fixed order, so the gradients are deterministic.
@@ -320,9 +321,10 @@ __device__ __forceinline__ M2<N> nan0(const M2<N>& m) {
 // groups in one launch (blockIdx.y) 0.90 ms; the central-ray group without
 // dual parts in the matrix algebra 0.82 ms; step groups carried at the
 // narrowest width that holds them 0.76 ms, and at most 2 step directions a
-// group 0.73 ms (1: 0.78; the central ray in groups of 2: 0.76).  Results
-// are bit-identical across these layouts.  The kernel takes 255 registers,
-// so an SM holds 8 of its warps.
+// group 0.73 ms (1: 0.78; the central ray in groups of 2: 0.76); the
+// central ray's group in closed form (beam_grad_ray) 0.69 ms.  Results are
+// bit-identical across these layouts.  The kernel takes 255 registers, so
+// an SM holds 8 of its warps, and it keeps the float64 pipe ~86 % busy.
 constexpr int kBGThreads = 64;
 constexpr int kBGDirs = 4;          // directions a thread carries (at most)
 constexpr int kBGRayDirs = 4;       // central-ray directions a thread carries
@@ -586,6 +588,181 @@ __device__ __forceinline__ void beam_grad_body(const DModel& M, const BGArgs& A,
   }
 }
 
+// The central ray's group (x, y, dx, dy): the ABCD algebra does not depend
+// on the ray, so S (= Q2, or Q1^-1 in the input plane), B^-1, P and the
+// prefactor are constants and only L, c0 (and, in the input plane, s0 = r -
+// r1m) carry derivatives.  Their partial derivatives with respect to each
+// ray coordinate are written out (float64, no dual numbers), which is about
+// a third of the float64 work of carrying four dual directions through the
+// whole polynomial.
+template <int NC>
+__device__ __forceinline__ void beam_grad_ray(const DModel& M, const BGArgs& A, int64_t b, int g0, int nd,
+                                              double (&contrib)[NC]) {
+  using XP = Cx<0>;
+  auto cr = [](double v) { return cx_<0>(v, 0.0); };
+  const double x0 = A.x[b], y0 = A.y[b], dx0 = A.dx[b], dy0 = A.dy[b];
+  const double PI = 3.141592653589793;
+  const double wl = A.wl ? A.wl[b] : A.wl_scalar;
+  const double k = 2.0 * PI / wl, hk = 0.5 * k;
+  const double wx = A.waist[2 * b], wy = A.waist[2 * b + 1];
+  const double Rx = A.radii[2 * b], Ry = A.radii[2 * b + 1];
+  const double qxr = isinf(Rx) ? 0.0 : -1.0 / Rx, qxi = wl / (PI * wx * wx);
+  const double qyr = isinf(Ry) ? 0.0 : -1.0 / Ry, qyi = wl / (PI * wy * wy);
+  const double th = A.theta ? A.theta[b] : 0.0;
+  double sth, cth;
+  sincos(th, &sth, &cth);
+  const M2<0> Q1i{cx_<0>(cth * cth * qxr + sth * sth * qyr, cth * cth * qxi + sth * sth * qyi),
+                  cx_<0>(cth * sth * (qxr - qyr), cth * sth * (qxi - qyi)),
+                  cx_<0>(cth * sth * (qxr - qyr), cth * sth * (qxi - qyi)),
+                  cx_<0>(sth * sth * qxr + cth * cth * qyr, sth * sth * qxi + cth * cth * qyi)};
+  XP Sxx, Syy, Sxy;
+  XP Lx, Ly;              // values (used in the input plane, where s0 moves with the ray)
+  XP dLx[4], dLy[4], dc0[4];
+  double ds0x[4], ds0y[4];  // d s0 / d (x, y, dx, dy)
+  double ox, oy;
+  if (A.input_plane) {  // gaussian.py:402-409: s = r1 - r1m, S = Q1^-1, L = 2 theta1m
+    Sxx = Q1i.a;
+    Syy = Q1i.d;
+    Sxy = 0.5 * (Q1i.b + Q1i.c);
+    Lx = cr(2.0 * dx0);
+    Ly = cr(2.0 * dy0);
+    for (int c = 0; c < 4; ++c) {
+      dLx[c] = cr(c == 2 ? 2.0 : 0.0);
+      dLy[c] = cr(c == 3 ? 2.0 : 0.0);
+      dc0[c] = cr(0.0);
+      ds0x[c] = c == 0 ? -1.0 : 0.0;
+      ds0y[c] = c == 1 ? -1.0 : 0.0;
+    }
+    ox = x0;
+    oy = y0;
+  } else {
+    double x = x0, y = y0, dx = dx0, dy = dy0;  // the central ray, for the biprism's sign
+    double m[5][5];
+    for (int i = 0; i < 5; ++i)
+      for (int j = 0; j < 5; ++j) m[i][j] = i == j ? 1.0 : 0.0;
+    for (int s = 0; s < M.n; ++s) {
+      const DStep& st = M.s[s];
+      switch (st.kind) {
+        case D_FREE:
+          for (int j = 0; j < 5; ++j) {
+            m[0][j] = m[0][j] + st.a[0] * m[2][j];
+            m[1][j] = m[1][j] + st.a[0] * m[3][j];
+          }
+          x += dx * st.a[0];
+          y += dy * st.a[0];
+          break;
+        case D_LENS:
+          for (int j = 0; j < 5; ++j) {
+            m[2][j] = m[2][j] - m[0][j] * st.a[1];
+            m[3][j] = m[3][j] - m[1][j] * st.a[1];
+          }
+          dx -= x * st.a[1];
+          dy -= y * st.a[1];
+          break;
+        case D_SHIFT:
+          m[0][4] += st.a[0]; m[1][4] += st.a[1]; m[2][4] += st.a[2]; m[3][4] += st.a[3];
+          x += st.a[0]; y += st.a[1]; dx += st.a[2]; dy += st.a[3];
+          break;
+        case D_BIPRISM: {
+          const double sg = x > 0.0 ? 1.0 : (x < 0.0 ? -1.0 : 0.0);
+          m[2][4] += sg * st.a[0];
+          dx += sg * st.a[0];
+        } break;
+        case D_ROTATE: {
+          const double c = st.a[0], sn = st.a[1];
+          for (int j = 0; j < 5; ++j) {
+            const double r0 = m[0][j], r1 = m[1][j], r2 = m[2][j], r3 = m[3][j];
+            m[0][j] = c * r0 - sn * r1;
+            m[1][j] = sn * r0 + c * r1;
+            m[2][j] = c * r2 - sn * r3;
+            m[3][j] = sn * r2 + c * r3;
+          }
+          const double nx = c * x - sn * y, ny = sn * x + c * y;
+          const double ndx = c * dx - sn * dy, ndy = sn * dx + c * dy;
+          x = nx; y = ny; dx = ndx; dy = ndy;
+        } break;
+        default:
+          break;
+      }
+    }
+    const M2<0> Am{cr(m[0][0]), cr(m[0][1]), cr(m[1][0]), cr(m[1][1])};
+    const M2<0> Bm{cr(m[0][2]), cr(m[0][3]), cr(m[1][2]), cr(m[1][3])};
+    const M2<0> Cm{cr(m[2][0]), cr(m[2][1]), cr(m[3][0]), cr(m[3][1])};
+    const M2<0> Dm{cr(m[2][2]), cr(m[2][3]), cr(m[3][2]), cr(m[3][3])};
+    const M2<0> Q2 = inv2(Am + Bm * Q1i) * (Cm + Dm * Q1i);
+    const M2<0> Binv = nan0(inv2(Bm));
+    const M2<0> Q1 = nan0(inv2(Q1i));
+    const M2<0> AB = Am * Binv;
+    const M2<0> P = Q1 * inv2(Bm * (Am * Q1 + Bm));
+    Sxx = Q2.a;
+    Syy = Q2.d;
+    Sxy = 0.5 * (Q2.b + Q2.c);
+    const double r2mx = m[0][0] * x0 + m[0][1] * y0 + m[0][2] * dx0 + m[0][3] * dy0;
+    const double r2my = m[1][0] * x0 + m[1][1] * y0 + m[1][2] * dx0 + m[1][3] * dy0;
+    const XP abx = AB.a * cr(x0) + AB.b * cr(y0), aby = AB.c * cr(x0) + AB.d * cr(y0);
+    const XP pmx = P.a * cr(r2mx) + P.b * cr(r2my), pmy = P.c * cr(r2mx) + P.d * cr(r2my);
+    for (int c = 0; c < 4; ++c) {
+      const double ex = c == 0 ? 1.0 : 0.0, ey = c == 1 ? 1.0 : 0.0;  // d (x0, y0)
+      const double erx = m[0][c], ery = m[1][c];                      // d (r2mx, r2my)
+      // L = 2 (m[2..3][4] - B^-1^T r1m + P^T r2m): the first part is constant
+      const XP dbx = Binv.a * cr(ex) + Binv.c * cr(ey), dby = Binv.b * cr(ex) + Binv.d * cr(ey);
+      const XP dpx = P.a * cr(erx) + P.c * cr(ery), dpy = P.b * cr(erx) + P.d * cr(ery);
+      dLx[c] = 2.0 * (dpx - dbx);
+      dLy[c] = 2.0 * (dpy - dby);
+      // c0 = r1m^T (A B^-1) r1m - r2m^T P r2m
+      const XP dq1 = cr(ex) * abx + cr(x0) * (AB.a * cr(ex) + AB.b * cr(ey)) + cr(ey) * aby +
+                     cr(y0) * (AB.c * cr(ex) + AB.d * cr(ey));
+      const XP dq2 = cr(erx) * pmx + cr(r2mx) * (P.a * cr(erx) + P.b * cr(ery)) + cr(ery) * pmy +
+                     cr(r2my) * (P.c * cr(erx) + P.d * cr(ery));
+      dc0[c] = dq1 - dq2;
+      ds0x[c] = 0.0;
+      ds0y[c] = 0.0;
+    }
+    Lx = cr(0.0);  // enters only with d s0, which is zero here
+    Ly = cr(0.0);
+    ox = m[0][4];
+    oy = m[1][4];
+  }
+  const double s0x = A.pm.t[5] - ox, s0y = A.pm.t[2] - oy;
+  const double ux = A.pm.t[3], uy = A.pm.t[0], vx = A.pm.t[4], vy = A.pm.t[1];
+  auto quad = [&](double ax, double ay, double bx2, double by2) -> XP {  // a^T S b
+    return (ax * bx2) * Sxx + (ay * by2) * Syy + (ax * by2 + ay * bx2) * Sxy;
+  };
+  // moments about the envelope centre -> moments of the monomials col, row, 1
+  const double* mo = A.mom + b * 12;
+  const double r0 = (double)A.rec[b].r0, cc0 = (double)A.rec[b].c0;
+  const double ur3 = mo[2] + cc0 * mo[0], ui3 = mo[3] + cc0 * mo[1];
+  const double ur4 = mo[4] + r0 * mo[0], ui4 = mo[5] + r0 * mo[1];
+  const double ur5 = mo[0], ui5 = mo[1];
+  const double ar = (double)A.amp[2 * b], ai = (double)A.amp[2 * b + 1];
+  const double wr3 = ar * ur3 - ai * ui3, wi3 = ar * ui3 + ai * ur3;
+  const double wr4 = ar * ur4 - ai * ui4, wi4 = ar * ui4 + ai * ur4;
+  const double wr5 = ar * ur5 - ai * ui5, wi5 = ar * ui5 + ai * ur5;
+  // dL/dp = -sum_j Im(dkap_j w_j) over j = col, row, 1 (kap_cc, kap_rr,
+  // kap_rc and the prefactor do not move with the central ray)
+  for (int d = 0; d < nd && d < NC; ++d) {
+    const int kd = A.dir_kind[g0 + d];
+    if (kd < DIR_X || kd > DIR_DY) continue;
+    const int c = kd;  // DIR_X .. DIR_DY = 0 .. 3
+    const XP k3 = hk * (2.0 * quad(ds0x[c], ds0y[c], vx, vy) + vx * dLx[c] + vy * dLy[c]);
+    const XP k4 = hk * (2.0 * quad(ds0x[c], ds0y[c], ux, uy) + ux * dLx[c] + uy * dLy[c]);
+    const XP k5 = hk * (2.0 * quad(ds0x[c], ds0y[c], s0x, s0y) + ds0x[c] * Lx + ds0y[c] * Ly + s0x * dLx[c] +
+                        s0y * dLy[c] + dc0[c]);
+    const double g = -(k3.re.v * wi3 + k3.im.v * wr3) - (k4.re.v * wi4 + k4.im.v * wr4) -
+                     (k5.re.v * wi5 + k5.im.v * wr5);
+    contrib[d] = g;
+    if (kd == DIR_X && A.gx) A.gx[b] = g;
+    if (kd == DIR_Y && A.gy) A.gy[b] = g;
+    if (kd == DIR_DX && A.gdx) A.gdx[b] = g;
+    if (kd == DIR_DY && A.gdy) A.gdy[b] = g;
+  }
+  if (A.gpl && blockIdx.y == 0) A.gpl[b] = -k * wi5;
+  if (A.gamp && blockIdx.y == 0) {
+    A.gamp[2 * b] = (float)ur5;
+    A.gamp[2 * b + 1] = (float)(-ui5);
+  }
+}
+
 // the body with the narrowest dual width that holds a group of nd <= CAP
 // directions
 template <bool STEP, int CAP, int NC>
@@ -624,7 +801,7 @@ k_field_beam_grad(const __grid_constant__ DModel M, const __grid_constant__ BGAr
     if (step)
       beam_grad_fit<true, kBGStepDirs>(M, A, b, g0, nd, contrib);
     else
-      beam_grad_fit<false, kBGRayDirs>(M, A, b, g0, nd, contrib);
+      beam_grad_ray(M, A, b, g0, nd, contrib);
   }
   // the block's sums of the model directions, in a fixed order
 #pragma unroll
