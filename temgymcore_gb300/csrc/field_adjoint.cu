@@ -36,6 +36,7 @@
 
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "field_common.cuh"
@@ -313,6 +314,33 @@ __device__ __forceinline__ M2<N> nan0(const M2<N>& m) {
   return M2<N>{f(m.a), f(m.b), f(m.c), f(m.d)};
 }
 
+// Products with a constant (N = 0) factor: a dual times a plain value costs
+// N + 1 multiplies instead of 2N + 1 (float64 is the adjoint's bound).
+template <int N, typename = std::enable_if_t<(N > 0)>>
+__device__ __forceinline__ Du<N> operator*(const Du<N>& a, const Du<0>& b) {
+  return b.v * a;
+}
+template <int N, typename = std::enable_if_t<(N > 0)>>
+__device__ __forceinline__ Du<N> operator*(const Du<0>& a, const Du<N>& b) {
+  return a.v * b;
+}
+template <int N, typename = std::enable_if_t<(N > 0)>>
+__device__ __forceinline__ Cx<N> operator*(const Cx<N>& a, const Cx<0>& b) {
+  return Cx<N>{a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+template <int N, typename = std::enable_if_t<(N > 0)>>
+__device__ __forceinline__ Cx<N> operator*(const Cx<0>& a, const Cx<N>& b) {
+  return Cx<N>{a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+template <int N, typename = std::enable_if_t<(N > 0)>>
+__device__ __forceinline__ M2<N> operator*(const M2<N>& x, const M2<0>& y) {
+  return M2<N>{x.a * y.a + x.b * y.c, x.a * y.b + x.b * y.d, x.c * y.a + x.d * y.c, x.c * y.b + x.d * y.d};
+}
+template <int N, typename = std::enable_if_t<(N > 0)>>
+__device__ __forceinline__ M2<N> operator*(const M2<0>& x, const M2<N>& y) {
+  return M2<N>{x.a * y.a + x.b * y.c, x.a * y.b + x.b * y.d, x.c * y.a + x.d * y.c, x.c * y.b + x.d * y.d};
+}
+
 // ------------------------------------------------------------ beam gradient
 // Direction groups, 64 threads a block.  Measured on the separable
 // 16,384-beam adjoint (whole call; Lens + Detector: the central ray's four
@@ -322,9 +350,11 @@ __device__ __forceinline__ M2<N> nan0(const M2<N>& m) {
 // dual parts in the matrix algebra 0.82 ms; step groups carried at the
 // narrowest width that holds them 0.76 ms, and at most 2 step directions a
 // group 0.73 ms (1: 0.78; the central ray in groups of 2: 0.76); the
-// central ray's group in closed form (beam_grad_ray) 0.69 ms.  Results are
-// bit-identical across these layouts.  The kernel takes 255 registers, so
-// an SM holds 8 of its warps, and it keeps the float64 pipe ~86 % busy.
+// central ray's group in closed form (beam_grad_ray) 0.69 ms, bit-identical
+// across these layouts; the step groups with their constant factors (Q1,
+// Q1^-1, the central ray, the pixel map) as plain values 0.65 ms.  The
+// kernel takes 254 registers, so an SM holds 8 of its warps, and it keeps
+// the float64 pipe ~86 % busy.
 constexpr int kBGThreads = 64;
 constexpr int kBGDirs = 4;          // directions a thread carries (at most)
 constexpr int kBGRayDirs = 4;       // central-ray directions a thread carries
@@ -383,15 +413,9 @@ __device__ __forceinline__ void beam_grad_body(const DModel& M, const BGArgs& A,
   using D = Du<ND>;
   using X = Cx<ND>;
   using DM = Du<NM>;
-  D x0 = dc_<ND>(A.x[b]), y0 = dc_<ND>(A.y[b]), dx0 = dc_<ND>(A.dx[b]), dy0 = dc_<ND>(A.dy[b]);
-#pragma unroll
-  for (int d = 0; d < ND; ++d) {
-    if (d >= nd) break;
-    if (A.dir_kind[g0 + d] == DIR_X) x0.d[d] = 1.0;
-    if (A.dir_kind[g0 + d] == DIR_Y) y0.d[d] = 1.0;
-    if (A.dir_kind[g0 + d] == DIR_DX) dx0.d[d] = 1.0;
-    if (A.dir_kind[g0 + d] == DIR_DY) dy0.d[d] = 1.0;
-  }
+  // a step group carries no central-ray direction (beam_grad_ray takes
+  // those): the central ray and Q1 are constants here
+  const double x0 = A.x[b], y0 = A.y[b], dx0 = A.dx[b], dy0 = A.dy[b];
   const double PI = 3.141592653589793;
   const double wl = A.wl ? A.wl[b] : A.wl_scalar;
   const double k = 2.0 * PI / wl, hk = 0.5 * k;
@@ -403,10 +427,10 @@ __device__ __forceinline__ void beam_grad_body(const DModel& M, const BGArgs& A,
   const double th = A.theta ? A.theta[b] : 0.0;
   double sth, cth;
   sincos(th, &sth, &cth);
-  const M2<NM> Q1i{cx_<NM>(cth * cth * qxr + sth * sth * qyr, cth * cth * qxi + sth * sth * qyi),
-                   cx_<NM>(cth * sth * (qxr - qyr), cth * sth * (qxi - qyi)),
-                   cx_<NM>(cth * sth * (qxr - qyr), cth * sth * (qxi - qyi)),
-                   cx_<NM>(sth * sth * qxr + cth * cth * qyr, sth * sth * qxi + cth * cth * qyi)};
+  const M2<0> Q1i{cx_<0>(cth * cth * qxr + sth * sth * qyr, cth * cth * qxi + sth * sth * qyi),
+                  cx_<0>(cth * sth * (qxr - qyr), cth * sth * (qxi - qyi)),
+                  cx_<0>(cth * sth * (qxr - qyr), cth * sth * (qxi - qyi)),
+                  cx_<0>(sth * sth * qxr + cth * cth * qyr, sth * sth * qxi + cth * cth * qyi)};
   X Sxx, Syy, Sxy, Lx, Ly, c0;
   D ox, oy;
   X dlp = cx_<ND>(0.0, 0.0);  // d log pref as a complex dual (its derivative parts are used)
@@ -414,15 +438,15 @@ __device__ __forceinline__ void beam_grad_body(const DModel& M, const BGArgs& A,
     Sxx = lift<ND>(Q1i.a);
     Syy = lift<ND>(Q1i.d);
     Sxy = lift<ND>(0.5 * (Q1i.b + Q1i.c));
-    Lx = cx_<ND>(2.0 * dx0);
-    Ly = cx_<ND>(2.0 * dy0);
+    Lx = cx_<ND>(2.0 * dx0, 0.0);
+    Ly = cx_<ND>(2.0 * dy0, 0.0);
     c0 = cx_<ND>(0.0, 0.0);
-    ox = x0;
-    oy = y0;
+    ox = dc_<ND>(x0);
+    oy = dc_<ND>(y0);
   } else {
     // central ray and 5x5 ABCD (rows x, y, dx, dy, 1) with the model's
     // step parameters as directions
-    double x = x0.v, y = y0.v, dx = dx0.v, dy = dy0.v;
+    double x = x0, y = y0, dx = dx0, dy = dy0;
     DM m[5][5];
 #pragma unroll
     for (int i = 0; i < 5; ++i)
@@ -499,9 +523,9 @@ __device__ __forceinline__ void beam_grad_body(const DModel& M, const BGArgs& A,
     const M2<NM> denom = Am + Bm * Q1i;
     const M2<NM> Q2 = inv2(denom) * (Cm + Dm * Q1i);
     const M2<NM> Binv = nan0(inv2(Bm));
-    const M2<NM> Q1 = nan0(inv2(Q1i));
-    const D r2mx = lift<ND>(m[0][0]) * x0 + lift<ND>(m[0][1]) * y0 + lift<ND>(m[0][2]) * dx0 + lift<ND>(m[0][3]) * dy0;
-    const D r2my = lift<ND>(m[1][0]) * x0 + lift<ND>(m[1][1]) * y0 + lift<ND>(m[1][2]) * dx0 + lift<ND>(m[1][3]) * dy0;
+    const M2<0> Q1 = nan0(inv2(Q1i));
+    const D r2mx = x0 * lift<ND>(m[0][0]) + y0 * lift<ND>(m[0][1]) + dx0 * lift<ND>(m[0][2]) + dy0 * lift<ND>(m[0][3]);
+    const D r2my = x0 * lift<ND>(m[1][0]) + y0 * lift<ND>(m[1][1]) + dx0 * lift<ND>(m[1][2]) + dy0 * lift<ND>(m[1][3]);
     // pref = amp / sqrt(det): d log pref = -d det / (2 det)
     if constexpr (STEP) {
       const Cx<NM> det = denom.a * denom.d - denom.b * denom.c;
@@ -517,14 +541,14 @@ __device__ __forceinline__ void beam_grad_body(const DModel& M, const BGArgs& A,
     Sxx = lift<ND>(Q2.a);
     Syy = lift<ND>(Q2.d);
     Sxy = lift<ND>(0.5 * (Q2.b + Q2.c));
-    const X bx = lift<ND>(Binv.a) * cx_<ND>(x0) + lift<ND>(Binv.c) * cx_<ND>(y0);
-    const X by = lift<ND>(Binv.b) * cx_<ND>(x0) + lift<ND>(Binv.d) * cx_<ND>(y0);
+    const X bx = x0 * lift<ND>(Binv.a) + y0 * lift<ND>(Binv.c);
+    const X by = x0 * lift<ND>(Binv.b) + y0 * lift<ND>(Binv.d);
     const X px = lift<ND>(P.a) * cx_<ND>(r2mx) + lift<ND>(P.c) * cx_<ND>(r2my);
     const X py = lift<ND>(P.b) * cx_<ND>(r2mx) + lift<ND>(P.d) * cx_<ND>(r2my);
     Lx = 2.0 * (cx_<ND>(lift<ND>(m[2][4])) - bx + px);
     Ly = 2.0 * (cx_<ND>(lift<ND>(m[3][4])) - by + py);
-    const X q1 = cx_<ND>(x0) * (lift<ND>(ABinv.a) * cx_<ND>(x0) + lift<ND>(ABinv.b) * cx_<ND>(y0)) +
-                 cx_<ND>(y0) * (lift<ND>(ABinv.c) * cx_<ND>(x0) + lift<ND>(ABinv.d) * cx_<ND>(y0));
+    const X q1 = x0 * (x0 * lift<ND>(ABinv.a) + y0 * lift<ND>(ABinv.b)) +
+                 y0 * (x0 * lift<ND>(ABinv.c) + y0 * lift<ND>(ABinv.d));
     const X q2 = cx_<ND>(r2mx) * (lift<ND>(P.a) * cx_<ND>(r2mx) + lift<ND>(P.b) * cx_<ND>(r2my)) +
                  cx_<ND>(r2my) * (lift<ND>(P.c) * cx_<ND>(r2mx) + lift<ND>(P.d) * cx_<ND>(r2my));
     c0 = q1 - q2;
@@ -534,17 +558,23 @@ __device__ __forceinline__ void beam_grad_body(const DModel& M, const BGArgs& A,
   // the polynomial in (row, col): s = s0 + row u + col v
   const D s0x = dc_<ND>(A.pm.t[5]) - ox, s0y = dc_<ND>(A.pm.t[2]) - oy;
   const double ux = A.pm.t[3], uy = A.pm.t[0], vx = A.pm.t[4], vy = A.pm.t[1];
-  auto quad = [&](const D& ax, const D& ay, const D& bx2, const D& by2) -> X {  // a^T S b
+  // a^T S b with constant a and b, with a dual and b constant, with both dual
+  auto quad_cc = [&](double ax, double ay, double bx2, double by2) -> X {
     return (ax * bx2) * Sxx + (ay * by2) * Syy + (ax * by2 + ay * bx2) * Sxy;
   };
-  const D U0 = dc_<ND>(ux), U1 = dc_<ND>(uy), V0 = dc_<ND>(vx), V1 = dc_<ND>(vy);
+  auto quad_dc = [&](const D& ax, const D& ay, double bx2, double by2) -> X {
+    return (bx2 * ax) * Sxx + (by2 * ay) * Syy + (by2 * ax + bx2 * ay) * Sxy;
+  };
+  auto quad_dd = [&](const D& ax, const D& ay, const D& bx2, const D& by2) -> X {
+    return (ax * bx2) * Sxx + (ay * by2) * Syy + (ax * by2 + ay * bx2) * Sxy;
+  };
   X kap[6];  // cc, rr, rc, c, r, 0
-  kap[0] = hk * quad(V0, V1, V0, V1);
-  kap[1] = hk * quad(U0, U1, U0, U1);
-  kap[2] = hk * (2.0 * quad(U0, U1, V0, V1));
-  kap[3] = hk * (2.0 * quad(s0x, s0y, V0, V1) + V0 * Lx + V1 * Ly);
-  kap[4] = hk * (2.0 * quad(s0x, s0y, U0, U1) + U0 * Lx + U1 * Ly);
-  kap[5] = hk * (quad(s0x, s0y, s0x, s0y) + s0x * Lx + s0y * Ly + c0);
+  kap[0] = hk * quad_cc(vx, vy, vx, vy);
+  kap[1] = hk * quad_cc(ux, uy, ux, uy);
+  kap[2] = hk * (2.0 * quad_cc(ux, uy, vx, vy));
+  kap[3] = hk * (2.0 * quad_dc(s0x, s0y, vx, vy) + vx * Lx + vy * Ly);
+  kap[4] = hk * (2.0 * quad_dc(s0x, s0y, ux, uy) + ux * Lx + uy * Ly);
+  kap[5] = hk * (quad_dd(s0x, s0y, s0x, s0y) + s0x * Lx + s0y * Ly + c0);
   // moments about the envelope centre -> moments of the monomials
   const double* mo = A.mom + b * 12;
   const double r0 = (double)A.rec[b].r0, cc0 = (double)A.rec[b].c0;
