@@ -385,36 +385,18 @@ struct BGArgs {
   double* model_part;           // [direction][gridDim.x] sums over the block's beams (DIR_STEP)
 };
 
-// lift a value with NM derivative directions to ND (zeros when NM = 0)
-template <int ND, int NM>
-__device__ __forceinline__ Du<ND> lift(const Du<NM>& a) {
-  if constexpr (NM == ND) {
-    return a;
-  } else {
-    return dc_<ND>(a.v);
-  }
-}
-template <int ND, int NM>
-__device__ __forceinline__ Cx<ND> lift(const Cx<NM>& a) {
-  return Cx<ND>{lift<ND>(a.re), lift<ND>(a.im)};
-}
-
-// One beam's contributions along directions [g0, g0 + ND) of the launch.
-// STEP: the group carries model-step directions, so the ABCD matrices, Q2,
-// the prefactor and everything built from them carry derivatives; without
-// them (the central ray's x, y, dx, dy) those quantities are constants and
-// are computed without dual parts (NM = 0), and only the terms that hold
-// the central ray carry the ND directions.  The propagated central ray is
-// needed by value only (the biprism's sign).
-template <int ND, bool STEP, int NC>
-__device__ __forceinline__ void beam_grad_body(const DModel& M, const BGArgs& A, int64_t b, int g0, int nd,
+// One beam's contributions along the model-step directions [g0, g0 + nd)
+// of the launch (nd <= ND): the ABCD matrices, Q2, B^-1, P, the prefactor
+// and everything built from them carry ND dual directions; Q1, Q1^-1, the
+// central ray and the pixel map are constants, so their products with duals
+// cost N + 1 float64 multiplies.  The propagated central ray is needed by
+// value only (the biprism's sign).  Step groups exist only for the detector
+// field: the input-plane field has no model (the host rejects its step sums).
+template <int ND, int NC>
+__device__ __forceinline__ void beam_grad_step(const DModel& M, const BGArgs& A, int64_t b, int g0, int nd,
                                                double (&contrib)[NC]) {
-  constexpr int NM = STEP ? ND : 0;
   using D = Du<ND>;
   using X = Cx<ND>;
-  using DM = Du<NM>;
-  // a step group carries no central-ray direction (beam_grad_ray takes
-  // those): the central ray and Q1 are constants here
   const double x0 = A.x[b], y0 = A.y[b], dx0 = A.dx[b], dy0 = A.dy[b];
   const double PI = 3.141592653589793;
   const double wl = A.wl ? A.wl[b] : A.wl_scalar;
@@ -434,127 +416,114 @@ __device__ __forceinline__ void beam_grad_body(const DModel& M, const BGArgs& A,
   X Sxx, Syy, Sxy, Lx, Ly, c0;
   D ox, oy;
   X dlp = cx_<ND>(0.0, 0.0);  // d log pref as a complex dual (its derivative parts are used)
-  if (A.input_plane) {  // gaussian.py:402-409: s = r1 - r1m, S = Q1^-1, L = 2 theta1m
-    Sxx = lift<ND>(Q1i.a);
-    Syy = lift<ND>(Q1i.d);
-    Sxy = lift<ND>(0.5 * (Q1i.b + Q1i.c));
-    Lx = cx_<ND>(2.0 * dx0, 0.0);
-    Ly = cx_<ND>(2.0 * dy0, 0.0);
-    c0 = cx_<ND>(0.0, 0.0);
-    ox = dc_<ND>(x0);
-    oy = dc_<ND>(y0);
-  } else {
-    // central ray and 5x5 ABCD (rows x, y, dx, dy, 1) with the model's
-    // step parameters as directions
-    double x = x0, y = y0, dx = dx0, dy = dy0;
-    DM m[5][5];
+  // central ray and 5x5 ABCD (rows x, y, dx, dy, 1) with the model's
+  // step parameters as directions
+  double x = x0, y = y0, dx = dx0, dy = dy0;
+  D m[5][5];
 #pragma unroll
-    for (int i = 0; i < 5; ++i)
+  for (int i = 0; i < 5; ++i)
 #pragma unroll
-      for (int j = 0; j < 5; ++j) m[i][j] = dc_<NM>(i == j ? 1.0 : 0.0);
-    for (int s = 0; s < M.n; ++s) {
-      const DStep& st = M.s[s];
-      DM a[4];
+    for (int j = 0; j < 5; ++j) m[i][j] = dc_<ND>(i == j ? 1.0 : 0.0);
+  for (int s = 0; s < M.n; ++s) {
+    const DStep& st = M.s[s];
+    D a[4];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) a[j] = dc_<NM>(st.a[j]);
-      if constexpr (STEP) {
+    for (int j = 0; j < 4; ++j) a[j] = dc_<ND>(st.a[j]);
 #pragma unroll
-        for (int d = 0; d < ND; ++d) {
-          if (d >= nd || A.dir_kind[g0 + d] != DIR_STEP || A.dir_step[g0 + d] != s) continue;
-          if (A.dir_a[g0 + d] >= 0) {
-            a[A.dir_a[g0 + d] & 3].d[d] = A.dir_seed[g0 + d];
-          } else {  // rotation angle (radians): d(cos, sin) = (-sin, cos)
-            a[0].d[d] = -st.a[1];
-            a[1].d[d] = st.a[0];
-          }
+    for (int d = 0; d < ND; ++d) {
+      if (d >= nd || A.dir_kind[g0 + d] != DIR_STEP || A.dir_step[g0 + d] != s) continue;
+      if (A.dir_a[g0 + d] >= 0) {
+        a[A.dir_a[g0 + d] & 3].d[d] = A.dir_seed[g0 + d];
+      } else {  // rotation angle (radians): d(cos, sin) = (-sin, cos)
+        a[0].d[d] = -st.a[1];
+        a[1].d[d] = st.a[0];
+      }
+    }
+    switch (st.kind) {
+      case D_FREE:
+        for (int j = 0; j < 5; ++j) {
+          m[0][j] = m[0][j] + a[0] * m[2][j];
+          m[1][j] = m[1][j] + a[0] * m[3][j];
         }
-      }
-      switch (st.kind) {
-        case D_FREE:
-          for (int j = 0; j < 5; ++j) {
-            m[0][j] = m[0][j] + a[0] * m[2][j];
-            m[1][j] = m[1][j] + a[0] * m[3][j];
-          }
-          x += dx * st.a[0];
-          y += dy * st.a[0];
-          break;
-        case D_LENS:  // a[1] = 1/f
-          for (int j = 0; j < 5; ++j) {
-            m[2][j] = m[2][j] - m[0][j] * a[1];
-            m[3][j] = m[3][j] - m[1][j] * a[1];
-          }
-          dx -= x * st.a[1];
-          dy -= y * st.a[1];
-          break;
-        case D_SHIFT:
-          m[0][4] = m[0][4] + a[0]; m[1][4] = m[1][4] + a[1];
-          m[2][4] = m[2][4] + a[2]; m[3][4] = m[3][4] + a[3];
-          x += st.a[0]; y += st.a[1]; dx += st.a[2]; dy += st.a[3];
-          break;
-        case D_BIPRISM: {
-          const double sg = x > 0.0 ? 1.0 : (x < 0.0 ? -1.0 : 0.0);
-          m[2][4] = m[2][4] + sg * a[0];
-          dx += sg * st.a[0];
-        } break;
-        case D_ROTATE:
-          for (int j = 0; j < 5; ++j) {
-            const DM r0 = m[0][j], r1 = m[1][j], r2 = m[2][j], r3 = m[3][j];
-            m[0][j] = a[0] * r0 - a[1] * r1;
-            m[1][j] = a[1] * r0 + a[0] * r1;
-            m[2][j] = a[0] * r2 - a[1] * r3;
-            m[3][j] = a[1] * r2 + a[0] * r3;
-          }
-          {
-            const double c = st.a[0], sn = st.a[1];
-            const double nx = c * x - sn * y, ny = sn * x + c * y;
-            const double ndx = c * dx - sn * dy, ndy = sn * dx + c * dy;
-            x = nx; y = ny; dx = ndx; dy = ndy;
-          }
-          break;
-        default:  // D_NOP (an aberrated lens is rejected on the host)
-          break;
-      }
+        x += dx * st.a[0];
+        y += dy * st.a[0];
+        break;
+      case D_LENS:  // a[1] = 1/f
+        for (int j = 0; j < 5; ++j) {
+          m[2][j] = m[2][j] - m[0][j] * a[1];
+          m[3][j] = m[3][j] - m[1][j] * a[1];
+        }
+        dx -= x * st.a[1];
+        dy -= y * st.a[1];
+        break;
+      case D_SHIFT:
+        m[0][4] = m[0][4] + a[0]; m[1][4] = m[1][4] + a[1];
+        m[2][4] = m[2][4] + a[2]; m[3][4] = m[3][4] + a[3];
+        x += st.a[0]; y += st.a[1]; dx += st.a[2]; dy += st.a[3];
+        break;
+      case D_BIPRISM: {
+        const double sg = x > 0.0 ? 1.0 : (x < 0.0 ? -1.0 : 0.0);
+        m[2][4] = m[2][4] + sg * a[0];
+        dx += sg * st.a[0];
+      } break;
+      case D_ROTATE:
+        for (int j = 0; j < 5; ++j) {
+          const D r0 = m[0][j], r1 = m[1][j], r2 = m[2][j], r3 = m[3][j];
+          m[0][j] = a[0] * r0 - a[1] * r1;
+          m[1][j] = a[1] * r0 + a[0] * r1;
+          m[2][j] = a[0] * r2 - a[1] * r3;
+          m[3][j] = a[1] * r2 + a[0] * r3;
+        }
+        {
+          const double c = st.a[0], sn = st.a[1];
+          const double nx = c * x - sn * y, ny = sn * x + c * y;
+          const double ndx = c * dx - sn * dy, ndy = sn * dx + c * dy;
+          x = nx; y = ny; dx = ndx; dy = ndy;
+        }
+        break;
+      default:  // D_NOP (an aberrated lens is rejected on the host)
+        break;
     }
-    const M2<NM> Am{cx_<NM>(m[0][0]), cx_<NM>(m[0][1]), cx_<NM>(m[1][0]), cx_<NM>(m[1][1])};
-    const M2<NM> Bm{cx_<NM>(m[0][2]), cx_<NM>(m[0][3]), cx_<NM>(m[1][2]), cx_<NM>(m[1][3])};
-    const M2<NM> Cm{cx_<NM>(m[2][0]), cx_<NM>(m[2][1]), cx_<NM>(m[3][0]), cx_<NM>(m[3][1])};
-    const M2<NM> Dm{cx_<NM>(m[2][2]), cx_<NM>(m[2][3]), cx_<NM>(m[3][2]), cx_<NM>(m[3][3])};
-    // Q2^-1 = (A + B Q1^-1)^-1 (C + D Q1^-1)   (gaussian.py:92-96)
-    const M2<NM> denom = Am + Bm * Q1i;
-    const M2<NM> Q2 = inv2(denom) * (Cm + Dm * Q1i);
-    const M2<NM> Binv = nan0(inv2(Bm));
-    const M2<0> Q1 = nan0(inv2(Q1i));
-    const D r2mx = x0 * lift<ND>(m[0][0]) + y0 * lift<ND>(m[0][1]) + dx0 * lift<ND>(m[0][2]) + dy0 * lift<ND>(m[0][3]);
-    const D r2my = x0 * lift<ND>(m[1][0]) + y0 * lift<ND>(m[1][1]) + dx0 * lift<ND>(m[1][2]) + dy0 * lift<ND>(m[1][3]);
-    // pref = amp / sqrt(det): d log pref = -d det / (2 det)
-    if constexpr (STEP) {
-      const Cx<NM> det = denom.a * denom.d - denom.b * denom.c;
-      Cx<NM> dd;
-      dd.re = det.re;
-      dd.im = det.im;
-      dd.re.v = 0.0;  // the quotient below uses only the derivative parts
-      dd.im.v = 0.0;
-      dlp = lift<ND>((-0.5) * (dd / cx_<NM>(det.re.v, det.im.v)));
-    }
-    const M2<NM> ABinv = Am * Binv;
-    const M2<NM> P = Q1 * inv2(Bm * (Am * Q1 + Bm));
-    Sxx = lift<ND>(Q2.a);
-    Syy = lift<ND>(Q2.d);
-    Sxy = lift<ND>(0.5 * (Q2.b + Q2.c));
-    const X bx = x0 * lift<ND>(Binv.a) + y0 * lift<ND>(Binv.c);
-    const X by = x0 * lift<ND>(Binv.b) + y0 * lift<ND>(Binv.d);
-    const X px = lift<ND>(P.a) * cx_<ND>(r2mx) + lift<ND>(P.c) * cx_<ND>(r2my);
-    const X py = lift<ND>(P.b) * cx_<ND>(r2mx) + lift<ND>(P.d) * cx_<ND>(r2my);
-    Lx = 2.0 * (cx_<ND>(lift<ND>(m[2][4])) - bx + px);
-    Ly = 2.0 * (cx_<ND>(lift<ND>(m[3][4])) - by + py);
-    const X q1 = x0 * (x0 * lift<ND>(ABinv.a) + y0 * lift<ND>(ABinv.b)) +
-                 y0 * (x0 * lift<ND>(ABinv.c) + y0 * lift<ND>(ABinv.d));
-    const X q2 = cx_<ND>(r2mx) * (lift<ND>(P.a) * cx_<ND>(r2mx) + lift<ND>(P.b) * cx_<ND>(r2my)) +
-                 cx_<ND>(r2my) * (lift<ND>(P.c) * cx_<ND>(r2mx) + lift<ND>(P.d) * cx_<ND>(r2my));
-    c0 = q1 - q2;
-    ox = lift<ND>(m[0][4]);
-    oy = lift<ND>(m[1][4]);
   }
+  const M2<ND> Am{cx_<ND>(m[0][0]), cx_<ND>(m[0][1]), cx_<ND>(m[1][0]), cx_<ND>(m[1][1])};
+  const M2<ND> Bm{cx_<ND>(m[0][2]), cx_<ND>(m[0][3]), cx_<ND>(m[1][2]), cx_<ND>(m[1][3])};
+  const M2<ND> Cm{cx_<ND>(m[2][0]), cx_<ND>(m[2][1]), cx_<ND>(m[3][0]), cx_<ND>(m[3][1])};
+  const M2<ND> Dm{cx_<ND>(m[2][2]), cx_<ND>(m[2][3]), cx_<ND>(m[3][2]), cx_<ND>(m[3][3])};
+  // Q2^-1 = (A + B Q1^-1)^-1 (C + D Q1^-1)   (gaussian.py:92-96)
+  const M2<ND> denom = Am + Bm * Q1i;
+  const M2<ND> Q2 = inv2(denom) * (Cm + Dm * Q1i);
+  const M2<ND> Binv = nan0(inv2(Bm));
+  const M2<0> Q1 = nan0(inv2(Q1i));
+  const D r2mx = x0 * m[0][0] + y0 * m[0][1] + dx0 * m[0][2] + dy0 * m[0][3];
+  const D r2my = x0 * m[1][0] + y0 * m[1][1] + dx0 * m[1][2] + dy0 * m[1][3];
+  // pref = amp / sqrt(det): d log pref = -d det / (2 det)
+  {
+    const Cx<ND> det = denom.a * denom.d - denom.b * denom.c;
+    Cx<ND> dd;
+    dd.re = det.re;
+    dd.im = det.im;
+    dd.re.v = 0.0;  // the quotient below uses only the derivative parts
+    dd.im.v = 0.0;
+    dlp = (-0.5) * (dd / cx_<ND>(det.re.v, det.im.v));
+  }
+  const M2<ND> ABinv = Am * Binv;
+  const M2<ND> P = Q1 * inv2(Bm * (Am * Q1 + Bm));
+  Sxx = Q2.a;
+  Syy = Q2.d;
+  Sxy = 0.5 * (Q2.b + Q2.c);
+  const X bx = x0 * Binv.a + y0 * Binv.c;
+  const X by = x0 * Binv.b + y0 * Binv.d;
+  const X px = P.a * cx_<ND>(r2mx) + P.c * cx_<ND>(r2my);
+  const X py = P.b * cx_<ND>(r2mx) + P.d * cx_<ND>(r2my);
+  Lx = 2.0 * (cx_<ND>(m[2][4]) - bx + px);
+  Ly = 2.0 * (cx_<ND>(m[3][4]) - by + py);
+  const X q1 = x0 * (x0 * ABinv.a + y0 * ABinv.b) +
+               y0 * (x0 * ABinv.c + y0 * ABinv.d);
+  const X q2 = cx_<ND>(r2mx) * (P.a * cx_<ND>(r2mx) + P.b * cx_<ND>(r2my)) +
+               cx_<ND>(r2my) * (P.c * cx_<ND>(r2mx) + P.d * cx_<ND>(r2my));
+  c0 = q1 - q2;
+  ox = m[0][4];
+  oy = m[1][4];
   // the polynomial in (row, col): s = s0 + row u + col v
   const D s0x = dc_<ND>(A.pm.t[5]) - ox, s0y = dc_<ND>(A.pm.t[2]) - oy;
   const double ux = A.pm.t[3], uy = A.pm.t[0], vx = A.pm.t[4], vy = A.pm.t[1];
@@ -793,21 +762,21 @@ __device__ __forceinline__ void beam_grad_ray(const DModel& M, const BGArgs& A, 
   }
 }
 
-// the body with the narrowest dual width that holds a group of nd <= CAP
+// the step body with the narrowest dual width that holds a group of nd <= CAP
 // directions
-template <bool STEP, int CAP, int NC>
+template <int CAP, int NC>
 __device__ __forceinline__ void beam_grad_fit(const DModel& M, const BGArgs& A, int64_t b, int g0, int nd,
                                               double (&contrib)[NC]) {
   if constexpr (CAP <= 1) {
-    beam_grad_body<1, STEP>(M, A, b, g0, nd, contrib);
+    beam_grad_step<1>(M, A, b, g0, nd, contrib);
   } else if constexpr (CAP == 2) {
-    if (nd <= 1) beam_grad_body<1, STEP>(M, A, b, g0, nd, contrib);
-    else beam_grad_body<2, STEP>(M, A, b, g0, nd, contrib);
+    if (nd <= 1) beam_grad_step<1>(M, A, b, g0, nd, contrib);
+    else beam_grad_step<2>(M, A, b, g0, nd, contrib);
   } else {
-    if (nd <= 1) beam_grad_body<1, STEP>(M, A, b, g0, nd, contrib);
-    else if (nd == 2) beam_grad_body<2, STEP>(M, A, b, g0, nd, contrib);
-    else if (nd == 3 || CAP == 3) beam_grad_body<3, STEP>(M, A, b, g0, nd, contrib);
-    else beam_grad_body<CAP, STEP>(M, A, b, g0, nd, contrib);
+    if (nd <= 1) beam_grad_step<1>(M, A, b, g0, nd, contrib);
+    else if (nd == 2) beam_grad_step<2>(M, A, b, g0, nd, contrib);
+    else if (nd == 3 || CAP == 3) beam_grad_step<3>(M, A, b, g0, nd, contrib);
+    else beam_grad_step<CAP>(M, A, b, g0, nd, contrib);
   }
 }
 
@@ -829,7 +798,7 @@ k_field_beam_grad(const __grid_constant__ DModel M, const __grid_constant__ BGAr
   if (b < A.n) {
     // the dual width that fits the group: fewer directions, shorter chains
     if (step)
-      beam_grad_fit<true, kBGStepDirs>(M, A, b, g0, nd, contrib);
+      beam_grad_fit<kBGStepDirs>(M, A, b, g0, nd, contrib);
     else
       beam_grad_ray(M, A, b, g0, nd, contrib);
   }
