@@ -658,7 +658,9 @@ typedef struct tg_field_grads {
  * Phi a complex quadratic in the pixel indices; the call reduces conj(grad) *
  * field against the six monomials of Phi per beam (one pass over beams x
  * pixels) and applies the chain rule from Phi's coefficients to the beam and
- * model parameters in float64 forward mode.  An aberrated lens in the model
+ * model parameters in float64 (forward-mode dual numbers for the model's step
+ * parameters, closed-form derivatives for the central ray, whose ABCD algebra
+ * does not depend on it).  An aberrated lens in the model
  * returns TG_ERR_UNSUPPORTED.  workspace: device, tg_field_vjp_workspace(n,
  * h, w) bytes, 256-byte aligned.  Deterministic (fixed-order reductions).
  */
