@@ -692,13 +692,18 @@ static int dir_blocks_per_sm() {
   }
   return cached;
 }
-// Beam chunks (blockIdx.y) for the direct sum: about kDirWaves waves of
-// resident blocks, chunk sizes not rounded to whole shared-memory batches so
-// every block carries the same beam count.  Measured on 512^2 (ms, 16,384 /
-// 4,096 astigmatic beams): one wave 2.31 / 0.59, two 1.94 / 0.50, three
-// 1.91 / 0.50, four 1.88 / 0.50; the earlier 64-beam-rounded chunks for ~4
-// blocks a SM 1.99 / 0.56.
+// Beam chunks (blockIdx.y) for the direct sum: kDirWaves waves of resident
+// blocks, more (up to kDirWavesMax) while every chunk keeps kDirChunkBeams
+// beams; chunk sizes are not rounded to whole shared-memory batches.  Blocks
+// differ in cost (beams far from a tile skip most strips), so finer chunks
+// balance better once they are long enough.  Measured on 512^2 (ms, 16,384
+// astigmatic / 16,384 / 4,096 / 1,024 beams): one wave 2.31 / 2.12 / 0.59 / 0.16,
+// two 1.94 / 1.95 / 0.50 / 0.14, three 1.91 / 1.91 / 0.50 / 0.15, four
+// 1.88 / 1.93 / 0.50 / 0.15, six 1.85 / 1.88 / 0.51 / 0.17; the earlier
+// 64-beam-rounded chunks for ~4 blocks a SM 1.99 / 2.02 / 0.56 / 0.15.
 constexpr int kDirWaves = 3;
+constexpr int kDirWavesMax = 6;
+constexpr int64_t kDirChunkBeams = 256;
 
 static FieldLayout field_layout(int64_t n, int h, int w, int method) {
   FieldLayout L;
@@ -710,7 +715,10 @@ static FieldLayout field_layout(int64_t n, int h, int w, int method) {
   const int sms = sm_count_field();
   if (method == TG_FIELD_DIRECT) {
     int tiles = ((h + kDirTileRows - 1) / kDirTileRows) * ((w + kDirStrips * kDirL - 1) / (kDirStrips * kDirL));
-    int want = (int)(((int64_t)sms * dir_blocks_per_sm() * kDirWaves + tiles - 1) / tiles);
+    const int64_t res = (int64_t)sms * dir_blocks_per_sm();
+    const int64_t lo = (res * kDirWaves + tiles - 1) / tiles, hi = (res * kDirWavesMax + tiles - 1) / tiles;
+    const int64_t by_beams = n / kDirChunkBeams;
+    int want = (int)(by_beams < lo ? lo : (by_beams > hi ? hi : by_beams));
     int64_t maxc = (n + 15) / 16;  // at least 16 beams a chunk
     L.chunks = (int)(want < maxc ? want : maxc);
     if (L.chunks < 1) L.chunks = 1;
