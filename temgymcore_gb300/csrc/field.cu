@@ -529,7 +529,7 @@ namespace tg {
 // + threadIdx.x the beam, so there is no index division and the line loop
 // needs no bound.  Consecutive threads take consecutive beams: each plane
 // store of a warp is one contiguous 64-byte run.
-constexpr int kOpLines = 16;
+constexpr int kOpLines = 32;  // measured (16,384 beams, 512^2, whole evaluation): 8 lines 0.108 ms, 16 0.0998, 32 0.0982, 64 0.0977
 
 __global__ void __launch_bounds__(256) k_field_operands(const __grid_constant__ OperandArgs A) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
